@@ -1,0 +1,339 @@
+#!/usr/bin/env python3
+"""Benchmark of the lattice-Boltzmann timestep on GB300.
+
+Workload (one "step" = one D3Q19 two-component Shan-Chen timestep over the
+whole lattice): the droplet-in-channel configuration, 256x128x128 sites,
+bounce-back walls on the z = 0 and z = 127 planes, periodic in x and y, a red
+sphere of radius 24 (rho_red 1.0 / rho_blue 0.05) in a blue bath (0.05 / 1.0),
+body force 1e-6 along x, tau = 1, g = 3.6, psi = 1 - exp(-rho), BDist2
+equilibrium.  The headline form is FP64 (the reference's arithmetic); FP32
+and FP16-offset-storage forms of the same workload are reported beside it.
+
+Prints one JSON line (rank 0).  ``--impl reference`` times the reference's
+algorithm on the host cores instead (the CPU oracle, all threads).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "MLUPS (D3Q19 2-comp Shan-Chen timestep)"
+UNIT = "MLUPS"
+WORKLOAD = "droplet-channel 256x128x128 D3Q19 two-component Shan-Chen, walls z=0/127, body force 1e-6"
+LATTICE = (256, 128, 128)
+
+
+def workload_params(n=LATTICE, eq="BDist2"):
+    from dlbc_gb300 import params
+    lines = [
+        "[lattice]", f"gn = [{n[0]}, {n[1]}, {n[2]}]",
+        "[lb]", "components = 2", 'fieldNames = ["red", "blue"]', "tau = [1.0, 1.0]",
+        f"eqdist.eqDistForm = {eq}",
+        "force.enableShanChen = true", "force.gcc = [[0.0, 3.6], [3.6, 0.0]]",
+        "force.psiForm = Exponential", "force.globalAcc = [1e-6, 0.0, 0.0]",
+        "init.fluidInit = [EqDistSphere, EqDistSphere]",
+        "init.fluidDensities = [[1.0, 0.05], [0.05, 1.0]]",
+        "init.initRadius = 24.0", "init.interfaceThickness = 0.0",
+        "mask.maskInit = Walls",
+        "mask.dimensionHasWall = [[false, false], [false, false], [true, true]]",
+        "mask.wallThickness = 1",
+    ]
+    return params.LBParams.from_dict(params.parse_lines(lines), "d3q19")
+
+
+def bytes_per_site(precision: int, walls: bool = True) -> int:
+    """Algorithmic bytes per site-update: every population read once and
+    written once (2 components x 19), plus the 1-byte mask when walls exist."""
+    s = {0: 8, 1: 4, 2: 2}[precision]
+    return 2 * 2 * 19 * s + (1 if walls else 0)
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(self.device)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        self.out = ""
+        if self.proc is not None:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+        return False
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in (self.out or "").splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": mx, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def time_form(p, fluids, mask, precision, steps, warmup, device, torch):
+    """Device-timed steps of one form: (ms/step, collide-kernel ms/launch,
+    density/psi-kernel ms/launch, kernel launches in the timed region)."""
+    from dlbc_gb300 import lbgpu
+    g = lbgpu.GPULattice(p, precision=precision, device=device)
+    g.upload(fluids, mask)
+    stream = torch.cuda.Stream(device=device)
+    g.set_stream(stream.cuda_stream)
+    g.step(warmup)
+    g.synchronize()
+    g.profile(True)
+    start = torch.cuda.Event(enable_timing=True)
+    stop = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize(device)
+    n0 = g.launch_count
+    start.record(stream)
+    g.step(steps)
+    stop.record(stream)
+    stop.synchronize()
+    torch.cuda.synchronize(device)
+    ms = start.elapsed_time(stop)
+    launches = g.launch_count - n0
+    k1_ms, k1_n = g.kernel_time(0)
+    k2_ms, k2_n = g.kernel_time(1)
+    g.profile(False)
+    g.close()
+    return ms / steps, k2_ms / max(k2_n, 1), k1_ms / max(k1_n, 1), launches
+
+
+def roofline(precision, sites, kernel_ms, peak, peak_kind, traffic=None):
+    alg = bytes_per_site(precision) * sites
+    achieved = alg / (kernel_ms * 1e-3) / 1e9
+    return {"bound": "hbm", "kernel": "k_collide", "achieved": round(achieved, 1), "peak": peak,
+            "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
+            "traffic": traffic, "algorithmic_bytes": alg}
+
+
+def read_traffic(form):
+    """DRAM bytes per k_collide launch from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "traffic_droplet_channel.json")
+    try:
+        with open(path) as fh:
+            return json.load(fh).get(form)
+    except Exception:
+        return None
+
+
+def cpu_baseline(p, budget_s=12.0, threads=None):
+    """The CPU oracle on the host cores, on a bounded number of steps of
+    the same lattice."""
+    from oracle import oracle as orc
+    threads = threads or os.cpu_count() or 1
+    o = orc.Oracle(p, exp_mode=1, threads=threads)
+    t0 = time.perf_counter()
+    o.run(1)
+    t1 = time.perf_counter() - t0
+    steps = max(1, min(50, int(budget_s / max(t1, 1e-6))))
+    t0 = time.perf_counter()
+    o.run(steps)
+    dt = time.perf_counter() - t0
+    sites = p.gn[0] * p.gn[1] * p.gn[2]
+    return {"value": round(sites * steps / dt / 1e6, 3), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{steps} timesteps of the full {p.gn[0]}x{p.gn[1]}x{p.gn[2]} lattice after 1 untimed "
+                      f"step (FP64 oracle, OpenMP over x-slabs)"}
+
+
+def run_reference(args):
+    """--impl reference: the reference's CPU algorithm (the oracle) on all host threads."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    from oracle import oracle as orc
+    p = workload_params()
+    threads = os.cpu_count() or 1
+    o = orc.Oracle(p, exp_mode=1, threads=threads)
+    o.run(max(0, min(args.warmup, 3)))
+    steps = max(1, min(args.steps, 20))
+    t0 = time.perf_counter()
+    o.run(steps)
+    dt = time.perf_counter() - t0
+    sites = LATTICE[0] * LATTICE[1] * LATTICE[2]
+    v = sites * steps / dt / 1e6
+    line = {
+        "metric": METRIC, "value": round(v, 3), "unit": UNIT, "n_gpus": args.gpus, "steps": steps,
+        "warmup": min(args.warmup, 3), "ms_per_step": round(dt / steps * 1e3, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "lattice": list(LATTICE), "form": "fp64", "eq_form": "BDist2"},
+        "impl": "reference",
+        "cpu_baseline": {"value": round(v, 3), "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{steps} timesteps of the full lattice (the reference's D/MPI build cannot "
+                                   f"be compiled: no D toolchain and an empty 'unstandard' submodule)"},
+        "e2e": {"value": round(v, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="native", choices=["native", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-forms", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=10)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import numpy as np
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    device = local
+
+    from dlbc_gb300 import build, init, lbgpu
+    build.build()
+    p = workload_params()
+    fluids, mask = init.init_fields(p)
+    sites = LATTICE[0] * LATTICE[1] * LATTICE[2]
+    peak, peak_kind = measured_peaks()
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize(device)
+
+    # ---- headline: FP64, inputs resident in HBM
+    barrier()
+    with ClockSampler(device) as clk:
+        ms_step, k2_ms, k1_ms, launches = time_form(p, fluids, mask, lbgpu.FP64, args.steps, args.warmup, device,
+                                                    torch)
+    barrier()
+    t_local = torch.tensor([ms_step], dtype=torch.float64, device=f"cuda:{device}")
+    if dist is not None:
+        dist.all_reduce(t_local, op=dist.ReduceOp.MAX)
+    ms_max = float(t_local.item())
+    value = world * sites / (ms_max * 1e-3) / 1e6
+
+    # ---- end to end through the C ABI with pinned host buffers:
+    # per step, upload the state (populations + mask), one timestep, download
+    g = lbgpu.GPULattice(p, precision=lbgpu.FP64, device=device)
+    hb = [torch.from_numpy(f).pin_memory() for f in fluids]
+    hm = torch.from_numpy(mask).pin_memory()
+    g.upload(hb, hm)
+    for _ in range(2):
+        g.step(1)
+        g.download(hb)
+        g.upload(hb, hm)
+    barrier()
+    n_e2e = args.e2e_steps
+    t0 = time.perf_counter()
+    for _ in range(n_e2e):
+        g.upload(hb, hm)
+        g.step(1)
+        g.download(hb)
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    e2e_t = torch.tensor([e2e_s], dtype=torch.float64, device=f"cuda:{device}")
+    if dist is not None:
+        dist.all_reduce(e2e_t, op=dist.ReduceOp.MAX)
+    e2e_value = world * sites * n_e2e / float(e2e_t.item()) / 1e6
+    h2d = sum(int(x.numel()) * 8 for x in hb) + int(hm.numel()) * 4
+    d2h = sum(int(x.numel()) * 8 for x in hb)
+    g.close()
+    del hb, hm
+
+    # ---- the reduced-precision forms of the same workload
+    forms = {}
+    if not args.no_forms:
+        for name, prec in (("fp32", lbgpu.FP32), ("fp16", lbgpu.FP16)):
+            f_ms, f_k2, f_k1, _ = time_form(p, fluids, mask, prec, args.steps, args.warmup, device, torch)
+            forms[name] = {"value": round(world * sites / (f_ms * 1e-3) / 1e6, 1),
+                           "ms_per_step": round(f_ms, 4),
+                           "k_density_psi_ms": round(f_k1, 4), "k_collide_ms": round(f_k2, 4),
+                           "roofline": roofline(prec, sites, f_k2, peak, peak_kind, read_traffic(name)),
+                           "step_roofline_frac": round(bytes_per_site(prec) * sites / (f_ms * 1e-3) / 1e9 / peak,
+                                                       4)}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(p)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms_max, 4), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "lattice": list(LATTICE), "form": "fp64", "eq_form": "BDist2",
+                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                       "l2": "inputs larger than L2 (FP64 populations 2x2.55 GB)"},
+            "roofline": roofline(lbgpu.FP64, sites, k2_ms, peak, peak_kind, read_traffic("fp64")),
+            "kernels_ms": {"k_density_psi": round(k1_ms, 4), "k_collide": round(k2_ms, 4)},
+            "cpu_baseline": cpu,
+            "e2e": {"value": round(e2e_value, 2), "unit": UNIT, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h,
+                    "call": "lbgpu_upload(pinned AoS haloed fluids + mask) -> lbgpu_step(1) -> lbgpu_download"},
+            "gpu_launches": launches,
+            "clocks": clk.summary(),
+            "forms": forms,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

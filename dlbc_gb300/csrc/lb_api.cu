@@ -1,0 +1,855 @@
+// C-ABI of the GB300 lattice-Boltzmann timestep (declared in include/lbgpu.h).
+//
+// Device layout (SoA, physical sites only, no halo):
+//   populations  f[buf][c][q][site], two buffers (streaming is pull: read one,
+//                write the other, swap), site = (x*ny + y)*nz + z;
+//   mask         uint8 [site], only when the lattice has a solid site;
+//   rho, psi     [c][site] scratch for the timestep's psi stencil;
+//   force        [c][site][d] doubles, only while force recording is on.
+// Host transfers go through a bounded device staging buffer holding whole
+// haloed x-planes of the reference's AoS layout.
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "../../include/lbgpu.h"
+#include "lb_launch.h"
+
+using lbk::StepParams;
+
+namespace {
+
+constexpr int kHalo = 2;
+constexpr size_t kStagingBytes = size_t(256) << 20;
+
+thread_local std::string g_create_error;
+
+size_t storage_size(int precision) { return precision == LBGPU_FP64 ? 8 : precision == LBGPU_FP32 ? 4 : 2; }
+size_t arith_size(int precision) { return precision == LBGPU_FP64 ? 8 : 4; }
+
+}  // namespace
+
+struct lbgpu_handle {
+  lbgpu_config cfg;
+  int d = 3, Q = 19, C = 2;
+  int nx = 1, ny = 1, nz = 1;       // kernel extents (nz = 1 for D2Q9)
+  int nxh = 1, nyh = 1, nzh = 1;    // haloed host extents
+  int hz = kHalo;                   // halo in z (0 for D2Q9)
+  int64_t n = 0;
+  cudaStream_t stream = nullptr;       // where work is queued
+  cudaStream_t own_stream = nullptr;   // created with the handle
+  void* f[2] = {nullptr, nullptr};
+  int cur = 0;
+  uint8_t* mask = nullptr;
+  void* rho = nullptr;
+  void* psi = nullptr;
+  double* force = nullptr;
+  int record_force = 0;
+  int force_valid = 0;
+  double* staging = nullptr;
+  size_t staging_bytes = 0;
+  double* moments = nullptr;        // device scratch for lbgpu_moments / lbgpu_reduce
+  size_t moments_bytes = 0;
+  StepParams P{};
+  bool uploaded = false;
+  // per-kernel event timing (lbgpu_profile)
+  bool profiling = false;
+  std::vector<lbk::StepEvents> ev_pending, ev_pool;
+  double kernel_ms[2] = {0.0, 0.0};
+  int64_t kernel_n[2] = {0, 0};
+  int64_t launches = 0;
+  int64_t device_bytes = 0;
+  std::string err;
+
+  int fail(int code, const std::string& msg) {
+    err = msg;
+    return code;
+  }
+  int cuda_fail(cudaError_t e, const char* what) {
+    err = std::string(what) + ": " + cudaGetErrorString(e);
+    return LBGPU_E_CUDA;
+  }
+};
+
+namespace {
+
+// --------------------------------------------------------------------------
+// transfer kernels
+// --------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ T to_storage(double v, int q, int c, const StepParams& P, int Q);
+
+template <>
+__device__ __forceinline__ double to_storage<double>(double v, int, int, const StepParams&, int) {
+  return v;
+}
+template <>
+__device__ __forceinline__ float to_storage<float>(double v, int, int, const StepParams&, int) {
+  return float(v);
+}
+__device__ __forceinline__ float wq(int Q, int q) {
+  return Q == 19 ? lbk::weight<19, float>(q) : lbk::weight<9, float>(q);
+}
+template <>
+__device__ __forceinline__ __half to_storage<__half>(double v, int q, int c, const StepParams& P, int Q) {
+  return __float2half_rn((float(v) - wq(Q, q) * P.rho0[c]) * P.inv_scale[c]);
+}
+
+template <typename T>
+__device__ __forceinline__ double from_storage(T v, int q, int c, const StepParams& P, int Q);
+template <>
+__device__ __forceinline__ double from_storage<double>(double v, int, int, const StepParams&, int) {
+  return v;
+}
+template <>
+__device__ __forceinline__ double from_storage<float>(float v, int, int, const StepParams&, int) {
+  return double(v);
+}
+template <>
+__device__ __forceinline__ double from_storage<__half>(__half v, int q, int c, const StepParams& P, int Q) {
+  return double(wq(Q, q) * P.rho0[c] + P.scale[c] * __half2float(v));
+}
+
+struct Geo {
+  int nx, ny, nz, nxh, nyh, nzh, hz, Q;
+  int64_t n;
+};
+
+// AoS haloed staging (haloed x-planes [xh0, xh0 + nplanes)) -> SoA physical
+template <typename T>
+__global__ void k_upload(const double* __restrict__ stage, T* __restrict__ f, int c, int xh0, int nplanes, Geo g,
+                         StepParams P) {
+  const int64_t per_plane = int64_t(g.ny) * g.nz;
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= per_plane * nplanes) return;
+  const int pl = int(i / per_plane);
+  const int64_t r = i - int64_t(pl) * per_plane;
+  const int y = int(r / g.nz), z = int(r - int64_t(y) * g.nz);
+  const int xh = xh0 + pl;
+  const int x = xh - kHalo;
+  if (x < 0 || x >= g.nx) return;
+  const double* src = stage + ((int64_t(pl) * g.nyh + (y + kHalo)) * g.nzh + (z + g.hz)) * g.Q;
+  const int64_t site = (int64_t(x) * g.ny + y) * g.nz + z;
+  T* fc = f + int64_t(c) * g.Q * g.n;
+  for (int q = 0; q < g.Q; ++q) fc[int64_t(q) * g.n + site] = to_storage<T>(src[q], q, c, P, g.Q);
+}
+
+// SoA physical -> AoS haloed staging (halo sites get periodic images)
+template <typename T>
+__global__ void k_download(double* __restrict__ stage, const T* __restrict__ f, int c, int xh0, int nplanes, Geo g,
+                           StepParams P) {
+  const int64_t per_plane = int64_t(g.nyh) * g.nzh;
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= per_plane * nplanes) return;
+  const int pl = int(i / per_plane);
+  const int64_t r = i - int64_t(pl) * per_plane;
+  const int yh = int(r / g.nzh), zh = int(r - int64_t(yh) * g.nzh);
+  const int x = ((xh0 + pl - kHalo) % g.nx + g.nx) % g.nx;
+  const int y = ((yh - kHalo) % g.ny + g.ny) % g.ny;
+  const int z = ((zh - g.hz) % g.nz + g.nz) % g.nz;
+  const int64_t site = (int64_t(x) * g.ny + y) * g.nz + z;
+  double* dst = stage + i * g.Q;
+  const T* fc = f + int64_t(c) * g.Q * g.n;
+  for (int q = 0; q < g.Q; ++q) dst[q] = from_storage<T>(fc[int64_t(q) * g.n + site], q, c, P, g.Q);
+}
+
+__global__ void k_upload_mask(const int32_t* __restrict__ stage_mask, uint8_t* __restrict__ mask, int xh0,
+                              int nplanes, Geo g, int* __restrict__ nsolid) {
+  const int64_t per_plane = int64_t(g.ny) * g.nz;
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= per_plane * nplanes) return;
+  const int pl = int(i / per_plane);
+  const int64_t r = i - int64_t(pl) * per_plane;
+  const int y = int(r / g.nz), z = int(r - int64_t(y) * g.nz);
+  const int x = xh0 + pl - kHalo;
+  if (x < 0 || x >= g.nx) return;
+  const int v = stage_mask[(int64_t(pl) * g.nyh + (y + kHalo)) * g.nzh + (z + g.hz)];
+  mask[(int64_t(x) * g.ny + y) * g.nz + z] = v != 0;
+  if (v != 0) atomicAdd(nsolid, 1);
+}
+
+// moments in double: density (pairwise sum), raw velocity, colour
+template <typename T, int Q>
+__global__ void k_moments(const T* __restrict__ f, const uint8_t* __restrict__ mask, int C, Geo g, StepParams P,
+                          double* __restrict__ den_out, double* __restrict__ vel_out, double* __restrict__ col_out) {
+  constexpr int D = lbk::Conn<Q>::D;
+  const int64_t s = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (s >= g.n) return;
+  const bool solid = mask && mask[s];
+  double den[2] = {0.0, 0.0};
+  for (int c = 0; c < C; ++c) {
+    double pop[Q];
+    const T* fc = f + int64_t(c) * Q * g.n;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) pop[q] = from_storage<T>(fc[int64_t(q) * g.n + s], q, c, P, Q);
+    den[c] = lbk::density<Q, double>(pop);
+    if (den_out) den_out[int64_t(c) * g.n + s] = den[c];
+    if (vel_out) {
+      const double recip = 1.0 / den[c];
+#pragma unroll
+      for (int vd = 0; vd < D; ++vd)
+        vel_out[(int64_t(c) * g.n + s) * D + vd] = solid ? 0.0 : lbk::moment<Q, double>(pop, vd) * recip;
+    }
+  }
+  if (col_out && C > 1) col_out[s] = solid ? 0.0 : den[0] - den[1];
+}
+
+// deterministic reduction: per-block sums in a fixed tree order, then one
+// block sums the partials in block order
+constexpr int kRedThreads = 256;
+
+template <typename T, int Q>
+__global__ void k_reduce_partial(const T* __restrict__ f, const uint8_t* __restrict__ mask, int C, Geo g,
+                                 StepParams P, int64_t per_block, double* __restrict__ partial) {
+  constexpr int D = lbk::Conn<Q>::D;
+  constexpr int NV = 2 * (1 + 3);
+  __shared__ double sh[kRedThreads][NV];
+  double acc[NV];
+  for (int k = 0; k < NV; ++k) acc[k] = 0.0;
+  const int64_t s0 = int64_t(blockIdx.x) * per_block;
+  const int64_t s1 = min(g.n, s0 + per_block);
+  for (int64_t s = s0 + threadIdx.x; s < s1; s += blockDim.x) {
+    if (mask && mask[s]) continue;
+    for (int c = 0; c < C; ++c) {
+      double pop[Q];
+      const T* fc = f + int64_t(c) * Q * g.n;
+#pragma unroll
+      for (int q = 0; q < Q; ++q) pop[q] = from_storage<T>(fc[int64_t(q) * g.n + s], q, c, P, Q);
+      acc[c * 4] += lbk::density<Q, double>(pop);
+#pragma unroll
+      for (int vd = 0; vd < D; ++vd) acc[c * 4 + 1 + vd] += lbk::moment<Q, double>(pop, vd);
+    }
+  }
+  for (int k = 0; k < NV; ++k) sh[threadIdx.x][k] = acc[k];
+  __syncthreads();
+  for (int w = kRedThreads / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w)
+      for (int k = 0; k < NV; ++k) sh[threadIdx.x][k] += sh[threadIdx.x + w][k];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    for (int k = 0; k < NV; ++k) partial[int64_t(blockIdx.x) * NV + k] = sh[0][k];
+}
+
+__global__ void k_reduce_final(const double* __restrict__ partial, int nblocks, double* __restrict__ out) {
+  constexpr int NV = 8;
+  if (threadIdx.x < NV) {
+    double s = 0.0;
+    for (int b = 0; b < nblocks; ++b) s += partial[int64_t(b) * NV + threadIdx.x];
+    out[threadIdx.x] = s;
+  }
+}
+
+int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+Geo geo_of(const lbgpu_handle* h) {
+  Geo g;
+  g.nx = h->nx;
+  g.ny = h->ny;
+  g.nz = h->nz;
+  g.nxh = h->nxh;
+  g.nyh = h->nyh;
+  g.nzh = h->nzh;
+  g.hz = h->hz;
+  g.Q = h->Q;
+  g.n = h->n;
+  return g;
+}
+
+template <typename T>
+cudaError_t launch_upload(lbgpu_handle* h, int c, int xh0, int np) {
+  const Geo g = geo_of(h);
+  const int64_t work = int64_t(g.ny) * g.nz * np;
+  k_upload<T><<<unsigned(ceil_div(work, 256)), 256, 0, h->stream>>>(h->staging, static_cast<T*>(h->f[h->cur]), c,
+                                                                     xh0, np, g, h->P);
+  h->launches++;
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_download(lbgpu_handle* h, int c, int xh0, int np) {
+  const Geo g = geo_of(h);
+  const int64_t work = int64_t(g.nyh) * g.nzh * np;
+  k_download<T><<<unsigned(ceil_div(work, 256)), 256, 0, h->stream>>>(
+      h->staging, static_cast<const T*>(h->f[h->cur]), c, xh0, np, g, h->P);
+  h->launches++;
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_moments(lbgpu_handle* h, double* den, double* vel, double* col) {
+  const Geo g = geo_of(h);
+  const unsigned blocks = unsigned(ceil_div(g.n, 128));
+  if (h->Q == 19)
+    k_moments<T, 19><<<blocks, 128, 0, h->stream>>>(static_cast<const T*>(h->f[h->cur]), h->mask, h->C, g, h->P,
+                                                     den, vel, col);
+  else
+    k_moments<T, 9><<<blocks, 128, 0, h->stream>>>(static_cast<const T*>(h->f[h->cur]), h->mask, h->C, g, h->P,
+                                                    den, vel, col);
+  h->launches++;
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_reduce(lbgpu_handle* h, double* partial, int nblocks, int64_t per_block, double* out) {
+  const Geo g = geo_of(h);
+  if (h->Q == 19)
+    k_reduce_partial<T, 19><<<nblocks, kRedThreads, 0, h->stream>>>(static_cast<const T*>(h->f[h->cur]), h->mask,
+                                                                     h->C, g, h->P, per_block, partial);
+  else
+    k_reduce_partial<T, 9><<<nblocks, kRedThreads, 0, h->stream>>>(static_cast<const T*>(h->f[h->cur]), h->mask,
+                                                                    h->C, g, h->P, per_block, partial);
+  k_reduce_final<<<1, 32, 0, h->stream>>>(partial, nblocks, out);
+  h->launches += 2;
+  return cudaGetLastError();
+}
+
+int validate(const lbgpu_config* c, std::string* why) {
+  if (!c) {
+    *why = "null config";
+    return LBGPU_E_INVALID;
+  }
+  if (!((c->d == 3 && c->q == 19) || (c->d == 2 && c->q == 9))) {
+    *why = "only D3Q19 and D2Q9 are supported";
+    return LBGPU_E_INVALID;
+  }
+  if (c->components < 1 || c->components > LBGPU_MAX_COMPONENTS) {
+    *why = "components must be 1 or 2";
+    return LBGPU_E_INVALID;
+  }
+  for (int i = 0; i < c->d; ++i)
+    if (c->gn[i] < 2) {
+      *why = "every lattice extent must be >= 2 (the halo of 2 holds periodic images)";
+      return LBGPU_E_INVALID;
+    }
+  int64_t n = 1;
+  for (int i = 0; i < c->d; ++i) n *= c->gn[i];
+  if (n > (int64_t(1) << 31)) {
+    *why = "lattice larger than 2^31 sites";
+    return LBGPU_E_INVALID;
+  }
+  if (c->precision < LBGPU_FP64 || c->precision > LBGPU_FP16) {
+    *why = "unknown precision";
+    return LBGPU_E_INVALID;
+  }
+  if (c->eq_form < 0 || c->eq_form > 2 || c->psi_form < 0 || c->psi_form > 1) {
+    *why = "unknown eqDistForm or psiForm";
+    return LBGPU_E_INVALID;
+  }
+  for (int i = 0; i < c->components; ++i)
+    if (!(c->tau[i] > 0.0)) {
+      *why = "tau must be positive";
+      return LBGPU_E_INVALID;
+    }
+  return LBGPU_OK;
+}
+
+// accumulate the elapsed times of all recorded steps (synchronizes)
+cudaError_t fold_kernel_times(lbgpu_handle* h) {
+  if (h->ev_pending.empty()) return cudaSuccess;
+  cudaError_t e = cudaStreamSynchronize(h->stream);
+  if (e != cudaSuccess) return e;
+  for (auto& se : h->ev_pending) {
+    float a = 0.f, b = 0.f;
+    cudaEventElapsedTime(&a, se.ev[0], se.ev[1]);
+    cudaEventElapsedTime(&b, se.ev[1], se.ev[2]);
+    h->kernel_ms[0] += a;
+    h->kernel_ms[1] += b;
+    h->kernel_n[0]++;
+    h->kernel_n[1]++;
+    h->ev_pool.push_back(se);
+  }
+  h->ev_pending.clear();
+  return cudaSuccess;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t lbgpu_abi_version(void) { return LBGPU_ABI_VERSION; }
+
+const char* lbgpu_last_error(const lbgpu_handle* h) { return h ? h->err.c_str() : g_create_error.c_str(); }
+
+int lbgpu_create(const lbgpu_config* cfg, lbgpu_handle** out) {
+  if (!out) return LBGPU_E_INVALID;
+  *out = nullptr;
+  std::string why;
+  int rc = validate(cfg, &why);
+  if (rc) {
+    g_create_error = why;
+    return rc;
+  }
+  cudaError_t e = cudaSetDevice(cfg->device);
+  if (e != cudaSuccess) {
+    g_create_error = std::string("cudaSetDevice: ") + cudaGetErrorString(e);
+    return LBGPU_E_CUDA;
+  }
+  lbgpu_handle* h = new lbgpu_handle;
+  h->cfg = *cfg;
+  h->d = cfg->d;
+  h->Q = cfg->q;
+  h->C = cfg->components;
+  h->nx = cfg->gn[0];
+  h->ny = cfg->gn[1];
+  h->nz = cfg->d == 3 ? cfg->gn[2] : 1;
+  h->hz = cfg->d == 3 ? kHalo : 0;
+  h->nxh = h->nx + 2 * kHalo;
+  h->nyh = h->ny + 2 * kHalo;
+  h->nzh = h->nz + 2 * h->hz;
+  h->n = int64_t(h->nx) * h->ny * h->nz;
+
+  StepParams& P = h->P;
+  P.nx = h->nx;
+  P.ny = h->ny;
+  P.nz = h->nz;
+  P.n = h->n;
+  P.shan_chen = cfg->shan_chen;
+  P.psi_form = cfg->psi_form;
+  P.eq_form = cfg->eq_form;
+  P.record_force = 0;
+  for (int c = 0; c < 2; ++c) {
+    const double tau = c < h->C ? cfg->tau[c] : 1.0;
+    P.tau[c] = tau;
+    P.omega[c] = 1.0 / tau;               // collision.d:199
+    P.one_minus_omega[c] = 1.0 - P.omega[c];
+    P.gwc[c] = c < h->C ? cfg->gwc[c] : 0.0;
+    for (int c2 = 0; c2 < 2; ++c2) P.gcc[c][c2] = (c < h->C && c2 < h->C) ? cfg->gcc[c][c2] : 0.0;
+    P.rho0[c] = 0.f;
+    P.scale[c] = 1.f;
+    P.inv_scale[c] = 1.f;
+  }
+  for (int i = 0; i < 3; ++i) P.acc[i] = i < cfg->d ? cfg->global_acc[i] : 0.0;
+
+  e = cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking);
+  h->stream = h->own_stream;
+  if (e != cudaSuccess) {
+    g_create_error = std::string("cudaStreamCreate: ") + cudaGetErrorString(e);
+    delete h;
+    return LBGPU_E_CUDA;
+  }
+  const size_t fbytes = size_t(h->C) * h->Q * h->n * storage_size(cfg->precision);
+  const size_t sbytes = size_t(h->C) * h->n * arith_size(cfg->precision);
+  const size_t plane_bytes = size_t(h->nyh) * h->nzh * h->Q * sizeof(double);
+  h->staging_bytes = std::max(plane_bytes, std::min(kStagingBytes, plane_bytes * h->nxh));
+  h->moments_bytes = size_t(h->C) * h->n * sizeof(double);
+  void* ptrs[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  const size_t sizes[6] = {fbytes, fbytes, sbytes, sbytes, h->staging_bytes, h->moments_bytes};
+  for (int i = 0; i < 6; ++i) {
+    e = cudaMalloc(&ptrs[i], sizes[i]);
+    if (e != cudaSuccess) {
+      for (int j = 0; j < i; ++j) cudaFree(ptrs[j]);
+      cudaStreamDestroy(h->own_stream);
+      g_create_error = std::string("device allocation of ") + std::to_string(sizes[i]) + " bytes failed: " +
+                       cudaGetErrorString(e);
+      cudaGetLastError();
+      delete h;
+      return LBGPU_E_NOMEM;
+    }
+    h->device_bytes += int64_t(sizes[i]);
+  }
+  h->f[0] = ptrs[0];
+  h->f[1] = ptrs[1];
+  h->rho = ptrs[2];
+  h->psi = ptrs[3];
+  h->staging = static_cast<double*>(ptrs[4]);
+  h->moments = static_cast<double*>(ptrs[5]);
+  *out = h;
+  return LBGPU_OK;
+}
+
+void lbgpu_destroy(lbgpu_handle* h) {
+  if (!h) return;
+  cudaSetDevice(h->cfg.device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  cudaFree(h->f[0]);
+  cudaFree(h->f[1]);
+  cudaFree(h->rho);
+  cudaFree(h->psi);
+  cudaFree(h->staging);
+  cudaFree(h->moments);
+  if (h->mask) cudaFree(h->mask);
+  if (h->force) cudaFree(h->force);
+  for (auto& e : h->ev_pending)
+    for (auto ev : e.ev) cudaEventDestroy(ev);
+  for (auto& e : h->ev_pool)
+    for (auto ev : e.ev) cudaEventDestroy(ev);
+  if (h->own_stream) cudaStreamDestroy(h->own_stream);
+  delete h;
+}
+
+int lbgpu_upload(lbgpu_handle* h, const double* const* fluids, const int32_t* mask) {
+  if (!h || !fluids) return LBGPU_E_INVALID;
+  for (int c = 0; c < h->C; ++c)
+    if (!fluids[c]) return h->fail(LBGPU_E_INVALID, "null fluid array");
+  cudaSetDevice(h->cfg.device);
+  cudaError_t e;
+  const size_t plane_vals = size_t(h->nyh) * h->nzh * h->Q;
+  const int planes_per_chunk = int(std::max<size_t>(1, h->staging_bytes / (plane_vals * sizeof(double))));
+
+  // FP16 offset storage: rest density and scale per component
+  if (h->cfg.precision == LBGPU_FP16) {
+    for (int c = 0; c < h->C; ++c) {
+      double rho0 = h->cfg.rho0[c];
+      double maxdev = 0.0;
+      const double* a = fluids[c];
+      // mean density and the largest |f_q - w_q rho0| over physical sites
+      double sum = 0.0;
+      int64_t cnt = 0;
+      for (int x = kHalo; x < h->nx + kHalo; ++x)
+        for (int y = kHalo; y < h->ny + kHalo; ++y)
+          for (int z = h->hz; z < h->nz + h->hz; ++z) {
+            const double* p = a + ((int64_t(x) * h->nyh + y) * h->nzh + z) * h->Q;
+            double s = 0.0;
+            for (int q = 0; q < h->Q; ++q) s += p[q];
+            sum += s;
+            ++cnt;
+          }
+      if (rho0 <= 0.0) rho0 = sum / double(cnt);
+      for (int x = kHalo; x < h->nx + kHalo; ++x)
+        for (int y = kHalo; y < h->ny + kHalo; ++y)
+          for (int z = h->hz; z < h->nz + h->hz; ++z) {
+            const double* p = a + ((int64_t(x) * h->nyh + y) * h->nzh + z) * h->Q;
+            for (int q = 0; q < h->Q; ++q) {
+              const double w = h->Q == 19 ? lbk::weight<19, double>(q) : lbk::weight<9, double>(q);
+              maxdev = std::max(maxdev, fabs(p[q] - w * rho0));
+            }
+          }
+      // offsets of up to 4x the initial spread stay inside half's normal range
+      // with ~11 significant bits; the scale maps that spread to 2^12
+      double scale = maxdev > 0.0 ? (4.0 * maxdev) / 4096.0 : 1.0 / 4096.0;
+      h->P.rho0[c] = float(rho0);
+      h->P.scale[c] = float(scale);
+      h->P.inv_scale[c] = float(1.0 / scale);
+    }
+  }
+
+  for (int c = 0; c < h->C; ++c) {
+    for (int xh0 = 0; xh0 < h->nxh; xh0 += planes_per_chunk) {
+      const int np = std::min(planes_per_chunk, h->nxh - xh0);
+      // only planes that hold physical sites matter
+      if (xh0 + np <= kHalo || xh0 >= h->nx + kHalo) continue;
+      e = cudaMemcpyAsync(h->staging, fluids[c] + size_t(xh0) * plane_vals, size_t(np) * plane_vals * sizeof(double),
+                          cudaMemcpyHostToDevice, h->stream);
+      if (e != cudaSuccess) return h->cuda_fail(e, "upload copy");
+      if (h->cfg.precision == LBGPU_FP64)
+        e = launch_upload<double>(h, c, xh0, np);
+      else if (h->cfg.precision == LBGPU_FP32)
+        e = launch_upload<float>(h, c, xh0, np);
+      else
+        e = launch_upload<__half>(h, c, xh0, np);
+      if (e != cudaSuccess) return h->cuda_fail(e, "upload kernel");
+    }
+  }
+
+  // mask: int32 haloed -> uint8 physical; dropped when nothing is solid
+  if (mask) {
+    if (!h->mask) {
+      e = cudaMalloc(&h->mask, size_t(h->n));
+      if (e != cudaSuccess) return h->cuda_fail(e, "mask allocation");
+      h->device_bytes += h->n;
+    }
+    int* d_count = reinterpret_cast<int*>(h->moments);
+    cudaMemsetAsync(d_count, 0, sizeof(int), h->stream);
+    const size_t plane_m = size_t(h->nyh) * h->nzh;
+    const int ppc = int(std::max<size_t>(1, h->staging_bytes / (plane_m * sizeof(int32_t))));
+    for (int xh0 = 0; xh0 < h->nxh; xh0 += ppc) {
+      const int np = std::min(ppc, h->nxh - xh0);
+      if (xh0 + np <= kHalo || xh0 >= h->nx + kHalo) continue;
+      e = cudaMemcpyAsync(h->staging, mask + size_t(xh0) * plane_m, size_t(np) * plane_m * sizeof(int32_t),
+                          cudaMemcpyHostToDevice, h->stream);
+      if (e != cudaSuccess) return h->cuda_fail(e, "mask copy");
+      const Geo g = geo_of(h);
+      const int64_t work = int64_t(g.ny) * g.nz * np;
+      k_upload_mask<<<unsigned(ceil_div(work, 256)), 256, 0, h->stream>>>(
+          reinterpret_cast<const int32_t*>(h->staging), h->mask, xh0, np, g, d_count);
+      h->launches++;
+    }
+    int nsolid = 0;
+    e = cudaMemcpyAsync(&nsolid, d_count, sizeof(int), cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return h->cuda_fail(e, "mask upload");
+    if (nsolid == 0) {
+      cudaFree(h->mask);
+      h->device_bytes -= h->n;
+      h->mask = nullptr;
+    }
+  } else if (h->mask) {
+    cudaFree(h->mask);
+    h->device_bytes -= h->n;
+    h->mask = nullptr;
+  }
+  e = cudaStreamSynchronize(h->stream);
+  if (e != cudaSuccess) return h->cuda_fail(e, "upload");
+  h->uploaded = true;
+  h->force_valid = 0;
+  return LBGPU_OK;
+}
+
+int lbgpu_set_record_force(lbgpu_handle* h, int32_t enable) {
+  if (!h) return LBGPU_E_INVALID;
+  cudaSetDevice(h->cfg.device);
+  if (enable && !h->force) {
+    const size_t bytes = size_t(h->C) * h->n * h->d * sizeof(double);
+    cudaError_t e = cudaMalloc(&h->force, bytes);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return h->fail(LBGPU_E_NOMEM, "force buffer allocation failed");
+    }
+    h->device_bytes += int64_t(bytes);
+  }
+  h->record_force = enable ? 1 : 0;
+  return LBGPU_OK;
+}
+
+int lbgpu_step(lbgpu_handle* h, int32_t nsteps) {
+  if (!h || nsteps < 0) return LBGPU_E_INVALID;
+  if (!h->uploaded) return h->fail(LBGPU_E_NOTREADY, "lbgpu_step before lbgpu_upload");
+  cudaSetDevice(h->cfg.device);
+  for (int t = 0; t < nsteps; ++t) {
+    lbk::StepBuffers b;
+    b.f = h->f[h->cur];
+    b.fout = h->f[1 - h->cur];
+    b.mask = h->mask;
+    b.rho = h->rho;
+    b.psi = h->psi;
+    b.force = h->force;
+    StepParams P = h->P;
+    P.record_force = (h->record_force && t == nsteps - 1) ? 1 : 0;
+    const lbk::StepEvents* evp = nullptr;
+    if (h->profiling) {
+      if (h->ev_pending.size() >= 4096) {
+        cudaError_t fe = fold_kernel_times(h);
+        if (fe != cudaSuccess) return h->cuda_fail(fe, "kernel timing");
+      }
+      lbk::StepEvents se;
+      if (!h->ev_pool.empty()) {
+        se = h->ev_pool.back();
+        h->ev_pool.pop_back();
+      } else {
+        for (auto& ev : se.ev) {
+          cudaError_t ce = cudaEventCreate(&ev);
+          if (ce != cudaSuccess) return h->cuda_fail(ce, "event create");
+        }
+      }
+      h->ev_pending.push_back(se);
+      evp = &h->ev_pending.back();
+    }
+    cudaError_t e;
+    if (h->cfg.precision == LBGPU_FP64)
+      e = lbk::launch_step_f64(h->Q, h->C, b, P, h->stream, &h->launches, evp);
+    else if (h->cfg.precision == LBGPU_FP32)
+      e = lbk::launch_step_f32(h->Q, h->C, b, P, h->stream, &h->launches, evp);
+    else
+      e = lbk::launch_step_f16(h->Q, h->C, b, P, h->stream, &h->launches, evp);
+    if (e != cudaSuccess) return h->cuda_fail(e, "step launch");
+    h->cur = 1 - h->cur;
+    if (P.record_force) h->force_valid = 1;
+  }
+  return LBGPU_OK;
+}
+
+int lbgpu_download(lbgpu_handle* h, double* const* fluids) {
+  if (!h || !fluids) return LBGPU_E_INVALID;
+  if (!h->uploaded) return h->fail(LBGPU_E_NOTREADY, "lbgpu_download before lbgpu_upload");
+  cudaSetDevice(h->cfg.device);
+  const size_t plane_vals = size_t(h->nyh) * h->nzh * h->Q;
+  const int planes_per_chunk = int(std::max<size_t>(1, h->staging_bytes / (plane_vals * sizeof(double))));
+  cudaError_t e;
+  for (int c = 0; c < h->C; ++c) {
+    if (!fluids[c]) continue;
+    for (int xh0 = 0; xh0 < h->nxh; xh0 += planes_per_chunk) {
+      const int np = std::min(planes_per_chunk, h->nxh - xh0);
+      if (h->cfg.precision == LBGPU_FP64)
+        e = launch_download<double>(h, c, xh0, np);
+      else if (h->cfg.precision == LBGPU_FP32)
+        e = launch_download<float>(h, c, xh0, np);
+      else
+        e = launch_download<__half>(h, c, xh0, np);
+      if (e != cudaSuccess) return h->cuda_fail(e, "download kernel");
+      e = cudaMemcpyAsync(fluids[c] + size_t(xh0) * plane_vals, h->staging, size_t(np) * plane_vals * sizeof(double),
+                          cudaMemcpyDeviceToHost, h->stream);
+      if (e != cudaSuccess) return h->cuda_fail(e, "download copy");
+    }
+  }
+  e = cudaStreamSynchronize(h->stream);
+  if (e != cudaSuccess) return h->cuda_fail(e, "download");
+  return LBGPU_OK;
+}
+
+int lbgpu_moments(lbgpu_handle* h, double* const* density, double* const* velocity, double* colour) {
+  if (!h) return LBGPU_E_INVALID;
+  if (!h->uploaded) return h->fail(LBGPU_E_NOTREADY, "lbgpu_moments before lbgpu_upload");
+  cudaSetDevice(h->cfg.device);
+  // the staging buffer holds C*N*d doubles of velocity when large enough,
+  // else velocities go one component at a time through the moments buffer
+  cudaError_t e;
+  const size_t n = size_t(h->n);
+  // densities (and colour) first
+  const bool want_den = density != nullptr || colour != nullptr;
+  if (want_den) {
+    double* col = h->staging;  // N doubles fit: staging >= one haloed plane... ensure below
+    const bool col_fits = h->staging_bytes >= n * sizeof(double);
+    std::vector<double> tmp;
+    double* dcol = (colour && h->C > 1 && col_fits) ? col : nullptr;
+    if (h->cfg.precision == LBGPU_FP64)
+      e = launch_moments<double>(h, h->moments, nullptr, dcol);
+    else if (h->cfg.precision == LBGPU_FP32)
+      e = launch_moments<float>(h, h->moments, nullptr, dcol);
+    else
+      e = launch_moments<__half>(h, h->moments, nullptr, dcol);
+    if (e != cudaSuccess) return h->cuda_fail(e, "moments kernel");
+    if (density)
+      for (int c = 0; c < h->C; ++c)
+        if (density[c]) {
+          e = cudaMemcpyAsync(density[c], h->moments + size_t(c) * n, n * sizeof(double), cudaMemcpyDeviceToHost,
+                              h->stream);
+          if (e != cudaSuccess) return h->cuda_fail(e, "density copy");
+        }
+    if (colour && h->C > 1) {
+      if (dcol) {
+        e = cudaMemcpyAsync(colour, dcol, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+        if (e != cudaSuccess) return h->cuda_fail(e, "colour copy");
+      } else {
+        // colour = rho0 - rho1 on fluid sites from the densities
+        tmp.resize(2 * n);
+        e = cudaMemcpyAsync(tmp.data(), h->moments, 2 * n * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+        if (e != cudaSuccess) return h->cuda_fail(e, "colour copy");
+        std::vector<uint8_t> m;
+        if (h->mask) {
+          m.resize(n);
+          e = cudaMemcpy(m.data(), h->mask, n, cudaMemcpyDeviceToHost);
+          if (e != cudaSuccess) return h->cuda_fail(e, "mask copy");
+        }
+        for (size_t i = 0; i < n; ++i) colour[i] = (h->mask && m[i]) ? 0.0 : tmp[i] - tmp[n + i];
+      }
+    }
+    e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return h->cuda_fail(e, "moments");
+  }
+  if (velocity) {
+    // d doubles per site per component: reuse the moments buffer (C*N
+    // doubles) one component-coordinate slab at a time is not possible in
+    // one kernel, so compute into a temporary device buffer
+    double* dvel = nullptr;
+    const size_t vbytes = size_t(h->C) * n * h->d * sizeof(double);
+    e = cudaMallocAsync(reinterpret_cast<void**>(&dvel), vbytes, h->stream);
+    if (e != cudaSuccess) return h->cuda_fail(e, "velocity buffer");
+    if (h->cfg.precision == LBGPU_FP64)
+      e = launch_moments<double>(h, nullptr, dvel, nullptr);
+    else if (h->cfg.precision == LBGPU_FP32)
+      e = launch_moments<float>(h, nullptr, dvel, nullptr);
+    else
+      e = launch_moments<__half>(h, nullptr, dvel, nullptr);
+    if (e != cudaSuccess) return h->cuda_fail(e, "velocity kernel");
+    for (int c = 0; c < h->C; ++c)
+      if (velocity[c]) {
+        e = cudaMemcpyAsync(velocity[c], dvel + size_t(c) * n * h->d, n * h->d * sizeof(double),
+                            cudaMemcpyDeviceToHost, h->stream);
+        if (e != cudaSuccess) return h->cuda_fail(e, "velocity copy");
+      }
+    cudaFreeAsync(dvel, h->stream);
+    e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return h->cuda_fail(e, "velocity");
+  }
+  return LBGPU_OK;
+}
+
+int lbgpu_force(lbgpu_handle* h, double* const* force) {
+  if (!h || !force) return LBGPU_E_INVALID;
+  if (!h->force || !h->force_valid)
+    return h->fail(LBGPU_E_NOTREADY, "no recorded force: call lbgpu_set_record_force(h, 1) before lbgpu_step");
+  cudaSetDevice(h->cfg.device);
+  const size_t per = size_t(h->n) * h->d;
+  for (int c = 0; c < h->C; ++c)
+    if (force[c]) {
+      cudaError_t e = cudaMemcpyAsync(force[c], h->force + size_t(c) * per, per * sizeof(double),
+                                      cudaMemcpyDeviceToHost, h->stream);
+      if (e != cudaSuccess) return h->cuda_fail(e, "force copy");
+    }
+  cudaError_t e = cudaStreamSynchronize(h->stream);
+  if (e != cudaSuccess) return h->cuda_fail(e, "force");
+  return LBGPU_OK;
+}
+
+int lbgpu_reduce(lbgpu_handle* h, double* mass, double* momentum) {
+  if (!h) return LBGPU_E_INVALID;
+  if (!h->uploaded) return h->fail(LBGPU_E_NOTREADY, "lbgpu_reduce before lbgpu_upload");
+  cudaSetDevice(h->cfg.device);
+  const int nblocks = int(std::min<int64_t>(1024, ceil_div(h->n, kRedThreads)));
+  const int64_t per_block = ceil_div(h->n, nblocks);
+  double* partial = h->moments;             // nblocks*8 doubles <= C*N doubles
+  double* out = h->moments + size_t(nblocks) * 8;
+  if (size_t(nblocks) * 8 + 8 > h->moments_bytes / sizeof(double))
+    return h->fail(LBGPU_E_INVALID, "lattice too small for the reduction scratch");
+  cudaError_t e;
+  if (h->cfg.precision == LBGPU_FP64)
+    e = launch_reduce<double>(h, partial, nblocks, per_block, out);
+  else if (h->cfg.precision == LBGPU_FP32)
+    e = launch_reduce<float>(h, partial, nblocks, per_block, out);
+  else
+    e = launch_reduce<__half>(h, partial, nblocks, per_block, out);
+  if (e != cudaSuccess) return h->cuda_fail(e, "reduce kernel");
+  double res[8];
+  e = cudaMemcpyAsync(res, out, sizeof res, cudaMemcpyDeviceToHost, h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  if (e != cudaSuccess) return h->cuda_fail(e, "reduce");
+  for (int c = 0; c < h->C; ++c) {
+    if (mass) mass[c] = res[c * 4];
+    if (momentum)
+      for (int vd = 0; vd < h->d; ++vd) momentum[c * h->d + vd] = res[c * 4 + 1 + vd];
+  }
+  return LBGPU_OK;
+}
+
+int lbgpu_synchronize(lbgpu_handle* h) {
+  if (!h) return LBGPU_E_INVALID;
+  cudaSetDevice(h->cfg.device);
+  cudaError_t e = cudaStreamSynchronize(h->stream);
+  if (e != cudaSuccess) return h->cuda_fail(e, "synchronize");
+  return LBGPU_OK;
+}
+
+int lbgpu_set_stream(lbgpu_handle* h, void* stream) {
+  if (!h) return LBGPU_E_INVALID;
+  cudaSetDevice(h->cfg.device);
+  cudaError_t e = fold_kernel_times(h);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  if (e != cudaSuccess) return h->cuda_fail(e, "set_stream");
+  h->stream = stream ? static_cast<cudaStream_t>(stream) : h->own_stream;
+  return LBGPU_OK;
+}
+
+int lbgpu_profile(lbgpu_handle* h, int32_t enable) {
+  if (!h) return LBGPU_E_INVALID;
+  cudaSetDevice(h->cfg.device);
+  cudaError_t e = fold_kernel_times(h);
+  if (e != cudaSuccess) return h->cuda_fail(e, "profile");
+  h->profiling = enable != 0;
+  h->kernel_ms[0] = h->kernel_ms[1] = 0.0;
+  h->kernel_n[0] = h->kernel_n[1] = 0;
+  return LBGPU_OK;
+}
+
+int lbgpu_kernel_time(lbgpu_handle* h, int32_t which, double* total_ms, int64_t* launches) {
+  if (!h || which < 0 || which > 1) return LBGPU_E_INVALID;
+  cudaSetDevice(h->cfg.device);
+  cudaError_t e = fold_kernel_times(h);
+  if (e != cudaSuccess) return h->cuda_fail(e, "kernel_time");
+  if (total_ms) *total_ms = h->kernel_ms[which];
+  if (launches) *launches = h->kernel_n[which];
+  return LBGPU_OK;
+}
+
+int64_t lbgpu_launch_count(const lbgpu_handle* h) { return h ? h->launches : 0; }
+int64_t lbgpu_device_bytes(const lbgpu_handle* h) { return h ? h->device_bytes : 0; }
+
+}  // extern "C"

@@ -1,0 +1,36 @@
+// Launchers for the timestep kernels, one translation unit per arithmetic
+// form (lb_step_f64.cu is compiled without FMA contraction).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "lb_kernels.cuh"
+
+namespace lbk {
+
+// Optional events recorded around each kernel (profiling): ev[0] before the
+// first kernel, ev[1] between the kernels, ev[2] after the second.
+struct StepEvents {
+  cudaEvent_t ev[3];
+};
+
+struct StepBuffers {
+  const void* f;        // populations in
+  void* fout;           // populations out
+  const uint8_t* mask;  // nullptr: no walls
+  void* rho;            // C*N (double for FP64, float otherwise)
+  void* psi;            // C*N
+  double* force;        // C*N*D when P.record_force
+};
+
+// Queue one timestep (two kernels) on `stream`.  Returns cudaSuccess or the
+// launch error; *launches is incremented by the number of kernels queued.
+cudaError_t launch_step_f64(int q, int c, const StepBuffers& b, const StepParams& P, cudaStream_t stream,
+                            int64_t* launches, const StepEvents* ev);
+cudaError_t launch_step_f32(int q, int c, const StepBuffers& b, const StepParams& P, cudaStream_t stream,
+                            int64_t* launches, const StepEvents* ev);
+cudaError_t launch_step_f16(int q, int c, const StepBuffers& b, const StepParams& P, cudaStream_t stream,
+                            int64_t* launches, const StepEvents* ev);
+
+}  // namespace lbk

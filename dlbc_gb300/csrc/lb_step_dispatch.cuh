@@ -1,0 +1,42 @@
+// Template dispatch shared by the per-form launch units.
+#pragma once
+
+#include "lb_launch.h"
+
+namespace lbk {
+
+constexpr int kStepThreads = 128;
+
+template <typename T, typename R, int Q, int C, bool W>
+cudaError_t launch_step_t(const StepBuffers& b, const StepParams& P, cudaStream_t st, int64_t* launches,
+                          const StepEvents* ev) {
+  const unsigned blocks = unsigned((P.n + kStepThreads - 1) / kStepThreads);
+  if (ev) cudaEventRecord(ev->ev[0], st);
+  k_density_psi<T, R, Q, C, W><<<blocks, kStepThreads, 0, st>>>(static_cast<const T*>(b.f), b.mask,
+                                                                 static_cast<R*>(b.rho), static_cast<R*>(b.psi), P);
+  if (ev) cudaEventRecord(ev->ev[1], st);
+  k_collide<T, R, Q, C, W><<<blocks, kStepThreads, 0, st>>>(static_cast<const T*>(b.f), static_cast<T*>(b.fout),
+                                                             b.mask, static_cast<const R*>(b.rho),
+                                                             static_cast<const R*>(b.psi), b.force, P);
+  if (ev) cudaEventRecord(ev->ev[2], st);
+  *launches += 2;
+  return cudaGetLastError();
+}
+
+template <typename T, typename R>
+cudaError_t dispatch_step(int q, int c, const StepBuffers& b, const StepParams& P, cudaStream_t st,
+                          int64_t* launches, const StepEvents* ev) {
+  const bool w = b.mask != nullptr;
+#define LB_CASE(QQ, CC)                                                     \
+  if (q == QQ && c == CC)                                                   \
+    return w ? launch_step_t<T, R, QQ, CC, true>(b, P, st, launches, ev)        \
+             : launch_step_t<T, R, QQ, CC, false>(b, P, st, launches, ev);
+  LB_CASE(19, 2)
+  LB_CASE(19, 1)
+  LB_CASE(9, 2)
+  LB_CASE(9, 1)
+#undef LB_CASE
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace lbk

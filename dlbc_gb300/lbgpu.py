@@ -1,0 +1,242 @@
+"""ctypes binding of the C ABI in include/lbgpu.h (``liblbgpu.so``).
+
+This is how the Python host side (tests, bench, the reference-style driver
+in :mod:`dlbc_gb300.driver`) reaches the CUDA kernels: exactly the calls a
+D program would make through ``extern(C)``.  The library is loaded from the
+package's ``_build`` directory; if it is missing the import fails loudly
+(there is no CPU fallback).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import List, Optional, Sequence
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liblbgpu.so")
+
+FP64, FP32, FP16 = 0, 1, 2
+PRECISIONS = {"fp64": FP64, "fp32": FP32, "fp16": FP16}
+MAXC = 2
+
+ERRORS = {0: "OK", -1: "LBGPU_E_INVALID", -2: "LBGPU_E_NOMEM", -3: "LBGPU_E_CUDA", -4: "LBGPU_E_BUDGET",
+          -5: "LBGPU_E_NOTREADY", -6: "LBGPU_E_NONFINITE"}
+
+EXPORTED = ["lbgpu_abi_version", "lbgpu_create", "lbgpu_destroy", "lbgpu_upload", "lbgpu_step",
+            "lbgpu_download", "lbgpu_moments", "lbgpu_set_record_force", "lbgpu_force", "lbgpu_reduce",
+            "lbgpu_synchronize", "lbgpu_set_stream", "lbgpu_profile", "lbgpu_kernel_time",
+            "lbgpu_launch_count", "lbgpu_device_bytes", "lbgpu_last_error"]
+
+
+class LbgpuConfig(C.Structure):
+    _fields_ = [
+        ("d", C.c_int32), ("q", C.c_int32), ("gn", C.c_int32 * 3), ("components", C.c_int32),
+        ("shan_chen", C.c_int32), ("psi_form", C.c_int32), ("eq_form", C.c_int32),
+        ("precision", C.c_int32), ("device", C.c_int32),
+        ("tau", C.c_double * MAXC), ("gcc", (C.c_double * MAXC) * MAXC), ("gwc", C.c_double * MAXC),
+        ("global_acc", C.c_double * 3), ("rho0", C.c_double * MAXC),
+    ]
+
+
+class LbgpuError(RuntimeError):
+    pass
+
+
+_lib: Optional[C.CDLL] = None
+
+
+def lib() -> C.CDLL:
+    """Load liblbgpu.so (built by dlbc_gb300.build)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise LbgpuError(f"{LIB_PATH} is missing: run `python -m dlbc_gb300.build` (needs nvcc)")
+        L = C.CDLL(LIB_PATH)
+        H = C.c_void_p
+        PP = C.POINTER(C.c_void_p)
+        L.lbgpu_abi_version.restype = C.c_int32
+        L.lbgpu_create.argtypes = [C.POINTER(LbgpuConfig), C.POINTER(H)]
+        L.lbgpu_destroy.argtypes = [H]
+        L.lbgpu_destroy.restype = None
+        L.lbgpu_upload.argtypes = [H, PP, C.c_void_p]
+        L.lbgpu_step.argtypes = [H, C.c_int32]
+        L.lbgpu_download.argtypes = [H, PP]
+        L.lbgpu_moments.argtypes = [H, PP, PP, C.c_void_p]
+        L.lbgpu_set_record_force.argtypes = [H, C.c_int32]
+        L.lbgpu_force.argtypes = [H, PP]
+        L.lbgpu_reduce.argtypes = [H, C.c_void_p, C.c_void_p]
+        L.lbgpu_synchronize.argtypes = [H]
+        L.lbgpu_set_stream.argtypes = [H, C.c_void_p]
+        L.lbgpu_profile.argtypes = [H, C.c_int32]
+        L.lbgpu_kernel_time.argtypes = [H, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_int64)]
+        L.lbgpu_launch_count.argtypes = [H]
+        L.lbgpu_launch_count.restype = C.c_int64
+        L.lbgpu_device_bytes.argtypes = [H]
+        L.lbgpu_device_bytes.restype = C.c_int64
+        L.lbgpu_last_error.argtypes = [H]
+        L.lbgpu_last_error.restype = C.c_char_p
+        _lib = L
+    return _lib
+
+
+def make_config(p, precision: int = FP64, device: int = 0, rho0: Sequence[float] = (0.0, 0.0)) -> LbgpuConfig:
+    """C config from :class:`dlbc_gb300.params.LBParams`."""
+    c = LbgpuConfig()
+    c.d, c.q = p.d, p.q
+    for i in range(p.d):
+        c.gn[i] = int(p.gn[i])
+    c.components = p.components
+    c.shan_chen = int(p.shan_chen)
+    c.psi_form = int(p.psi_form)
+    c.eq_form = int(p.eq_form)
+    c.precision = int(precision)
+    c.device = int(device)
+    for f in range(p.components):
+        c.tau[f] = p.tau[f] if p.tau else 1.0
+        c.gwc[f] = p.gwc[f]
+        c.rho0[f] = rho0[f] if f < len(rho0) else 0.0
+        for g in range(p.components):
+            c.gcc[f][g] = p.gcc[f][g]
+    for i in range(p.d):
+        c.global_acc[i] = p.global_acc[i]
+    return c
+
+
+def _ptrs(arrays: Sequence[Optional[np.ndarray]], n: int):
+    arr = (C.c_void_p * n)()
+    for i in range(n):
+        a = arrays[i] if i < len(arrays) else None
+        arr[i] = None if a is None else a.ctypes.data
+    return arr
+
+
+def _ptr_of(a) -> int:
+    """Address of a numpy array or a (host) torch tensor."""
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    return a.data_ptr()
+
+
+class GPULattice:
+    """One device-resident lattice behind the C ABI."""
+
+    def __init__(self, p, precision: int = FP64, device: int = 0, rho0: Sequence[float] = (0.0, 0.0)):
+        self.p = p
+        self.precision = precision
+        self.cfg = make_config(p, precision, device, rho0)
+        self.h = C.c_void_p()
+        rc = lib().lbgpu_create(C.byref(self.cfg), C.byref(self.h))
+        if rc != 0:
+            raise LbgpuError(f"lbgpu_create: {ERRORS.get(rc, rc)}: {lib().lbgpu_last_error(None).decode()}")
+        self.n = tuple(int(x) for x in p.gn[: p.d])
+        self.nH = tuple(x + 4 for x in self.n)
+
+    def _check(self, rc: int, what: str):
+        if rc != 0:
+            raise LbgpuError(f"{what}: {ERRORS.get(rc, rc)}: {lib().lbgpu_last_error(self.h).decode()}")
+
+    def close(self):
+        if self.h:
+            lib().lbgpu_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- reference-layout transfers -----------------------------------------
+    def upload(self, fluids: List, mask=None) -> None:
+        """fluids[c]: haloed AoS float64 arrays (nH..., q); mask: haloed int32 or None.
+        Accepts numpy arrays or pinned host torch tensors."""
+        ptrs = (C.c_void_p * MAXC)()
+        for i, a in enumerate(fluids):
+            if isinstance(a, np.ndarray):
+                assert a.dtype == np.float64 and a.flags.c_contiguous and a.shape == self.nH + (self.p.q,)
+            ptrs[i] = _ptr_of(a)
+        m = None
+        if mask is not None:
+            if isinstance(mask, np.ndarray):
+                assert mask.dtype == np.int32 and mask.flags.c_contiguous and mask.shape == self.nH
+            m = _ptr_of(mask)
+        self._check(lib().lbgpu_upload(self.h, ptrs, m), "lbgpu_upload")
+
+    def download(self, out: Optional[List] = None) -> List:
+        if out is None:
+            out = [np.empty(self.nH + (self.p.q,), np.float64) for _ in range(self.p.components)]
+        ptrs = (C.c_void_p * MAXC)()
+        for i, a in enumerate(out):
+            ptrs[i] = _ptr_of(a)
+        self._check(lib().lbgpu_download(self.h, ptrs), "lbgpu_download")
+        return out
+
+    def step(self, n: int = 1) -> None:
+        self._check(lib().lbgpu_step(self.h, int(n)), "lbgpu_step")
+
+    def synchronize(self) -> None:
+        self._check(lib().lbgpu_synchronize(self.h), "lbgpu_synchronize")
+
+    def set_stream(self, stream_handle: Optional[int]) -> None:
+        """Queue work on a caller-owned cudaStream_t (an integer handle, e.g.
+        ``torch.cuda.Stream().cuda_stream``); None restores the own stream."""
+        self._check(lib().lbgpu_set_stream(self.h, stream_handle), "lbgpu_set_stream")
+
+    def profile(self, on: bool = True) -> None:
+        self._check(lib().lbgpu_profile(self.h, int(on)), "lbgpu_profile")
+
+    def kernel_time(self, which: int):
+        """(total ms, launches) of kernel 0 (density/psi) or 1 (collide)."""
+        ms = C.c_double()
+        n = C.c_int64()
+        self._check(lib().lbgpu_kernel_time(self.h, which, C.byref(ms), C.byref(n)), "lbgpu_kernel_time")
+        return ms.value, n.value
+
+    def set_record_force(self, on: bool = True) -> None:
+        self._check(lib().lbgpu_set_record_force(self.h, int(on)), "lbgpu_set_record_force")
+
+    # -- outputs -----------------------------------------------------------------
+    def density(self) -> List[np.ndarray]:
+        out = [np.empty(self.n, np.float64) for _ in range(self.p.components)]
+        self._check(lib().lbgpu_moments(self.h, _ptrs(out, MAXC), None, None), "lbgpu_moments")
+        return out
+
+    def velocity(self) -> List[np.ndarray]:
+        out = [np.empty(self.n + (self.p.d,), np.float64) for _ in range(self.p.components)]
+        self._check(lib().lbgpu_moments(self.h, None, _ptrs(out, MAXC), None), "lbgpu_moments")
+        return out
+
+    def colour(self) -> np.ndarray:
+        out = np.empty(self.n, np.float64)
+        self._check(lib().lbgpu_moments(self.h, None, None, out.ctypes.data), "lbgpu_moments")
+        return out
+
+    def force(self) -> List[np.ndarray]:
+        out = [np.empty(self.n + (self.p.d,), np.float64) for _ in range(self.p.components)]
+        self._check(lib().lbgpu_force(self.h, _ptrs(out, MAXC)), "lbgpu_force")
+        return out
+
+    def population(self) -> List[np.ndarray]:
+        """Physical-site populations [x][y][z][q] (like the population dumps)."""
+        full = self.download()
+        sl = tuple(slice(2, 2 + n) for n in self.n)
+        return [np.ascontiguousarray(a[sl]) for a in full]
+
+    def reduce(self):
+        C_ = self.p.components
+        mass = np.zeros(C_, np.float64)
+        mom = np.zeros(C_ * self.p.d, np.float64)
+        self._check(lib().lbgpu_reduce(self.h, mass.ctypes.data, mom.ctypes.data), "lbgpu_reduce")
+        return mass, mom.reshape(C_, self.p.d)
+
+    @property
+    def launch_count(self) -> int:
+        return int(lib().lbgpu_launch_count(self.h))
+
+    @property
+    def device_bytes(self) -> int:
+        return int(lib().lbgpu_device_bytes(self.h))

@@ -1,0 +1,154 @@
+/* lbgpu: GB300 (sm_103a) lattice-Boltzmann timestep behind a C ABI.
+ *
+ * This is the drop-in boundary for the DLBC time loop.  In the reference,
+ * one timestep is (src/main.d:174-199):
+ *
+ *   L.exchangeHalo();        // src/dlbc/fields/parallel.d:40
+ *   L.advectFields();        // src/dlbc/lb/advection.d:35
+ *   L.resetForce();          // src/dlbc/lb/force.d:165
+ *   L.addShanChenForce();    // src/dlbc/lb/force.d:223
+ *   L.distributeForce();     // src/dlbc/lb/force.d:179
+ *   L.prepareToCollide();    // src/dlbc/lb/collision.d:141
+ *   L.collideFields(tau, globalAcc);   // src/dlbc/lb/collision.d:161
+ *
+ * lbgpu_step() replaces that whole sequence (halo exchange becomes periodic
+ * index wrap on one in-GPU domain).  The lattice fields stay resident on the
+ * device between calls; the host exchanges them in the reference's own layout
+ * (Field.arr of src/dlbc/fields/field.d:114-125: row-major [x][y][z] over the
+ * haloed lattice, halo width 2, the Q populations of a site contiguous), so a
+ * D program passes `L.fluids[i].arr._data.ptr` and `L.mask.arr._data.ptr`
+ * unchanged.
+ *
+ * Conventions: every entry point returns 0 on success or a negative
+ * LBGPU_E_* code; nothing throws or exits across the ABI.  A handle is used
+ * from one host thread at a time; work is ordered on the handle's stream.
+ * Host buffers are borrowed for the duration of a call only.
+ */
+#ifndef LBGPU_H
+#define LBGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LBGPU_ABI_VERSION 1
+#define LBGPU_MAX_COMPONENTS 2
+
+/* status codes */
+#define LBGPU_OK 0
+#define LBGPU_E_INVALID (-1)     /* bad argument or unsupported configuration */
+#define LBGPU_E_NOMEM (-2)       /* device or pinned-host allocation failed */
+#define LBGPU_E_CUDA (-3)        /* CUDA runtime error (see lbgpu_last_error) */
+#define LBGPU_E_BUDGET (-4)      /* request exceeds the configured HBM budget */
+#define LBGPU_E_NOTREADY (-5)    /* no state uploaded yet */
+#define LBGPU_E_NONFINITE (-6)   /* a non-finite value was detected on the device */
+
+/* lb.eqdist.eqDistForm (src/dlbc/lb/eqdist.d:23-36) */
+#define LBGPU_EQ_SECOND_ORDER 0
+#define LBGPU_EQ_THIRD_ORDER 1
+#define LBGPU_EQ_BDIST2 2
+/* lb.force.psiForm (src/dlbc/lb/force.d:48-57) */
+#define LBGPU_PSI_LINEAR 0
+#define LBGPU_PSI_EXPONENTIAL 1
+/* storage/arithmetic forms */
+#define LBGPU_FP64 0        /* double storage + double arithmetic: the reference's numbers */
+#define LBGPU_FP32 1        /* float storage + float arithmetic */
+#define LBGPU_FP16 2        /* half storage of f - w_q*rho0 (scaled) + float arithmetic */
+
+typedef struct lbgpu_config {
+  int32_t d, q;               /* 3/19 (D3Q19) or 2/9 (D2Q9): gconn (src/dlbc/lb/connectivity.d) */
+  int32_t gn[3];              /* lattice.gn (gn[2] ignored when d == 2); each >= 2 */
+  int32_t components;         /* lb.components, 1 or 2 */
+  int32_t shan_chen;          /* lb.force.enableShanChen */
+  int32_t psi_form;           /* lb.force.psiForm */
+  int32_t eq_form;            /* lb.eqdist.eqDistForm */
+  int32_t precision;          /* LBGPU_FP64 / LBGPU_FP32 / LBGPU_FP16 */
+  int32_t device;             /* CUDA device ordinal */
+  double tau[LBGPU_MAX_COMPONENTS];                        /* lb.tau */
+  double gcc[LBGPU_MAX_COMPONENTS][LBGPU_MAX_COMPONENTS];  /* lb.force.gcc */
+  double gwc[LBGPU_MAX_COMPONENTS];                        /* lb.force.gwc */
+  double global_acc[3];                                    /* lb.force.globalAcc */
+  double rho0[LBGPU_MAX_COMPONENTS];  /* LBGPU_FP16: rest density of the stored offsets
+                                         f_q - w_q*rho0 (0: use the mean density at upload) */
+} lbgpu_config;
+
+typedef struct lbgpu_handle lbgpu_handle;
+
+/* Create a lattice on cfg->device.  No field data yet: call lbgpu_upload.
+ * Replaces the allocation in prepareLBFields/prepareForce
+ * (src/dlbc/lb/init.d:60-72, src/dlbc/lb/force.d:67-107). */
+int lbgpu_create(const lbgpu_config* cfg, lbgpu_handle** out);
+void lbgpu_destroy(lbgpu_handle* h);
+
+/* Copy the host fields to the device.  fluids[c] points at component c's
+ * haloed AoS array ((gn+4)^d sites x q doubles, i.e. Field.arr._data of
+ * L.fluids[c]); mask points at the haloed Mask array (int32: 0 None, 1 Solid),
+ * or is NULL for an all-fluid lattice.  Halo entries are ignored: the device
+ * uses periodic images, which is what exchangeHalo (src/dlbc/fields/parallel.d:40)
+ * puts there on one process. */
+int lbgpu_upload(lbgpu_handle* h, const double* const* fluids, const int32_t* mask);
+
+/* Advance nsteps timesteps (one call = nsteps iterations of runTimeloop's
+ * body, src/main.d:175-199, without dumpData). */
+int lbgpu_step(lbgpu_handle* h, int32_t nsteps);
+
+/* Copy the current populations back into haloed AoS host arrays (halo sites
+ * are filled with their periodic images, as after exchangeHalo). */
+int lbgpu_download(lbgpu_handle* h, double* const* fluids);
+
+/* Fields as dumpLBData writes them (src/dlbc/lb/io.d:56-101), over the
+ * physical lattice, row-major [x][y][z] (+ vector component fastest):
+ *   density[c]   N doubles  (densityField, src/dlbc/lb/density.d:89)
+ *   velocity[c]  N*d doubles (rawVelocityField, src/dlbc/lb/velocity.d:106; 0 on solids)
+ *   colour       N doubles  (colourField of components 0 and 1, src/dlbc/lb/density.d:284)
+ * Any pointer may be NULL to skip that field. */
+int lbgpu_moments(lbgpu_handle* h, double* const* density, double* const* velocity, double* colour);
+
+/* Force field of the last step (L.force, dumped as force-<name>), N*d
+ * doubles per component; requires lbgpu_set_record_force(h, 1) before the
+ * step. */
+int lbgpu_set_record_force(lbgpu_handle* h, int32_t enable);
+int lbgpu_force(lbgpu_handle* h, double* const* force);
+
+/* Global mass and momentum over fluid sites (globalTotalMass,
+ * src/dlbc/lb/density.d:172; globalTotalMomentum, src/dlbc/lb/momentum.d:172),
+ * reduced in a fixed order in double precision.  mass: components doubles;
+ * momentum: components*d doubles.  Either may be NULL. */
+int lbgpu_reduce(lbgpu_handle* h, double* mass, double* momentum);
+
+/* Wait for all work queued on the handle's stream. */
+int lbgpu_synchronize(lbgpu_handle* h);
+
+/* Queue the handle's work on a caller-owned cudaStream_t (passed as void*;
+ * NULL restores the handle's own stream).  The caller keeps the stream alive
+ * while the handle uses it. */
+int lbgpu_set_stream(lbgpu_handle* h, void* stream);
+
+/* Per-kernel timing with CUDA events on the handle's stream.  While enabled,
+ * lbgpu_step brackets each timestep kernel with events; lbgpu_kernel_time
+ * returns the accumulated milliseconds and launch count of kernel `which`
+ * (LBGPU_KERNEL_*) since the last reset (it synchronizes the stream). */
+#define LBGPU_KERNEL_DENSITY_PSI 0
+#define LBGPU_KERNEL_COLLIDE 1
+int lbgpu_profile(lbgpu_handle* h, int32_t enable);
+int lbgpu_kernel_time(lbgpu_handle* h, int32_t which, double* total_ms, int64_t* launches);
+
+/* Number of kernel launches issued by this handle since creation. */
+int64_t lbgpu_launch_count(const lbgpu_handle* h);
+
+/* Device bytes held by the handle. */
+int64_t lbgpu_device_bytes(const lbgpu_handle* h);
+
+/* Message for the last failed call on h (or on lbgpu_create when h is NULL). */
+const char* lbgpu_last_error(const lbgpu_handle* h);
+
+/* ABI version of the loaded library (LBGPU_ABI_VERSION). */
+int32_t lbgpu_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LBGPU_H */

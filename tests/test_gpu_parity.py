@@ -1,0 +1,178 @@
+"""CUDA path (through the C ABI) against the CPU oracle on the same inputs.
+
+The FP64 form must be bit-identical to the oracle run with the kernels' exp
+(exp_mode=1): both evaluate the reference's operations in the same order in
+IEEE double without contraction.  Reduced-precision forms are checked
+against the FP64 oracle within stated error bounds.
+"""
+import numpy as np
+import pytest
+
+from dlbc_gb300 import init, lbgpu
+from golden_util import compare, golden_arrays, load_case, times
+from lbcases import droplet_channel, spinodal
+from oracle import oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+
+def run_both(p, steps, precision=lbgpu.FP64, record_force=False):
+    fl, m = init.init_fields(p)
+    o = orc.Oracle(p, exp_mode=1, threads=8)
+    g = lbgpu.GPULattice(p, precision=precision)
+    g.upload(fl, m)
+    if record_force:
+        g.set_record_force(True)
+    o.run(steps)
+    g.step(steps)
+    g.synchronize()
+    return o, g
+
+
+def assert_bitwise(o, g, p, check_force=False):
+    pops = g.population()
+    for c in range(p.components):
+        a, b = pops[c], o.population(c)
+        assert np.array_equal(a, b), f"component {c}: max |diff| {np.nanmax(np.abs(a - b)):.3e}"
+    dens = g.density()
+    vel = g.velocity()
+    for c in range(p.components):
+        assert np.array_equal(dens[c], o.density(c))
+        assert np.array_equal(vel[c], o.velocity(c))
+    if p.components == 2:
+        assert np.array_equal(g.colour(), o.colour(0, 1))
+    if check_force:
+        fo = g.force()
+        for c in range(p.components):
+            assert np.array_equal(fo[c], o.force(c))
+
+
+@pytest.mark.parametrize("eq", ["BDist2", "SecondOrder", "ThirdOrder"])
+def test_fp64_spinodal_bitwise(eq):
+    p = spinodal((24, 20, 16), eq=eq)
+    o, g = run_both(p, 50, record_force=True)
+    assert_bitwise(o, g, p, check_force=True)
+
+
+def test_fp64_spinodal_long_run_bitwise():
+    """Config-0 physics at 32^3 for 300 steps: chaotic enough that any
+    last-bit difference would have grown visibly."""
+    p = spinodal((32, 32, 32), eq="BDist2")
+    o, g = run_both(p, 300)
+    assert_bitwise(o, g, p)
+
+
+@pytest.mark.parametrize("gwc", [(0.0, 0.0), (0.3, -0.2)])
+def test_fp64_droplet_channel_walls_bitwise(gwc):
+    """Config-1 physics (walls, body force, sphere) incl. the wall force."""
+    p = droplet_channel((24, 12, 14), radius=4.0, acc=1e-3, gwc=gwc)
+    o, g = run_both(p, 40, record_force=True)
+    assert_bitwise(o, g, p, check_force=True)
+
+
+def test_fp64_odd_and_minimal_sizes():
+    for n in [(5, 7, 3), (2, 2, 2), (3, 2, 9)]:
+        p = spinodal(n, eq="BDist2")
+        o, g = run_both(p, 7)
+        assert_bitwise(o, g, p)
+
+
+def test_fp64_unequal_tau_and_single_component():
+    p = droplet_channel((16, 10, 12), radius=3.0, acc=2e-4, tau=(0.8, 1.3), eq="SecondOrder")
+    o, g = run_both(p, 20)
+    assert_bitwise(o, g, p)
+    p1 = spinodal((12, 10, 8))
+    p1.components = 1
+    p1.field_names = ["red"]
+    p1.tau = [0.9]
+    p1.gcc = [[-4.0]]
+    p1.gwc = [0.0]
+    p1.fluid_init = p1.fluid_init[:1]
+    p1.fluid_densities = p1.fluid_densities[:1]
+    p1.fluid_perturb = p1.fluid_perturb[:1]
+    p1.random_reseed = p1.random_reseed[:1]
+    p1.random_seed = p1.random_seed[:1]
+    o, g = run_both(p1, 15)
+    assert_bitwise(o, g, p1)
+
+
+@pytest.mark.parametrize("name", ["merging-droplets-3d", "bdist2-sc-3d", "laplace-droplet-3d",
+                                  "merging-droplets-2d", "bdist2-sc-2d", "poiseuille-2d",
+                                  "laplace-quasi-1d-d2q9"])
+def test_fp64_reference_cases_bitwise_and_goldens(name):
+    """The reference's own test inputs: bitwise vs the oracle, and within the
+    reference's accuracies of its golden files at the first dump times."""
+    z, p = load_case(name)
+    fl, m = init.init_fields(p)
+    g = lbgpu.GPULattice(p)
+    g.upload(fl, m)
+    o = orc.Oracle(p, exp_mode=1, threads=8)
+    t_now = 0
+    for t in times(z):
+        if t > 100:
+            break
+        g.step(t - t_now)
+        o.run(t - t_now)
+        t_now = t
+        assert_bitwise(o, g, p)
+        for key, kind in golden_arrays(z, t):
+            if kind.startswith("force") or kind == "mask":
+                continue
+            tol = max(float(z[key + "/tol"]), 2.5e-15 if t > 0 else 0.0)
+            if kind == "colour":
+                a = g.colour()
+            else:
+                what, nm = kind.split("-", 1)
+                c = p.field_names.index(nm)
+                a = {"density": g.density, "velocity": g.velocity, "population": g.population}[what]()[c]
+            assert compare(z, key, a, tol), key
+
+
+def test_download_roundtrip_and_halo():
+    p = droplet_channel((10, 8, 6), radius=2.0)
+    fl, m = init.init_fields(p)
+    g = lbgpu.GPULattice(p)
+    g.upload(fl, m)
+    back = g.download()
+    for c in range(2):
+        assert np.array_equal(back[c], fl[c])
+
+
+def test_mass_conservation_and_reduction():
+    p = spinodal((32, 24, 16))
+    o, g = run_both(p, 100)
+    mass, mom = g.reduce()
+    for c in range(2):
+        ref = o.total_mass(c)
+        assert abs(mass[c] - ref) <= 1e-13 * abs(ref)
+    fl, _ = init.init_fields(p)
+    m0 = [fl[c][2:-2, 2:-2, 2:-2].sum() for c in range(2)]
+    for c in range(2):
+        assert abs(mass[c] - m0[c]) <= 1e-12 * m0[c]
+
+
+@pytest.mark.parametrize("precision,tol", [(lbgpu.FP32, 2e-5), (lbgpu.FP16, 2e-3)])
+def test_reduced_precision_error_vs_fp64(precision, tol):
+    """Relative L2 density error of the FP32 / FP16-storage forms against the
+    FP64 oracle after 100 steps of spinodal decomposition."""
+    p = spinodal((32, 32, 32), perturb=0.02)
+    o, g = run_both(p, 100, precision=precision)
+    dens = g.density()
+    for c in range(2):
+        ref = o.density(c)
+        err = np.linalg.norm(dens[c] - ref) / np.linalg.norm(ref)
+        assert err < tol, (c, err)
+
+
+def test_launch_count_and_errors():
+    p = spinodal((8, 8, 8))
+    fl, m = init.init_fields(p)
+    g = lbgpu.GPULattice(p)
+    with pytest.raises(lbgpu.LbgpuError):
+        g.step(1)  # before upload
+    g.upload(fl, m)
+    n0 = g.launch_count
+    g.step(5)
+    assert g.launch_count - n0 == 10
+    with pytest.raises(lbgpu.LbgpuError):
+        g.force()  # force not recorded
