@@ -224,7 +224,14 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-forms", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--form", default="fp64", choices=["fp64", "fp32", "fp16"],
+                    help="headline form (the others are reported under 'forms')")
+    ap.add_argument("--lattice", default=None,
+                    help="override the lattice as X,Y,Z (small cases for profiling; the default is the workload)")
     args = ap.parse_args()
+    if args.lattice:
+        global LATTICE
+        LATTICE = tuple(int(v) for v in args.lattice.split(","))
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
@@ -245,21 +252,23 @@ def main():
 
     from dlbc_gb300 import build, init, lbgpu
     build.build()
-    p = workload_params()
+    p = workload_params(LATTICE)
     fluids, mask = init.init_fields(p)
     sites = LATTICE[0] * LATTICE[1] * LATTICE[2]
     peak, peak_kind = measured_peaks()
+    forms_all = {"fp64": lbgpu.FP64, "fp32": lbgpu.FP32, "fp16": lbgpu.FP16}
+    head = forms_all[args.form]
+    dtype = {"fp64": "f64", "fp32": "f32", "fp16": "f16-storage/f32"}[args.form]
 
     def barrier():
         if dist is not None:
             dist.barrier()
         torch.cuda.synchronize(device)
 
-    # ---- headline: FP64, inputs resident in HBM
+    # ---- headline form, inputs resident in HBM
     barrier()
     with ClockSampler(device) as clk:
-        ms_step, k2_ms, k1_ms, launches = time_form(p, fluids, mask, lbgpu.FP64, args.steps, args.warmup, device,
-                                                    torch)
+        ms_step, k2_ms, k1_ms, launches = time_form(p, fluids, mask, head, args.steps, args.warmup, device, torch)
     barrier()
     t_local = torch.tensor([ms_step], dtype=torch.float64, device=f"cuda:{device}")
     if dist is not None:
@@ -269,36 +278,42 @@ def main():
 
     # ---- end to end through the C ABI with pinned host buffers:
     # per step, upload the state (populations + mask), one timestep, download
-    g = lbgpu.GPULattice(p, precision=lbgpu.FP64, device=device)
-    hb = [torch.from_numpy(f).pin_memory() for f in fluids]
-    hm = torch.from_numpy(mask).pin_memory()
-    g.upload(hb, hm)
-    for _ in range(2):
-        g.step(1)
-        g.download(hb)
+    e2e = None
+    if args.e2e_steps > 0:
+        g = lbgpu.GPULattice(p, precision=head, device=device)
+        hb = [torch.from_numpy(f).pin_memory() for f in fluids]
+        hm = torch.from_numpy(mask).pin_memory()
         g.upload(hb, hm)
-    barrier()
-    n_e2e = args.e2e_steps
-    t0 = time.perf_counter()
-    for _ in range(n_e2e):
-        g.upload(hb, hm)
-        g.step(1)
-        g.download(hb)
-    barrier()
-    e2e_s = time.perf_counter() - t0
-    e2e_t = torch.tensor([e2e_s], dtype=torch.float64, device=f"cuda:{device}")
-    if dist is not None:
-        dist.all_reduce(e2e_t, op=dist.ReduceOp.MAX)
-    e2e_value = world * sites * n_e2e / float(e2e_t.item()) / 1e6
-    h2d = sum(int(x.numel()) * 8 for x in hb) + int(hm.numel()) * 4
-    d2h = sum(int(x.numel()) * 8 for x in hb)
-    g.close()
-    del hb, hm
+        for _ in range(2):
+            g.step(1)
+            g.download(hb)
+            g.upload(hb, hm)
+        barrier()
+        n_e2e = args.e2e_steps
+        t0 = time.perf_counter()
+        for _ in range(n_e2e):
+            g.upload(hb, hm)
+            g.step(1)
+            g.download(hb)
+        barrier()
+        e2e_s = time.perf_counter() - t0
+        e2e_t = torch.tensor([e2e_s], dtype=torch.float64, device=f"cuda:{device}")
+        if dist is not None:
+            dist.all_reduce(e2e_t, op=dist.ReduceOp.MAX)
+        e2e_value = world * sites * n_e2e / float(e2e_t.item()) / 1e6
+        e2e = {"value": round(e2e_value, 2), "unit": UNIT,
+               "h2d_bytes_per_step": sum(int(x.numel()) * 8 for x in hb) + int(hm.numel()) * 4,
+               "d2h_bytes_per_step": sum(int(x.numel()) * 8 for x in hb), "steps": n_e2e,
+               "call": "lbgpu_upload(pinned AoS haloed fluids + mask) -> lbgpu_step(1) -> lbgpu_download"}
+        g.close()
+        del hb, hm
 
-    # ---- the reduced-precision forms of the same workload
+    # ---- the other forms of the same workload
     forms = {}
     if not args.no_forms:
-        for name, prec in (("fp32", lbgpu.FP32), ("fp16", lbgpu.FP16)):
+        for name, prec in forms_all.items():
+            if name == args.form:
+                continue
             f_ms, f_k2, f_k1, _ = time_form(p, fluids, mask, prec, args.steps, args.warmup, device, torch)
             forms[name] = {"value": round(world * sites / (f_ms * 1e-3) / 1e6, 1),
                            "ms_per_step": round(f_ms, 4),
@@ -312,19 +327,19 @@ def main():
         cpu = cpu_baseline(p)
 
     if rank == 0:
+        pop_gb = 2 * 2 * 19 * {0: 8, 1: 4, 2: 2}[head] * sites / 1e9
         line = {
             "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms_max, 4), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "lattice": list(LATTICE), "form": "fp64", "eq_form": "BDist2",
+            "vs_baseline": None, "dtype": dtype, "data": "synthetic",
+            "config": {"workload": WORKLOAD if LATTICE == (256, 128, 128) else f"droplet-channel {LATTICE}",
+                       "lattice": list(LATTICE), "form": args.form, "eq_form": "BDist2",
                        "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
-                       "l2": "inputs larger than L2 (FP64 populations 2x2.55 GB)"},
-            "roofline": roofline(lbgpu.FP64, sites, k2_ms, peak, peak_kind, read_traffic("fp64")),
+                       "l2": f"inputs larger than L2 (populations, both buffers: {pop_gb:.2f} GB)"},
+            "roofline": roofline(head, sites, k2_ms, peak, peak_kind, read_traffic(args.form)),
             "kernels_ms": {"k_density_psi": round(k1_ms, 4), "k_collide": round(k2_ms, 4)},
             "cpu_baseline": cpu,
-            "e2e": {"value": round(e2e_value, 2), "unit": UNIT, "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h,
-                    "call": "lbgpu_upload(pinned AoS haloed fluids + mask) -> lbgpu_step(1) -> lbgpu_download"},
+            "e2e": e2e,
             "gpu_launches": launches,
             "clocks": clk.summary(),
             "forms": forms,
