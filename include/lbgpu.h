@@ -136,6 +136,26 @@ int lbgpu_set_stream(lbgpu_handle* h, void* stream);
 int lbgpu_profile(lbgpu_handle* h, int32_t enable);
 int lbgpu_kernel_time(lbgpu_handle* h, int32_t which, double* total_ms, int64_t* launches);
 
+/* One timestep on caller-owned device buffers, allocating no device memory.
+ * It has no counterpart in the reference: it exists for callers that cannot
+ * let a library call cudaMalloc (a host framework whose memory pool already
+ * owns the GPU, or a caller that cannot take cudaMalloc's implicit device
+ * synchronisation while its other streams run).  The caller passes device
+ * pointers: f_in and f_out hold the populations in the kernels' SoA layout,
+ * element [c][q][site] with site = (x*gn[1] + y)*gn[2] + z (D2Q9: x*gn[1] + y),
+ * as doubles (LBGPU_FP64) or floats (LBGPU_FP32); mask is uint8 [site]
+ * (nonzero = solid) or NULL.  The work is queued on `stream` (a cudaStream_t,
+ * NULL for the legacy default stream) and `cfg->device` is used.
+ * The psi/density scratch is a 64 MiB static device array that every GPU
+ * loading this library holds until exit, so at most 64 MiB /
+ * (components * 2 * sizeof(arithmetic type)) sites are accepted (2,097,152
+ * two-component FP64 sites); larger lattices return LBGPU_E_INVALID.  The
+ * first call on a device looks up the array's address (make it before any
+ * stream capture).  All calls share the array: calls that overlap on the GPU
+ * race.  Error text goes to errbuf (may be NULL). */
+int lbgpu_step_noalloc(const lbgpu_config* cfg, const void* f_in, void* f_out, const uint8_t* mask,
+                       void* stream, char* errbuf, size_t errbuf_len);
+
 /* Number of kernel launches issued by this handle since creation. */
 int64_t lbgpu_launch_count(const lbgpu_handle* h);
 
