@@ -27,6 +27,7 @@ UNITS = {
     "lb_step_f64.cu": ["-fmad=false"],
     "lb_api.cu": ["-fmad=false"],
     "lb_step_lp.cu": [],
+    "lb_fused.cu": [],
     "lb_noalloc.cu": [],
 }
 

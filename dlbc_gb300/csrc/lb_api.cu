@@ -13,6 +13,7 @@
 #include <math.h>
 #include <stdint.h>
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
@@ -59,6 +60,9 @@ struct lbgpu_handle {
   size_t moments_bytes = 0;
   StepParams P{};
   bool uploaded = false;
+  // FP32/FP16 D3Q19 run the fused single-pass kernel; LBGPU_TWO_KERNEL=1 in
+  // the environment at lbgpu_create selects the two-kernel step instead
+  bool fused = false;
   // per-kernel event timing (lbgpu_profile)
   bool profiling = false;
   std::vector<lbk::StepEvents> ev_pending, ev_pool;
@@ -405,6 +409,10 @@ int lbgpu_create(const lbgpu_config* cfg, lbgpu_handle** out) {
   h->nyh = h->ny + 2 * kHalo;
   h->nzh = h->nz + 2 * h->hz;
   h->n = int64_t(h->nx) * h->ny * h->nz;
+  {
+    const char* tk = getenv("LBGPU_TWO_KERNEL");
+    h->fused = cfg->precision != LBGPU_FP64 && cfg->q == 19 && !(tk && tk[0] == '1');
+  }
 
   StepParams& P = h->P;
   P.nx = h->nx;
@@ -645,6 +653,9 @@ int lbgpu_step(lbgpu_handle* h, int32_t nsteps) {
     cudaError_t e;
     if (h->cfg.precision == LBGPU_FP64)
       e = lbk::launch_step_f64(h->Q, h->C, b, P, h->stream, &h->launches, evp);
+    else if (h->fused)
+      e = lbk::launch_fused(h->cfg.precision == LBGPU_FP16, h->C, b, P, h->stream, &h->launches, evp,
+                            h->cfg.device);
     else if (h->cfg.precision == LBGPU_FP32)
       e = lbk::launch_step_f32(h->Q, h->C, b, P, h->stream, &h->launches, evp);
     else

@@ -1,0 +1,396 @@
+// Fused single-pass D3Q19 timestep for the bandwidth forms (float
+// arithmetic; float or half-offset storage).
+//
+// The two-kernel step (lb_kernels.cuh) reads every population twice: once to
+// get the post-streaming densities for psi, once to collide.  This kernel
+// reads them once.  A CTA owns a TY x TZ tile of the (y, z) plane and marches
+// along x.  For each plane x+1 it pull-gathers the populations of the tile
+// and of a one-site ring around it, computes rho and psi there and keeps them
+// in a three-plane shared-memory ring; the tile's own gathered populations
+// stay in shared memory until the next iteration, when plane x is collided
+// with the psi stencil of planes x-1, x, x+1 and written out.  Ring sites are
+// re-read by the neighbouring tile (from L2); the populations of a site are
+// read from HBM once and written once.  With walls, the mask of planes
+// x .. x+2 over the tile and a two-site border is staged in shared memory so
+// the bounce-back tests never touch global memory.
+//
+// Scheduling is persistent and balanced: the (tile, x) plane-tiles are laid
+// out tile-major and split into equal contiguous ranges, one per CTA; every
+// run of consecutive x inside a range starts with two warm-up planes.
+//
+// Per-site arithmetic restates the reference (addShanChenForcePsi
+// force.d:238-309, distributeForce force.d:179-197,
+// precalculateWeightedVelocity collision.d:256-296, collideFieldsKernel
+// collision.d:190-219, eqDist eqdist.d:61-278) in float, re-associated where
+// that saves work: the Shan-Chen sum of component c1 is
+// -psi_c1 * sum_c2 g_c1c2 * S_c2 with S_c2 = sum_q w_q psi_c2(x + c_q) c_q
+// (the same mathematical value as the reference's per-term products), and
+// divisions by the density use a correctly rounded reciprocal.
+#pragma once
+
+#include <cuda_fp16.h>
+#include <stdint.h>
+
+#include "lb_kernels.cuh"
+
+namespace lbk {
+
+constexpr int kFusedTY = 8;
+constexpr int kFusedTZ = 32;
+constexpr int kFusedThreads = kFusedTY * kFusedTZ;
+constexpr int kFusedRY = kFusedTY + 2;   // tile + one-site ring
+constexpr int kFusedRZ = kFusedTZ + 2;
+constexpr int kFusedMY = kFusedTY + 4;   // tile + two-site border (mask)
+constexpr int kFusedMZ = kFusedTZ + 4;
+
+// float copies of the step parameters (no double arithmetic in the kernel)
+struct FusedParams {
+  int32_t nx, ny, nz;
+  int64_t n;
+  int32_t tiles_y, tiles_z;
+  int64_t work;            // tiles * nx plane-tiles
+  int32_t shan_chen, psi_form, eq_form, record_force;
+  float tau[2], inv_tau[2], omega[2], one_minus_omega[2];
+  float gcc[2][2], gwc[2], acc[3];
+  float rho0[2], scale[2], inv_scale[2];
+};
+
+template <typename T>
+struct FStore;
+template <>
+struct FStore<float> {
+  __device__ static __forceinline__ float load(const float* p, int, int, const FusedParams&) { return __ldg(p); }
+  __device__ static __forceinline__ void store(float* p, float v, int, int, const FusedParams&) { *p = v; }
+};
+template <>
+struct FStore<__half> {
+  __device__ static __forceinline__ float load(const __half* p, int c, int q, const FusedParams& P) {
+    return fmaf(P.scale[c], __half2float(__ldg(p)), weight<19, float>(q) * P.rho0[c]);
+  }
+  __device__ static __forceinline__ void store(__half* p, float v, int c, int q, const FusedParams& P) {
+    *p = __float2half_rn((v - weight<19, float>(q) * P.rho0[c]) * P.inv_scale[c]);
+  }
+};
+
+struct FusedShared {
+  float pops[2][2][19][kFusedThreads];   // [buffer][c][q][site in tile]
+  float psi[3][2][kFusedRY][kFusedRZ];   // [plane slot][c][y+1][z+1]
+  float rho[3][2][kFusedRY][kFusedRZ];
+  uint8_t solid[4][kFusedMY][kFusedMZ];  // mask, [plane slot][y+2][z+2]
+};
+
+__device__ __forceinline__ int wrap(int v, int n) { return v < 0 ? v + n : (v >= n ? v - n : v); }
+
+// acc += v * c for a lattice velocity c with components in {-1, 0, 1}
+__device__ __forceinline__ void stencil_acc(float (&acc)[3], int cx, int cy, int cz, float v) {
+  if (cx > 0) acc[0] += v;
+  if (cx < 0) acc[0] -= v;
+  if (cy > 0) acc[1] += v;
+  if (cy < 0) acc[1] -= v;
+  if (cz > 0) acc[2] += v;
+  if (cz < 0) acc[2] -= v;
+}
+
+// (y, z) offsets of a site and its 8 in-plane neighbours: off[cy+1][cz+1]
+struct YZ {
+  int off[3][3];
+};
+
+__device__ __forceinline__ YZ make_yz(int y, int z, const FusedParams& P) {
+  YZ r;
+  const int ys[3] = {wrap(y - 1, P.ny), y, wrap(y + 1, P.ny)};
+  const int zs[3] = {wrap(z - 1, P.nz), z, wrap(z + 1, P.nz)};
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = 0; b < 3; ++b) r.off[a][b] = ys[a] * P.nz + zs[b];
+  return r;
+}
+
+// Pull-gather one site of plane slot pl (planes[0..2] = offsets of x-1, x, x+1
+// of the gathered plane x).  ms, my, mz locate the site in the mask ring.
+template <typename T, bool WALLS, int C>
+__device__ __forceinline__ void fused_gather(const T* __restrict__ f, const FusedShared& sh, const FusedParams& P,
+                                             const int64_t planes[3], const YZ& yz, int mslot[3], int my, int mz,
+                                             bool solid, float pop[C][19]) {
+  const int64_t s = planes[1] + yz.off[1][1];
+  if (solid) {
+#pragma unroll
+    for (int c = 0; c < C; ++c)
+#pragma unroll
+      for (int q = 0; q < 19; ++q) pop[c][q] = FStore<T>::load(f + (int64_t(c) * 19 + q) * P.n + s, c, q, P);
+    return;
+  }
+#pragma unroll
+  for (int q = 0; q < 19; ++q) {
+    const int cx = Conn<19>::cx(q), cy = Conn<19>::cy(q), cz = Conn<19>::cz(q);
+    // upstream site x - c_q
+    const int64_t nb = planes[1 - cx] + yz.off[1 - cy][1 - cz];
+    bool bb = false;
+    if (WALLS && q > 0) bb = sh.solid[mslot[1 - cx]][my - cy][mz - cz];
+    const int b = Conn<19>::bounce(q);
+#pragma unroll
+    for (int c = 0; c < C; ++c) {
+      const T* src = bb ? f + (int64_t(c) * 19 + b) * P.n + s : f + (int64_t(c) * 19 + q) * P.n + nb;
+      pop[c][q] = FStore<T>::load(src, c, bb ? b : q, P);
+    }
+  }
+}
+
+template <typename T, int C, bool WALLS>
+__global__ void __launch_bounds__(kFusedThreads, 2)
+    k_fused(const T* __restrict__ f, T* __restrict__ fout, const uint8_t* __restrict__ mask,
+            double* __restrict__ force_out, FusedParams P) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  FusedShared& sh = *reinterpret_cast<FusedShared*>(smem_raw);
+  const int t = threadIdx.x;
+  const int ty = t / kFusedTZ, tz = t % kFusedTZ;
+  const int64_t plane_sz = int64_t(P.ny) * P.nz;
+  const int64_t w0 = P.work * blockIdx.x / gridDim.x;
+  const int64_t w1 = P.work * (blockIdx.x + 1) / gridDim.x;
+  int64_t w = w0;
+  while (w < w1) {
+    const int tile = int(w / P.nx);
+    const int xs = int(w - int64_t(tile) * P.nx);
+    const int run = int(min(w1 - w, int64_t(P.nx - xs)));
+    const int y0 = (tile / P.tiles_z) * kFusedTY, z0 = (tile % P.tiles_z) * kFusedTZ;
+    const int tyv = min(kFusedTY, P.ny - y0), tzv = min(kFusedTZ, P.nz - z0);
+    const bool active = ty < tyv && tz < tzv;
+    // interior site offsets and this thread's ring site (if any)
+    const YZ yz_in = make_yz(y0 + ty, z0 + tz, P);
+    const int ring = 2 * (tzv + 2) + 2 * tyv;
+    int rry = 0, rrz = 0;
+    const bool has_ring = t < ring;
+    if (has_ring) {
+      if (t < tzv + 2) {
+        rry = -1;
+        rrz = t - 1;
+      } else if (t < 2 * (tzv + 2)) {
+        rry = tyv;
+        rrz = t - (tzv + 2) - 1;
+      } else {
+        const int k = t - 2 * (tzv + 2);
+        rry = k >> 1;
+        rrz = (k & 1) ? tzv : -1;
+      }
+    }
+    const YZ yz_ring = make_yz(wrap(y0 + rry, P.ny), wrap(z0 + rrz, P.nz), P);
+
+    // mask ring loader: plane x into slot ms, tile + two-site border
+    auto load_mask = [&](int ms, int x) {
+      if (!WALLS) return;
+      const int64_t base = int64_t(x) * plane_sz;
+      for (int i = t; i < kFusedMY * kFusedMZ; i += kFusedThreads) {
+        const int my = i / kFusedMZ, mz = i % kFusedMZ;
+        if (my > tyv + 3 || mz > tzv + 3) continue;
+        const int y = wrap(y0 + my - 2, P.ny), z = wrap(z0 + mz - 2, P.nz);
+        sh.solid[ms][my][mz] = __ldg(mask + base + int64_t(y) * P.nz + z);
+      }
+    };
+    // rho/psi of plane xg into psi slot ps (and the tile's populations into
+    // buffer keep, unless keep < 0); the mask of planes xg-1..xg+1 must be in
+    // mask slots mslot[0..2]
+    auto gather_plane = [&](int ps, int xg, int keep, int mslot[3]) {
+      const int64_t planes[3] = {int64_t(wrap(xg - 1, P.nx)) * plane_sz, int64_t(xg) * plane_sz,
+                                 int64_t(wrap(xg + 1, P.nx)) * plane_sz};
+      if (active) {
+        const bool solid = WALLS && sh.solid[mslot[1]][ty + 2][tz + 2];
+        float pop[C][19];
+        fused_gather<T, WALLS, C>(f, sh, P, planes, yz_in, mslot, ty + 2, tz + 2, solid, pop);
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+          const float den = density<19, float>(pop[c]);
+          sh.rho[ps][c][ty + 1][tz + 1] = den;
+          sh.psi[ps][c][ty + 1][tz + 1] = P.psi_form ? 1.0f - __expf(-den) : den;
+          if (keep >= 0) {
+#pragma unroll
+            for (int q = 0; q < 19; ++q) sh.pops[keep][c][q][t] = pop[c][q];
+          }
+        }
+      }
+      if (has_ring) {
+        const bool solid = WALLS && sh.solid[mslot[1]][rry + 2][rrz + 2];
+        float pop[C][19];
+        fused_gather<T, WALLS, C>(f, sh, P, planes, yz_ring, mslot, rry + 2, rrz + 2, solid, pop);
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+          const float den = density<19, float>(pop[c]);
+          sh.rho[ps][c][rry + 1][rrz + 1] = den;
+          sh.psi[ps][c][rry + 1][rrz + 1] = P.psi_form ? 1.0f - __expf(-den) : den;
+        }
+      }
+    };
+
+    // warm-up: mask of planes xs-2 .. xs+1; rho/psi of xs-1; rho/psi +
+    // populations of xs
+    __syncthreads();
+    load_mask(0, wrap(xs - 2, P.nx));
+    load_mask(1, wrap(xs - 1, P.nx));
+    load_mask(2, xs);
+    load_mask(3, wrap(xs + 1, P.nx));
+    __syncthreads();
+    {
+      int m0[3] = {0, 1, 2};
+      gather_plane(0, wrap(xs - 1, P.nx), -1, m0);
+      int m1[3] = {1, 2, 3};
+      gather_plane(1, xs, 0, m1);
+    }
+    int cur = 0;
+    for (int k = 0; k < run; ++k) {
+      const int x = xs + k;
+      const int sm = k % 3, s0 = (k + 1) % 3, sp = (k + 2) % 3;  // psi slots of x-1, x, x+1
+      // mask slots: plane p is in slot (p - xs + 2) % 4, so x-1, x, x+1, x+2
+      // are in (k+1)%4, (k+2)%4, (k+3)%4, k%4
+      int mg[3] = {(k + 2) % 4, (k + 3) % 4, k % 4};  // planes x, x+1, x+2
+      __syncthreads();  // psi slot sp, pops buffer 1-cur and mask slot k%4 (plane x-2) are free
+      load_mask(k % 4, wrap(x + 2, P.nx));
+      __syncthreads();
+      gather_plane(sp, wrap(x + 1, P.nx), 1 - cur, mg);
+      __syncthreads();
+      if (active) {
+        const int64_t s = int64_t(x) * plane_sz + yz_in.off[1][1];
+        const int c1y = ty + 1, c1z = tz + 1;
+        const bool solid = WALLS && sh.solid[(k + 2) % 4][ty + 2][tz + 2];
+        float den[C];
+#pragma unroll
+        for (int c = 0; c < C; ++c) den[c] = sh.rho[s0][c][c1y][c1z];
+        if (solid) {
+#pragma unroll
+          for (int c = 0; c < C; ++c)
+#pragma unroll
+            for (int q = 0; q < 19; ++q)
+              FStore<T>::store(fout + (int64_t(c) * 19 + q) * P.n + s, sh.pops[cur][c][q][t], c, q, P);
+          if (P.record_force) {
+            float tot = den[0];
+            if (C > 1) tot = tot + den[1];
+#pragma unroll
+            for (int c = 0; c < C; ++c) {
+              const bool bad = tot == 0.f || isnan(tot) || isinf(den[c]) || isnan(den[c]);
+              for (int vd = 0; vd < 3; ++vd) force_out[(int64_t(c) * P.n + s) * 3 + vd] = bad ? double(NAN) : 0.0;
+            }
+          }
+        } else {
+          const int pslot[3] = {sm, s0, sp};                       // by cx + 1
+          const int mslot[3] = {(k + 1) % 4, (k + 2) % 4, (k + 3) % 4};  // mask of x-1, x, x+1
+          // --- Shan-Chen force: S_c = sum_q w_q psi_c(x + c_q) c_q, a solid
+          // neighbour contributing the site's own psi (force.d:273)
+          float F[C][3];
+#pragma unroll
+          for (int c = 0; c < C; ++c) F[c][0] = F[c][1] = F[c][2] = 0.f;
+          if (P.shan_chen) {
+            float S[C][3];
+            float own[C];
+#pragma unroll
+            for (int c = 0; c < C; ++c) {
+              own[c] = sh.psi[s0][c][c1y][c1z];
+              float a[3] = {0.f, 0.f, 0.f}, d[3] = {0.f, 0.f, 0.f};  // axis and diagonal sums
+#pragma unroll
+              for (int q = 1; q < 19; ++q) {
+                const int cx = Conn<19>::cx(q), cy = Conn<19>::cy(q), cz = Conn<19>::cz(q);
+                float v = sh.psi[pslot[cx + 1]][c][c1y + cy][c1z + cz];
+                if (WALLS && sh.solid[mslot[cx + 1]][ty + 2 + cy][tz + 2 + cz]) v = own[c];
+                if (Conn<19>::wclass(q) == 1)
+                  stencil_acc(a, cx, cy, cz, v);
+                else
+                  stencil_acc(d, cx, cy, cz, v);
+              }
+#pragma unroll
+              for (int vd = 0; vd < 3; ++vd) S[c][vd] = (1.0f / 18.0f) * a[vd] + (1.0f / 36.0f) * d[vd];
+            }
+#pragma unroll
+            for (int f1 = 0; f1 < C; ++f1) {
+              float g[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+              for (int f2 = 0; f2 < C; ++f2) {
+                const float cc = P.gcc[f1][f2];
+#pragma unroll
+                for (int vd = 0; vd < 3; ++vd) g[vd] = fmaf(cc, S[f2][vd], g[vd]);
+              }
+#pragma unroll
+              for (int vd = 0; vd < 3; ++vd) F[f1][vd] = -own[f1] * g[vd];
+              if (WALLS) {
+                const float wc = P.gwc[f1];
+                if (wc != 0.f) {
+                  float a[3] = {0.f, 0.f, 0.f}, d[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+                  for (int q = 1; q < 19; ++q) {
+                    const int cx = Conn<19>::cx(q), cy = Conn<19>::cy(q), cz = Conn<19>::cz(q);
+                    if (!sh.solid[mslot[cx + 1]][ty + 2 + cy][tz + 2 + cz]) continue;
+                    const float v = sh.rho[pslot[cx + 1]][f1][c1y + cy][c1z + cz];
+                    if (Conn<19>::wclass(q) == 1)
+                      stencil_acc(a, cx, cy, cz, v);
+                    else
+                      stencil_acc(d, cx, cy, cz, v);
+                  }
+#pragma unroll
+                  for (int vd = 0; vd < 3; ++vd)
+                    F[f1][vd] -= own[f1] * wc * ((1.0f / 18.0f) * a[vd] + (1.0f / 36.0f) * d[vd]);
+                }
+              }
+            }
+          }
+          float tot = den[0];
+          if (C > 1) tot = tot + den[1];
+          {
+#pragma unroll
+            for (int c = 0; c < C; ++c) {
+              const bool bad = tot == 0.f || isnan(tot) || isinf(den[c]) || isnan(den[c]);
+              if (bad) F[c][0] = F[c][1] = F[c][2] = NAN;
+            }
+          }
+          if (P.record_force) {
+#pragma unroll
+            for (int c = 0; c < C; ++c)
+#pragma unroll
+              for (int vd = 0; vd < 3; ++vd) force_out[(int64_t(c) * P.n + s) * 3 + vd] = double(F[c][vd]);
+          }
+          // --- BDist2 weighted velocity
+          float wv[3] = {0.f, 0.f, 0.f};
+          if (P.eq_form == 2) {
+            const float rtot = __frcp_rn(tot);
+#pragma unroll
+            for (int vd = 0; vd < 3; ++vd) {
+              float a = 0.f;
+#pragma unroll
+              for (int c = 0; c < C; ++c) {
+                float m = 0.f;
+#pragma unroll
+                for (int q = 1; q < 19; ++q) {
+                  const int cv = cvel<19>(q, vd);
+                  if (cv > 0) m += sh.pops[cur][c][q][t];
+                  if (cv < 0) m -= sh.pops[cur][c][q][t];
+                }
+                a = fmaf(m, P.inv_tau[c], a);
+              }
+              wv[vd] = a * rtot;
+            }
+          }
+          // --- collision
+#pragma unroll
+          for (int c = 0; c < C; ++c) {
+            float pop[19];
+#pragma unroll
+            for (int q = 0; q < 19; ++q) pop[q] = sh.pops[cur][c][q][t];
+            const float rden = __frcp_rn(den[c]);
+            float dv[3];
+#pragma unroll
+            for (int vd = 0; vd < 3; ++vd) dv[vd] = P.tau[c] * fmaf(F[c][vd], rden, P.acc[vd]) + wv[vd];
+            float eq[19];
+            if (P.eq_form == 2)
+              eq_bdist2<19, float>(dv, den[c], eq);
+            else
+              eq_poly<19, float>(pop, dv, den[c], P.eq_form == 1, eq);
+            const float omega = P.omega[c], omo = P.one_minus_omega[c];
+#pragma unroll
+            for (int q = 0; q < 19; ++q)
+              FStore<T>::store(fout + (int64_t(c) * 19 + q) * P.n + s, pop[q] * omo + omega * eq[q], c, q, P);
+          }
+        }
+      }
+      cur = 1 - cur;
+    }
+    w += run;
+  }
+}
+
+}  // namespace lbk

@@ -34,3 +34,12 @@ cudaError_t launch_step_f16(int q, int c, const StepBuffers& b, const StepParams
                             int64_t* launches, const StepEvents* ev);
 
 }  // namespace lbk
+
+namespace lbk {
+
+// Fused single-pass D3Q19 step (lb_fused.cuh) for the float-arithmetic
+// forms.  `half_storage` selects half offsets instead of float storage.
+cudaError_t launch_fused(bool half_storage, int c, const StepBuffers& b, const StepParams& P, cudaStream_t stream,
+                         int64_t* launches, const StepEvents* ev, int device);
+
+}  // namespace lbk

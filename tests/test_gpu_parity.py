@@ -176,3 +176,47 @@ def test_launch_count_and_errors():
     assert g.launch_count - n0 == 10
     with pytest.raises(lbgpu.LbgpuError):
         g.force()  # force not recorded
+
+
+def _run_form(p, steps, precision, two_kernel, record_force=False):
+    import os
+    old = os.environ.get("LBGPU_TWO_KERNEL")
+    os.environ["LBGPU_TWO_KERNEL"] = "1" if two_kernel else "0"
+    try:
+        fl, m = init.init_fields(p)
+        g = lbgpu.GPULattice(p, precision=precision)
+    finally:
+        if old is None:
+            del os.environ["LBGPU_TWO_KERNEL"]
+        else:
+            os.environ["LBGPU_TWO_KERNEL"] = old
+    g.upload(fl, m)
+    if record_force:
+        g.set_record_force(True)
+    g.step(steps)
+    out = g.population()
+    f = g.force() if record_force else None
+    return out, f
+
+
+@pytest.mark.parametrize("precision", [lbgpu.FP32, lbgpu.FP16])
+@pytest.mark.parametrize("case", ["spinodal", "walls", "partial_tiles"])
+def test_fused_step_matches_two_kernel_step(precision, case):
+    """The fused single-pass kernel computes the same per-site arithmetic as
+    the two-kernel step; only FMA contraction may differ (float)."""
+    if case == "spinodal":
+        p = spinodal((24, 20, 40), eq="BDist2")
+    elif case == "walls":
+        p = droplet_channel((20, 18, 36), radius=5.0, acc=1e-3, gwc=(0.25, -0.15))
+    else:
+        p = spinodal((7, 13, 37), eq="SecondOrder")
+    a, fa = _run_form(p, 30, precision, two_kernel=False, record_force=True)
+    b, fb = _run_form(p, 30, precision, two_kernel=True, record_force=True)
+    tol = 2e-6 if precision == lbgpu.FP32 else 2e-3
+    # the force is a cancelling sum of terms w_q*psi*psi*g ~ 0.03: compare it
+    # on that scale (the fused kernel sums the stencil in another order)
+    ftol = 3e-7 if precision == lbgpu.FP32 else 3e-4
+    for c in range(2):
+        scale = np.abs(b[c]).max()
+        assert np.abs(a[c] - b[c]).max() <= tol * scale, (c, np.abs(a[c] - b[c]).max())
+        assert np.abs(fa[c] - fb[c]).max() <= ftol, (c, np.abs(fa[c] - fb[c]).max())
