@@ -435,6 +435,9 @@ int lbgpu_create(const lbgpu_config* cfg, lbgpu_handle** out) {
     P.inv_scale[c] = 1.f;
   }
   for (int i = 0; i < 3; ++i) P.acc[i] = i < cfg->d ? cfg->global_acc[i] : 0.0;
+  P.unit_tau = 1;
+  for (int c = 0; c < h->C; ++c)
+    if (cfg->tau[c] != 1.0) P.unit_tau = 0;
 
   e = cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking);
   h->stream = h->own_stream;

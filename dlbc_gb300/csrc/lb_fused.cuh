@@ -11,8 +11,8 @@
 // with the psi stencil of planes x-1, x, x+1 and written out.  Ring sites are
 // re-read by the neighbouring tile (from L2); the populations of a site are
 // read from HBM once and written once.  With walls, the mask of planes
-// x .. x+2 over the tile and a two-site border is staged in shared memory so
-// the bounce-back tests never touch global memory.
+// x-1 .. x+3 over the tile and a two-site border is staged in shared memory
+// (one plane ahead) so the bounce-back tests never touch global memory.
 //
 // Scheduling is persistent and balanced: the (tile, x) plane-tiles are laid
 // out tile-major and split into equal contiguous ranges, one per CTA; every
@@ -76,7 +76,7 @@ struct FusedShared {
   float pops[2][2][19][kFusedThreads];   // [buffer][c][q][site in tile]
   float psi[3][2][kFusedRY][kFusedRZ];   // [plane slot][c][y+1][z+1]
   float rho[3][2][kFusedRY][kFusedRZ];
-  uint8_t solid[4][kFusedMY][kFusedMZ];  // mask, [plane slot][y+2][z+2]
+  uint8_t solid[5][kFusedMY][kFusedMZ];  // mask, [plane slot][y+2][z+2]
 };
 
 __device__ __forceinline__ int wrap(int v, int n) { return v < 0 ? v + n : (v >= n ? v - n : v); }
@@ -114,26 +114,20 @@ __device__ __forceinline__ void fused_gather(const T* __restrict__ f, const Fuse
                                              const int64_t planes[3], const YZ& yz, int mslot[3], int my, int mz,
                                              bool solid, float pop[C][19]) {
   const int64_t s = planes[1] + yz.off[1][1];
-  if (solid) {
-#pragma unroll
-    for (int c = 0; c < C; ++c)
-#pragma unroll
-      for (int q = 0; q < 19; ++q) pop[c][q] = FStore<T>::load(f + (int64_t(c) * 19 + q) * P.n + s, c, q, P);
-    return;
-  }
+  // branch-free (warps straddling a wall must not run two code paths):
+  // a solid site keeps its own populations, a fluid site pulls from x - c_q
+  // or, when that site is solid, bounces back its own opposite population
 #pragma unroll
   for (int q = 0; q < 19; ++q) {
     const int cx = Conn<19>::cx(q), cy = Conn<19>::cy(q), cz = Conn<19>::cz(q);
-    // upstream site x - c_q
     const int64_t nb = planes[1 - cx] + yz.off[1 - cy][1 - cz];
     bool bb = false;
-    if (WALLS && q > 0) bb = sh.solid[mslot[1 - cx]][my - cy][mz - cz];
+    if (WALLS && q > 0) bb = sh.solid[mslot[1 - cx]][my - cy][mz - cz] && !solid;
     const int b = Conn<19>::bounce(q);
+    const int64_t site = (WALLS && (solid || bb)) ? s : nb;
+    const int qq = bb ? b : q;
 #pragma unroll
-    for (int c = 0; c < C; ++c) {
-      const T* src = bb ? f + (int64_t(c) * 19 + b) * P.n + s : f + (int64_t(c) * 19 + q) * P.n + nb;
-      pop[c][q] = FStore<T>::load(src, c, bb ? b : q, P);
-    }
+    for (int c = 0; c < C; ++c) pop[c][q] = FStore<T>::load(f + (int64_t(c) * 19 + qq) * P.n + site, c, qq, P);
   }
 }
 
@@ -221,13 +215,10 @@ __global__ void __launch_bounds__(kFusedThreads, 2)
       }
     };
 
-    // warm-up: mask of planes xs-2 .. xs+1; rho/psi of xs-1; rho/psi +
-    // populations of xs
+    // warm-up: mask of planes xs-2 .. xs+2 (plane p lives in mask slot
+    // (p - xs + 2) % 5); rho/psi of xs-1; rho/psi + populations of xs
     __syncthreads();
-    load_mask(0, wrap(xs - 2, P.nx));
-    load_mask(1, wrap(xs - 1, P.nx));
-    load_mask(2, xs);
-    load_mask(3, wrap(xs + 1, P.nx));
+    for (int j = 0; j < 5; ++j) load_mask(j, wrap(xs - 2 + j, P.nx));
     __syncthreads();
     {
       int m0[3] = {0, 1, 2};
@@ -239,151 +230,137 @@ __global__ void __launch_bounds__(kFusedThreads, 2)
     for (int k = 0; k < run; ++k) {
       const int x = xs + k;
       const int sm = k % 3, s0 = (k + 1) % 3, sp = (k + 2) % 3;  // psi slots of x-1, x, x+1
-      // mask slots: plane p is in slot (p - xs + 2) % 4, so x-1, x, x+1, x+2
-      // are in (k+1)%4, (k+2)%4, (k+3)%4, k%4
-      int mg[3] = {(k + 2) % 4, (k + 3) % 4, k % 4};  // planes x, x+1, x+2
-      __syncthreads();  // psi slot sp, pops buffer 1-cur and mask slot k%4 (plane x-2) are free
-      load_mask(k % 4, wrap(x + 2, P.nx));
-      __syncthreads();
+      // mask slots of planes x-1, x, x+1, x+2: (k+1)%5 .. (k+4)%5
+      int mg[3] = {(k + 2) % 5, (k + 3) % 5, (k + 4) % 5};  // planes x, x+1, x+2
+      __syncthreads();  // psi slot sp, pops buffer 1-cur and mask slot k%5 (plane x-2) are free
+      load_mask(k % 5, wrap(x + 3, P.nx));  // for the next iteration
       gather_plane(sp, wrap(x + 1, P.nx), 1 - cur, mg);
       __syncthreads();
       if (active) {
         const int64_t s = int64_t(x) * plane_sz + yz_in.off[1][1];
         const int c1y = ty + 1, c1z = tz + 1;
-        const bool solid = WALLS && sh.solid[(k + 2) % 4][ty + 2][tz + 2];
+        // branch-free: solid sites compute like fluid ones and store their
+        // own populations (warps straddling a wall run one code path)
+        const bool solid = WALLS && sh.solid[(k + 2) % 5][ty + 2][tz + 2];
         float den[C];
 #pragma unroll
         for (int c = 0; c < C; ++c) den[c] = sh.rho[s0][c][c1y][c1z];
-        if (solid) {
+        const int pslot[3] = {sm, s0, sp};                              // by cx + 1
+        const int mslot[3] = {(k + 1) % 5, (k + 2) % 5, (k + 3) % 5};  // mask of x-1, x, x+1
+        // --- Shan-Chen force: S_c = sum_q w_q psi_c(x + c_q) c_q, a solid
+        // neighbour contributing the site's own psi (force.d:273)
+        float F[C][3];
+#pragma unroll
+        for (int c = 0; c < C; ++c) F[c][0] = F[c][1] = F[c][2] = 0.f;
+        if (P.shan_chen) {
+          float S[C][3];
+          float own[C];
+#pragma unroll
+          for (int c = 0; c < C; ++c) {
+            own[c] = sh.psi[s0][c][c1y][c1z];
+            float a[3] = {0.f, 0.f, 0.f}, d[3] = {0.f, 0.f, 0.f};  // axis and diagonal sums
+#pragma unroll
+            for (int q = 1; q < 19; ++q) {
+              const int cx = Conn<19>::cx(q), cy = Conn<19>::cy(q), cz = Conn<19>::cz(q);
+              float v = sh.psi[pslot[cx + 1]][c][c1y + cy][c1z + cz];
+              if (WALLS && sh.solid[mslot[cx + 1]][ty + 2 + cy][tz + 2 + cz]) v = own[c];
+              if (Conn<19>::wclass(q) == 1)
+                stencil_acc(a, cx, cy, cz, v);
+              else
+                stencil_acc(d, cx, cy, cz, v);
+            }
+#pragma unroll
+            for (int vd = 0; vd < 3; ++vd) S[c][vd] = (1.0f / 18.0f) * a[vd] + (1.0f / 36.0f) * d[vd];
+          }
+#pragma unroll
+          for (int f1 = 0; f1 < C; ++f1) {
+            float g[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+            for (int f2 = 0; f2 < C; ++f2) {
+              const float cc = P.gcc[f1][f2];
+#pragma unroll
+              for (int vd = 0; vd < 3; ++vd) g[vd] = fmaf(cc, S[f2][vd], g[vd]);
+            }
+#pragma unroll
+            for (int vd = 0; vd < 3; ++vd) F[f1][vd] = -own[f1] * g[vd];
+            if (WALLS) {
+              const float wc = P.gwc[f1];
+              if (wc != 0.f) {
+                float a[3] = {0.f, 0.f, 0.f}, d[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+                for (int q = 1; q < 19; ++q) {
+                  const int cx = Conn<19>::cx(q), cy = Conn<19>::cy(q), cz = Conn<19>::cz(q);
+                  const float v = sh.solid[mslot[cx + 1]][ty + 2 + cy][tz + 2 + cz]
+                                      ? sh.rho[pslot[cx + 1]][f1][c1y + cy][c1z + cz]
+                                      : 0.f;
+                  if (Conn<19>::wclass(q) == 1)
+                    stencil_acc(a, cx, cy, cz, v);
+                  else
+                    stencil_acc(d, cx, cy, cz, v);
+                }
+#pragma unroll
+                for (int vd = 0; vd < 3; ++vd)
+                  F[f1][vd] -= own[f1] * wc * ((1.0f / 18.0f) * a[vd] + (1.0f / 36.0f) * d[vd]);
+              }
+            }
+          }
+        }
+        float tot = den[0];
+        if (C > 1) tot = tot + den[1];
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+          // distributeForce with no distributed force: only its NaN cases matter
+          const bool bad = tot == 0.f || isnan(tot) || isinf(den[c]) || isnan(den[c]);
+          if (bad) F[c][0] = F[c][1] = F[c][2] = NAN;
+          if (solid && !bad) F[c][0] = F[c][1] = F[c][2] = 0.f;
+        }
+        if (P.record_force) {
 #pragma unroll
           for (int c = 0; c < C; ++c)
 #pragma unroll
-            for (int q = 0; q < 19; ++q)
-              FStore<T>::store(fout + (int64_t(c) * 19 + q) * P.n + s, sh.pops[cur][c][q][t], c, q, P);
-          if (P.record_force) {
-            float tot = den[0];
-            if (C > 1) tot = tot + den[1];
+            for (int vd = 0; vd < 3; ++vd) force_out[(int64_t(c) * P.n + s) * 3 + vd] = double(F[c][vd]);
+        }
+        // --- BDist2 weighted velocity
+        float wv[3] = {0.f, 0.f, 0.f};
+        if (P.eq_form == 2) {
+          const float rtot = __frcp_rn(tot);
+#pragma unroll
+          for (int vd = 0; vd < 3; ++vd) {
+            float a = 0.f;
 #pragma unroll
             for (int c = 0; c < C; ++c) {
-              const bool bad = tot == 0.f || isnan(tot) || isinf(den[c]) || isnan(den[c]);
-              for (int vd = 0; vd < 3; ++vd) force_out[(int64_t(c) * P.n + s) * 3 + vd] = bad ? double(NAN) : 0.0;
-            }
-          }
-        } else {
-          const int pslot[3] = {sm, s0, sp};                       // by cx + 1
-          const int mslot[3] = {(k + 1) % 4, (k + 2) % 4, (k + 3) % 4};  // mask of x-1, x, x+1
-          // --- Shan-Chen force: S_c = sum_q w_q psi_c(x + c_q) c_q, a solid
-          // neighbour contributing the site's own psi (force.d:273)
-          float F[C][3];
-#pragma unroll
-          for (int c = 0; c < C; ++c) F[c][0] = F[c][1] = F[c][2] = 0.f;
-          if (P.shan_chen) {
-            float S[C][3];
-            float own[C];
-#pragma unroll
-            for (int c = 0; c < C; ++c) {
-              own[c] = sh.psi[s0][c][c1y][c1z];
-              float a[3] = {0.f, 0.f, 0.f}, d[3] = {0.f, 0.f, 0.f};  // axis and diagonal sums
+              float m = 0.f;
 #pragma unroll
               for (int q = 1; q < 19; ++q) {
-                const int cx = Conn<19>::cx(q), cy = Conn<19>::cy(q), cz = Conn<19>::cz(q);
-                float v = sh.psi[pslot[cx + 1]][c][c1y + cy][c1z + cz];
-                if (WALLS && sh.solid[mslot[cx + 1]][ty + 2 + cy][tz + 2 + cz]) v = own[c];
-                if (Conn<19>::wclass(q) == 1)
-                  stencil_acc(a, cx, cy, cz, v);
-                else
-                  stencil_acc(d, cx, cy, cz, v);
+                const int cv = cvel<19>(q, vd);
+                if (cv > 0) m += sh.pops[cur][c][q][t];
+                if (cv < 0) m -= sh.pops[cur][c][q][t];
               }
-#pragma unroll
-              for (int vd = 0; vd < 3; ++vd) S[c][vd] = (1.0f / 18.0f) * a[vd] + (1.0f / 36.0f) * d[vd];
+              a = fmaf(m, P.inv_tau[c], a);
             }
-#pragma unroll
-            for (int f1 = 0; f1 < C; ++f1) {
-              float g[3] = {0.f, 0.f, 0.f};
-#pragma unroll
-              for (int f2 = 0; f2 < C; ++f2) {
-                const float cc = P.gcc[f1][f2];
-#pragma unroll
-                for (int vd = 0; vd < 3; ++vd) g[vd] = fmaf(cc, S[f2][vd], g[vd]);
-              }
-#pragma unroll
-              for (int vd = 0; vd < 3; ++vd) F[f1][vd] = -own[f1] * g[vd];
-              if (WALLS) {
-                const float wc = P.gwc[f1];
-                if (wc != 0.f) {
-                  float a[3] = {0.f, 0.f, 0.f}, d[3] = {0.f, 0.f, 0.f};
-#pragma unroll
-                  for (int q = 1; q < 19; ++q) {
-                    const int cx = Conn<19>::cx(q), cy = Conn<19>::cy(q), cz = Conn<19>::cz(q);
-                    if (!sh.solid[mslot[cx + 1]][ty + 2 + cy][tz + 2 + cz]) continue;
-                    const float v = sh.rho[pslot[cx + 1]][f1][c1y + cy][c1z + cz];
-                    if (Conn<19>::wclass(q) == 1)
-                      stencil_acc(a, cx, cy, cz, v);
-                    else
-                      stencil_acc(d, cx, cy, cz, v);
-                  }
-#pragma unroll
-                  for (int vd = 0; vd < 3; ++vd)
-                    F[f1][vd] -= own[f1] * wc * ((1.0f / 18.0f) * a[vd] + (1.0f / 36.0f) * d[vd]);
-                }
-              }
-            }
+            wv[vd] = a * rtot;
           }
-          float tot = den[0];
-          if (C > 1) tot = tot + den[1];
-          {
+        }
+        // --- collision; solid sites store their populations unchanged
 #pragma unroll
-            for (int c = 0; c < C; ++c) {
-              const bool bad = tot == 0.f || isnan(tot) || isinf(den[c]) || isnan(den[c]);
-              if (bad) F[c][0] = F[c][1] = F[c][2] = NAN;
-            }
-          }
-          if (P.record_force) {
+        for (int c = 0; c < C; ++c) {
+          float pop[19];
 #pragma unroll
-            for (int c = 0; c < C; ++c)
+          for (int q = 0; q < 19; ++q) pop[q] = sh.pops[cur][c][q][t];
+          const float rden = __frcp_rn(den[c]);
+          float dv[3];
 #pragma unroll
-              for (int vd = 0; vd < 3; ++vd) force_out[(int64_t(c) * P.n + s) * 3 + vd] = double(F[c][vd]);
-          }
-          // --- BDist2 weighted velocity
-          float wv[3] = {0.f, 0.f, 0.f};
-          if (P.eq_form == 2) {
-            const float rtot = __frcp_rn(tot);
+          for (int vd = 0; vd < 3; ++vd) dv[vd] = P.tau[c] * fmaf(F[c][vd], rden, P.acc[vd]) + wv[vd];
+          float eq[19];
+          if (P.eq_form == 2)
+            eq_bdist2<19, float>(dv, den[c], eq);
+          else
+            eq_poly<19, float>(pop, dv, den[c], P.eq_form == 1, eq);
+          const float omega = P.omega[c], omo = P.one_minus_omega[c];
 #pragma unroll
-            for (int vd = 0; vd < 3; ++vd) {
-              float a = 0.f;
-#pragma unroll
-              for (int c = 0; c < C; ++c) {
-                float m = 0.f;
-#pragma unroll
-                for (int q = 1; q < 19; ++q) {
-                  const int cv = cvel<19>(q, vd);
-                  if (cv > 0) m += sh.pops[cur][c][q][t];
-                  if (cv < 0) m -= sh.pops[cur][c][q][t];
-                }
-                a = fmaf(m, P.inv_tau[c], a);
-              }
-              wv[vd] = a * rtot;
-            }
-          }
-          // --- collision
-#pragma unroll
-          for (int c = 0; c < C; ++c) {
-            float pop[19];
-#pragma unroll
-            for (int q = 0; q < 19; ++q) pop[q] = sh.pops[cur][c][q][t];
-            const float rden = __frcp_rn(den[c]);
-            float dv[3];
-#pragma unroll
-            for (int vd = 0; vd < 3; ++vd) dv[vd] = P.tau[c] * fmaf(F[c][vd], rden, P.acc[vd]) + wv[vd];
-            float eq[19];
-            if (P.eq_form == 2)
-              eq_bdist2<19, float>(dv, den[c], eq);
-            else
-              eq_poly<19, float>(pop, dv, den[c], P.eq_form == 1, eq);
-            const float omega = P.omega[c], omo = P.one_minus_omega[c];
-#pragma unroll
-            for (int q = 0; q < 19; ++q)
-              FStore<T>::store(fout + (int64_t(c) * 19 + q) * P.n + s, pop[q] * omo + omega * eq[q], c, q, P);
+          for (int q = 0; q < 19; ++q) {
+            const float v = pop[q] * omo + omega * eq[q];
+            FStore<T>::store(fout + (int64_t(c) * 19 + q) * P.n + s, solid ? pop[q] : v, c, q, P);
           }
         }
       }

@@ -30,6 +30,10 @@ struct StepParams {
   int32_t psi_form;
   int32_t eq_form;
   int32_t record_force;
+  // every component has tau == 1: m/tau, tau*x and pop*(1-omega) + omega*eq
+  // reduce exactly to m, x and eq (for finite populations), which saves
+  // about a quarter of the FP64 work of k_collide
+  int32_t unit_tau;
   double tau[2];
   double omega[2];        // 1/tau
   double one_minus_omega[2];
@@ -268,11 +272,12 @@ __global__ void __launch_bounds__(128) k_collide(const T* __restrict__ f, T* __r
 
   // --- BDist2 weighted velocity (collision.d:256-296)
   R wv[3] = {R(0), R(0), R(0)};
+  const bool unit = P.unit_tau != 0;
   if (P.eq_form == 2) {
 #pragma unroll
     for (int vd = 0; vd < D; ++vd) {
-      R acc = moment<Q, R>(pop[0], vd) / R(P.tau[0]);
-      if (C > 1) acc = acc + moment<Q, R>(pop[1], vd) / R(P.tau[1]);
+      R acc = unit ? moment<Q, R>(pop[0], vd) : moment<Q, R>(pop[0], vd) / R(P.tau[0]);
+      if (C > 1) acc = acc + (unit ? moment<Q, R>(pop[1], vd) : moment<Q, R>(pop[1], vd) / R(P.tau[1]));
       wv[vd] = acc;
     }
     R tot = den[0];
@@ -288,7 +293,8 @@ __global__ void __launch_bounds__(128) k_collide(const T* __restrict__ f, T* __r
     R dv[3];
 #pragma unroll
     for (int vd = 0; vd < D; ++vd) {
-      dv[vd] = tau * (R(P.acc[vd]) + F[c][vd] / den[c]);
+      const R a = R(P.acc[vd]) + F[c][vd] / den[c];
+      dv[vd] = unit ? a : tau * a;
       if (P.eq_form == 2) dv[vd] = dv[vd] + wv[vd];
     }
     R eq[Q];
@@ -299,9 +305,14 @@ __global__ void __launch_bounds__(128) k_collide(const T* __restrict__ f, T* __r
     const R omega = R(P.omega[c]);
     const R omo = R(P.one_minus_omega[c]);
     T* oc = fout + int64_t(c) * Q * P.n;
+    if (unit) {
 #pragma unroll
-    for (int q = 0; q < Q; ++q)
-      Store<T, R, Q>::store(oc + int64_t(q) * P.n + s, pop[c][q] * omo + omega * eq[q], c, q, P);
+      for (int q = 0; q < Q; ++q) Store<T, R, Q>::store(oc + int64_t(q) * P.n + s, eq[q], c, q, P);
+    } else {
+#pragma unroll
+      for (int q = 0; q < Q; ++q)
+        Store<T, R, Q>::store(oc + int64_t(q) * P.n + s, pop[c][q] * omo + omega * eq[q], c, q, P);
+    }
   }
 }
 
