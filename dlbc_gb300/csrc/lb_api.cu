@@ -411,7 +411,9 @@ int lbgpu_create(const lbgpu_config* cfg, lbgpu_handle** out) {
   h->n = int64_t(h->nx) * h->ny * h->nz;
   {
     const char* tk = getenv("LBGPU_TWO_KERNEL");
-    h->fused = cfg->precision != LBGPU_FP64 && cfg->q == 19 && !(tk && tk[0] == '1');
+    // the fused kernel indexes a component's populations with 32-bit offsets
+    h->fused = cfg->precision != LBGPU_FP64 && cfg->q == 19 && !(tk && tk[0] == '1') &&
+               19 * h->n < (int64_t(1) << 32);
   }
 
   StepParams& P = h->P;

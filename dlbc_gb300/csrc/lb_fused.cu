@@ -35,6 +35,10 @@ FusedParams to_fused(const StepParams& P) {
     F.inv_scale[c] = P.inv_scale[c];
   }
   for (int i = 0; i < 3; ++i) F.acc[i] = float(P.acc[i]);
+  for (int q = 0; q < 19; ++q) {
+    F.qn[q] = uint32_t(int64_t(q) * P.n);
+    for (int c = 0; c < 2; ++c) F.wrho[c][q] = weight<19, float>(q) * P.rho0[c];
+  }
   return F;
 }
 

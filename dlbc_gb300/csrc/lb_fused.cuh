@@ -53,6 +53,8 @@ struct FusedParams {
   float tau[2], inv_tau[2], omega[2], one_minus_omega[2];
   float gcc[2][2], gwc[2], acc[3];
   float rho0[2], scale[2], inv_scale[2];
+  uint32_t qn[19];         // q * n: population q's offset inside a component (19 n < 2^32)
+  float wrho[2][19];       // w_q * rho0_c (half-offset storage)
 };
 
 template <typename T>
@@ -60,15 +62,23 @@ struct FStore;
 template <>
 struct FStore<float> {
   __device__ static __forceinline__ float load(const float* p, int, int, const FusedParams&) { return __ldg(p); }
+  // population q or, bounced back, population b (q, b compile-time constants)
+  __device__ static __forceinline__ float load2(const float* p, int, int, int, bool, const FusedParams&) {
+    return __ldg(p);
+  }
   __device__ static __forceinline__ void store(float* p, float v, int, int, const FusedParams&) { *p = v; }
 };
 template <>
 struct FStore<__half> {
   __device__ static __forceinline__ float load(const __half* p, int c, int q, const FusedParams& P) {
-    return fmaf(P.scale[c], __half2float(__ldg(p)), weight<19, float>(q) * P.rho0[c]);
+    return fmaf(P.scale[c], __half2float(__ldg(p)), P.wrho[c][q]);
+  }
+  __device__ static __forceinline__ float load2(const __half* p, int c, int q, int b, bool bb,
+                                                const FusedParams& P) {
+    return fmaf(P.scale[c], __half2float(__ldg(p)), bb ? P.wrho[c][b] : P.wrho[c][q]);
   }
   __device__ static __forceinline__ void store(__half* p, float v, int c, int q, const FusedParams& P) {
-    *p = __float2half_rn((v - weight<19, float>(q) * P.rho0[c]) * P.inv_scale[c]);
+    *p = __float2half_rn((v - P.wrho[c][q]) * P.inv_scale[c]);
   }
 };
 
@@ -107,27 +117,26 @@ __device__ __forceinline__ YZ make_yz(int y, int z, const FusedParams& P) {
   return r;
 }
 
-// Pull-gather one site of plane slot pl (planes[0..2] = offsets of x-1, x, x+1
-// of the gathered plane x).  ms, my, mz locate the site in the mask ring.
+// Pull-gather one site; planes[0..2] are the offsets of planes xg-1, xg,
+// xg+1 of the gathered plane xg; (my, mz) locate the site in the mask ring.
 template <typename T, bool WALLS, int C>
-__device__ __forceinline__ void fused_gather(const T* __restrict__ f, const FusedShared& sh, const FusedParams& P,
-                                             const int64_t planes[3], const YZ& yz, int mslot[3], int my, int mz,
-                                             bool solid, float pop[C][19]) {
-  const int64_t s = planes[1] + yz.off[1][1];
+__device__ __forceinline__ void fused_gather(const T* const (&fc)[2], const FusedShared& sh, const FusedParams& P,
+                                             const uint32_t (&planes)[3], const YZ& yz, const int (&mslot)[3],
+                                             int my, int mz, bool solid, float (&pop)[C][19]) {
+  const uint32_t s = planes[1] + uint32_t(yz.off[1][1]);
   // branch-free (warps straddling a wall must not run two code paths):
   // a solid site keeps its own populations, a fluid site pulls from x - c_q
   // or, when that site is solid, bounces back its own opposite population
 #pragma unroll
   for (int q = 0; q < 19; ++q) {
     const int cx = Conn<19>::cx(q), cy = Conn<19>::cy(q), cz = Conn<19>::cz(q);
-    const int64_t nb = planes[1 - cx] + yz.off[1 - cy][1 - cz];
+    const uint32_t nb = planes[1 - cx] + uint32_t(yz.off[1 - cy][1 - cz]);
     bool bb = false;
     if (WALLS && q > 0) bb = sh.solid[mslot[1 - cx]][my - cy][mz - cz] && !solid;
     const int b = Conn<19>::bounce(q);
-    const int64_t site = (WALLS && (solid || bb)) ? s : nb;
-    const int qq = bb ? b : q;
+    const uint32_t off = (bb ? P.qn[b] : P.qn[q]) + ((WALLS && (solid || bb)) ? s : nb);
 #pragma unroll
-    for (int c = 0; c < C; ++c) pop[c][q] = FStore<T>::load(f + (int64_t(c) * 19 + qq) * P.n + site, c, qq, P);
+    for (int c = 0; c < C; ++c) pop[c][q] = FStore<T>::load2(fc[c] + off, c, q, b, bb, P);
   }
 }
 
@@ -139,7 +148,9 @@ __global__ void __launch_bounds__(kFusedThreads, 2)
   FusedShared& sh = *reinterpret_cast<FusedShared*>(smem_raw);
   const int t = threadIdx.x;
   const int ty = t / kFusedTZ, tz = t % kFusedTZ;
-  const int64_t plane_sz = int64_t(P.ny) * P.nz;
+  const uint32_t plane_sz = uint32_t(P.ny) * uint32_t(P.nz);
+  const T* const fc[2] = {f, f + size_t(19) * size_t(P.n)};
+  T* const fo[2] = {fout, fout + size_t(19) * size_t(P.n)};
   const int64_t w0 = P.work * blockIdx.x / gridDim.x;
   const int64_t w1 = P.work * (blockIdx.x + 1) / gridDim.x;
   int64_t w = w0;
@@ -173,24 +184,24 @@ __global__ void __launch_bounds__(kFusedThreads, 2)
     // mask ring loader: plane x into slot ms, tile + two-site border
     auto load_mask = [&](int ms, int x) {
       if (!WALLS) return;
-      const int64_t base = int64_t(x) * plane_sz;
+      const size_t base = size_t(x) * plane_sz;
       for (int i = t; i < kFusedMY * kFusedMZ; i += kFusedThreads) {
         const int my = i / kFusedMZ, mz = i % kFusedMZ;
         if (my > tyv + 3 || mz > tzv + 3) continue;
         const int y = wrap(y0 + my - 2, P.ny), z = wrap(z0 + mz - 2, P.nz);
-        sh.solid[ms][my][mz] = __ldg(mask + base + int64_t(y) * P.nz + z);
+        sh.solid[ms][my][mz] = __ldg(mask + base + size_t(y) * P.nz + z);
       }
     };
     // rho/psi of plane xg into psi slot ps (and the tile's populations into
     // buffer keep, unless keep < 0); the mask of planes xg-1..xg+1 must be in
     // mask slots mslot[0..2]
-    auto gather_plane = [&](int ps, int xg, int keep, int mslot[3]) {
-      const int64_t planes[3] = {int64_t(wrap(xg - 1, P.nx)) * plane_sz, int64_t(xg) * plane_sz,
-                                 int64_t(wrap(xg + 1, P.nx)) * plane_sz};
+    auto gather_plane = [&](int ps, int xg, int keep, const int (&mslot)[3]) {
+      const uint32_t planes[3] = {uint32_t(wrap(xg - 1, P.nx)) * plane_sz, uint32_t(xg) * plane_sz,
+                                  uint32_t(wrap(xg + 1, P.nx)) * plane_sz};
       if (active) {
         const bool solid = WALLS && sh.solid[mslot[1]][ty + 2][tz + 2];
         float pop[C][19];
-        fused_gather<T, WALLS, C>(f, sh, P, planes, yz_in, mslot, ty + 2, tz + 2, solid, pop);
+        fused_gather<T, WALLS, C>(fc, sh, P, planes, yz_in, mslot, ty + 2, tz + 2, solid, pop);
 #pragma unroll
         for (int c = 0; c < C; ++c) {
           const float den = density<19, float>(pop[c]);
@@ -205,7 +216,7 @@ __global__ void __launch_bounds__(kFusedThreads, 2)
       if (has_ring) {
         const bool solid = WALLS && sh.solid[mslot[1]][rry + 2][rrz + 2];
         float pop[C][19];
-        fused_gather<T, WALLS, C>(f, sh, P, planes, yz_ring, mslot, rry + 2, rrz + 2, solid, pop);
+        fused_gather<T, WALLS, C>(fc, sh, P, planes, yz_ring, mslot, rry + 2, rrz + 2, solid, pop);
 #pragma unroll
         for (int c = 0; c < C; ++c) {
           const float den = density<19, float>(pop[c]);
@@ -221,9 +232,9 @@ __global__ void __launch_bounds__(kFusedThreads, 2)
     for (int j = 0; j < 5; ++j) load_mask(j, wrap(xs - 2 + j, P.nx));
     __syncthreads();
     {
-      int m0[3] = {0, 1, 2};
+      const int m0[3] = {0, 1, 2};
       gather_plane(0, wrap(xs - 1, P.nx), -1, m0);
-      int m1[3] = {1, 2, 3};
+      const int m1[3] = {1, 2, 3};
       gather_plane(1, xs, 0, m1);
     }
     int cur = 0;
@@ -231,13 +242,13 @@ __global__ void __launch_bounds__(kFusedThreads, 2)
       const int x = xs + k;
       const int sm = k % 3, s0 = (k + 1) % 3, sp = (k + 2) % 3;  // psi slots of x-1, x, x+1
       // mask slots of planes x-1, x, x+1, x+2: (k+1)%5 .. (k+4)%5
-      int mg[3] = {(k + 2) % 5, (k + 3) % 5, (k + 4) % 5};  // planes x, x+1, x+2
+      const int mg[3] = {(k + 2) % 5, (k + 3) % 5, (k + 4) % 5};  // planes x, x+1, x+2
       __syncthreads();  // psi slot sp, pops buffer 1-cur and mask slot k%5 (plane x-2) are free
       load_mask(k % 5, wrap(x + 3, P.nx));  // for the next iteration
       gather_plane(sp, wrap(x + 1, P.nx), 1 - cur, mg);
       __syncthreads();
       if (active) {
-        const int64_t s = int64_t(x) * plane_sz + yz_in.off[1][1];
+        const uint32_t s = uint32_t(x) * plane_sz + uint32_t(yz_in.off[1][1]);
         const int c1y = ty + 1, c1z = tz + 1;
         // branch-free: solid sites compute like fluid ones and store their
         // own populations (warps straddling a wall run one code path)
@@ -318,35 +329,33 @@ __global__ void __launch_bounds__(kFusedThreads, 2)
 #pragma unroll
           for (int c = 0; c < C; ++c)
 #pragma unroll
-            for (int vd = 0; vd < 3; ++vd) force_out[(int64_t(c) * P.n + s) * 3 + vd] = double(F[c][vd]);
+            for (int vd = 0; vd < 3; ++vd) force_out[(size_t(c) * P.n + s) * 3 + vd] = double(F[c][vd]);
         }
-        // --- BDist2 weighted velocity
+        // --- BDist2 weighted velocity (collision.d:256-296); the populations
+        // of the last component stay in registers for its collision
+        float pop[19];
         float wv[3] = {0.f, 0.f, 0.f};
         if (P.eq_form == 2) {
+          float a[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+          for (int c = 0; c < C; ++c) {
+#pragma unroll
+            for (int q = 0; q < 19; ++q) pop[q] = sh.pops[cur][c][q][t];
+#pragma unroll
+            for (int vd = 0; vd < 3; ++vd) a[vd] = fmaf(moment<19, float>(pop, vd), P.inv_tau[c], a[vd]);
+          }
           const float rtot = __frcp_rn(tot);
 #pragma unroll
-          for (int vd = 0; vd < 3; ++vd) {
-            float a = 0.f;
-#pragma unroll
-            for (int c = 0; c < C; ++c) {
-              float m = 0.f;
-#pragma unroll
-              for (int q = 1; q < 19; ++q) {
-                const int cv = cvel<19>(q, vd);
-                if (cv > 0) m += sh.pops[cur][c][q][t];
-                if (cv < 0) m -= sh.pops[cur][c][q][t];
-              }
-              a = fmaf(m, P.inv_tau[c], a);
-            }
-            wv[vd] = a * rtot;
-          }
+          for (int vd = 0; vd < 3; ++vd) wv[vd] = a[vd] * rtot;
         }
         // --- collision; solid sites store their populations unchanged
 #pragma unroll
-        for (int c = 0; c < C; ++c) {
-          float pop[19];
+        for (int cc = 0; cc < C; ++cc) {
+          const int c = C - 1 - cc;  // last component first: its populations are loaded
+          if (!(P.eq_form == 2 && cc == 0)) {
 #pragma unroll
-          for (int q = 0; q < 19; ++q) pop[q] = sh.pops[cur][c][q][t];
+            for (int q = 0; q < 19; ++q) pop[q] = sh.pops[cur][c][q][t];
+          }
           const float rden = __frcp_rn(den[c]);
           float dv[3];
 #pragma unroll
@@ -360,7 +369,7 @@ __global__ void __launch_bounds__(kFusedThreads, 2)
 #pragma unroll
           for (int q = 0; q < 19; ++q) {
             const float v = pop[q] * omo + omega * eq[q];
-            FStore<T>::store(fout + (int64_t(c) * 19 + q) * P.n + s, solid ? pop[q] : v, c, q, P);
+            FStore<T>::store(fo[c] + (P.qn[q] + s), solid ? pop[q] : v, c, q, P);
           }
         }
       }
