@@ -28,6 +28,7 @@ UNITS = {
     "lb_api.cu": ["-fmad=false"],
     "lb_step_lp.cu": [],
     "lb_fused.cu": [],
+    "lb_batch.cu": [],
     "lb_noalloc.cu": [],
 }
 

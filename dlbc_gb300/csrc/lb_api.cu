@@ -23,11 +23,8 @@
 #include "../../include/lbgpu.h"
 #include "lb_launch.h"
 
-using lbk::StepParams;
-
 namespace {
 
-constexpr int kHalo = 2;
 constexpr size_t kStagingBytes = size_t(256) << 20;
 
 thread_local std::string g_create_error;
@@ -37,50 +34,7 @@ size_t arith_size(int precision) { return precision == LBGPU_FP64 ? 8 : 4; }
 
 }  // namespace
 
-struct lbgpu_handle {
-  lbgpu_config cfg;
-  int d = 3, Q = 19, C = 2;
-  int nx = 1, ny = 1, nz = 1;       // kernel extents (nz = 1 for D2Q9)
-  int nxh = 1, nyh = 1, nzh = 1;    // haloed host extents
-  int hz = kHalo;                   // halo in z (0 for D2Q9)
-  int64_t n = 0;
-  cudaStream_t stream = nullptr;       // where work is queued
-  cudaStream_t own_stream = nullptr;   // created with the handle
-  void* f[2] = {nullptr, nullptr};
-  int cur = 0;
-  uint8_t* mask = nullptr;
-  void* rho = nullptr;
-  void* psi = nullptr;
-  double* force = nullptr;
-  int record_force = 0;
-  int force_valid = 0;
-  double* staging = nullptr;
-  size_t staging_bytes = 0;
-  double* moments = nullptr;        // device scratch for lbgpu_moments / lbgpu_reduce
-  size_t moments_bytes = 0;
-  StepParams P{};
-  bool uploaded = false;
-  // FP32/FP16 D3Q19 run the fused single-pass kernel; LBGPU_TWO_KERNEL=1 in
-  // the environment at lbgpu_create selects the two-kernel step instead
-  bool fused = false;
-  // per-kernel event timing (lbgpu_profile)
-  bool profiling = false;
-  std::vector<lbk::StepEvents> ev_pending, ev_pool;
-  double kernel_ms[2] = {0.0, 0.0};
-  int64_t kernel_n[2] = {0, 0};
-  int64_t launches = 0;
-  int64_t device_bytes = 0;
-  std::string err;
-
-  int fail(int code, const std::string& msg) {
-    err = msg;
-    return code;
-  }
-  int cuda_fail(cudaError_t e, const char* what) {
-    err = std::string(what) + ": " + cudaGetErrorString(e);
-    return LBGPU_E_CUDA;
-  }
-};
+#include "lb_handle.h"
 
 namespace {
 
@@ -376,24 +330,15 @@ cudaError_t fold_kernel_times(lbgpu_handle* h) {
 
 }  // namespace
 
-extern "C" {
-
-int32_t lbgpu_abi_version(void) { return LBGPU_ABI_VERSION; }
-
-const char* lbgpu_last_error(const lbgpu_handle* h) { return h ? h->err.c_str() : g_create_error.c_str(); }
-
-int lbgpu_create(const lbgpu_config* cfg, lbgpu_handle** out) {
+int lb_handle_create(const lbgpu_config* cfg, bool lite, double* staging, size_t staging_bytes,
+                     cudaStream_t stream, lbgpu_handle** out, std::string* err) {
   if (!out) return LBGPU_E_INVALID;
   *out = nullptr;
-  std::string why;
-  int rc = validate(cfg, &why);
-  if (rc) {
-    g_create_error = why;
-    return rc;
-  }
+  int rc = validate(cfg, err);
+  if (rc) return rc;
   cudaError_t e = cudaSetDevice(cfg->device);
   if (e != cudaSuccess) {
-    g_create_error = std::string("cudaSetDevice: ") + cudaGetErrorString(e);
+    *err = std::string("cudaSetDevice: ") + cudaGetErrorString(e);
     return LBGPU_E_CUDA;
   }
   lbgpu_handle* h = new lbgpu_handle;
@@ -409,11 +354,17 @@ int lbgpu_create(const lbgpu_config* cfg, lbgpu_handle** out) {
   h->nyh = h->ny + 2 * kHalo;
   h->nzh = h->nz + 2 * h->hz;
   h->n = int64_t(h->nx) * h->ny * h->nz;
+  h->lite = lite;
   {
     const char* tk = getenv("LBGPU_TWO_KERNEL");
     // the fused kernel indexes a component's populations with 32-bit offsets
-    h->fused = cfg->precision != LBGPU_FP64 && cfg->q == 19 && !(tk && tk[0] == '1') &&
+    h->fused = cfg->precision != LBGPU_FP64 && cfg->q == 19 && !(tk && tk[0] == '1' && !lite) &&
                19 * h->n < (int64_t(1) << 32);
+  }
+  if (lite && !h->fused) {
+    *err = "batch members must be FP32/FP16 D3Q19 lattices below 2^32/19 sites";
+    delete h;
+    return LBGPU_E_INVALID;
   }
 
   StepParams& P = h->P;
@@ -441,27 +392,36 @@ int lbgpu_create(const lbgpu_config* cfg, lbgpu_handle** out) {
   for (int c = 0; c < h->C; ++c)
     if (cfg->tau[c] != 1.0) P.unit_tau = 0;
 
-  e = cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking);
-  h->stream = h->own_stream;
-  if (e != cudaSuccess) {
-    g_create_error = std::string("cudaStreamCreate: ") + cudaGetErrorString(e);
-    delete h;
-    return LBGPU_E_CUDA;
+  if (lite) {
+    h->stream = stream;
+    h->staging = staging;
+    h->staging_bytes = staging_bytes;
+    h->owns_staging = false;
+  } else {
+    e = cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking);
+    h->stream = h->own_stream;
+    if (e != cudaSuccess) {
+      *err = std::string("cudaStreamCreate: ") + cudaGetErrorString(e);
+      delete h;
+      return LBGPU_E_CUDA;
+    }
   }
   const size_t fbytes = size_t(h->C) * h->Q * h->n * storage_size(cfg->precision);
-  const size_t sbytes = size_t(h->C) * h->n * arith_size(cfg->precision);
+  const size_t sbytes = lite ? 0 : size_t(h->C) * h->n * arith_size(cfg->precision);
   const size_t plane_bytes = size_t(h->nyh) * h->nzh * h->Q * sizeof(double);
-  h->staging_bytes = std::max(plane_bytes, std::min(kStagingBytes, plane_bytes * h->nxh));
+  if (!lite) h->staging_bytes = std::max(plane_bytes, std::min(kStagingBytes, plane_bytes * h->nxh));
   h->moments_bytes = size_t(h->C) * h->n * sizeof(double);
-  void* ptrs[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
-  const size_t sizes[6] = {fbytes, fbytes, sbytes, sbytes, h->staging_bytes, h->moments_bytes};
-  for (int i = 0; i < 6; ++i) {
+  void* ptrs[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  const size_t sizes[5] = {fbytes, fbytes, sbytes, sbytes, lite ? 0 : h->staging_bytes};
+  for (int i = 0; i < 5; ++i) {
+    if (sizes[i] == 0) continue;
     e = cudaMalloc(&ptrs[i], sizes[i]);
     if (e != cudaSuccess) {
-      for (int j = 0; j < i; ++j) cudaFree(ptrs[j]);
-      cudaStreamDestroy(h->own_stream);
-      g_create_error = std::string("device allocation of ") + std::to_string(sizes[i]) + " bytes failed: " +
-                       cudaGetErrorString(e);
+      for (int j = 0; j < i; ++j)
+        if (ptrs[j]) cudaFree(ptrs[j]);
+      if (h->own_stream) cudaStreamDestroy(h->own_stream);
+      *err = std::string("device allocation of ") + std::to_string(sizes[i]) + " bytes failed: " +
+             cudaGetErrorString(e);
       cudaGetLastError();
       delete h;
       return LBGPU_E_NOMEM;
@@ -472,10 +432,40 @@ int lbgpu_create(const lbgpu_config* cfg, lbgpu_handle** out) {
   h->f[1] = ptrs[1];
   h->rho = ptrs[2];
   h->psi = ptrs[3];
-  h->staging = static_cast<double*>(ptrs[4]);
-  h->moments = static_cast<double*>(ptrs[5]);
+  if (!lite) h->staging = static_cast<double*>(ptrs[4]);
   *out = h;
   return LBGPU_OK;
+}
+
+int64_t lb_member_bytes(const lbgpu_config* cfg) {
+  int64_t n = 1;
+  for (int i = 0; i < cfg->d; ++i) n *= cfg->gn[i];
+  return 2 * int64_t(cfg->components) * cfg->q * n * int64_t(storage_size(cfg->precision)) + n;
+}
+
+int lb_ensure_moments(lbgpu_handle* h) {
+  if (h->moments) return LBGPU_OK;
+  cudaError_t e = cudaMalloc(&h->moments, h->moments_bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    h->moments = nullptr;
+    return h->fail(LBGPU_E_NOMEM, "moments scratch allocation failed");
+  }
+  h->device_bytes += int64_t(h->moments_bytes);
+  return LBGPU_OK;
+}
+
+extern "C" {
+
+int32_t lbgpu_abi_version(void) { return LBGPU_ABI_VERSION; }
+
+const char* lbgpu_last_error(const lbgpu_handle* h) { return h ? h->err.c_str() : g_create_error.c_str(); }
+
+int lbgpu_create(const lbgpu_config* cfg, lbgpu_handle** out) {
+  std::string why;
+  const int rc = lb_handle_create(cfg, false, nullptr, 0, nullptr, out, &why);
+  if (rc) g_create_error = why;
+  return rc;
 }
 
 void lbgpu_destroy(lbgpu_handle* h) {
@@ -484,10 +474,10 @@ void lbgpu_destroy(lbgpu_handle* h) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   cudaFree(h->f[0]);
   cudaFree(h->f[1]);
-  cudaFree(h->rho);
-  cudaFree(h->psi);
-  cudaFree(h->staging);
-  cudaFree(h->moments);
+  if (h->rho) cudaFree(h->rho);
+  if (h->psi) cudaFree(h->psi);
+  if (h->owns_staging && h->staging) cudaFree(h->staging);
+  if (h->moments) cudaFree(h->moments);
   if (h->mask) cudaFree(h->mask);
   if (h->force) cudaFree(h->force);
   for (auto& e : h->ev_pending)
@@ -569,10 +559,12 @@ int lbgpu_upload(lbgpu_handle* h, const double* const* fluids, const int32_t* ma
       if (e != cudaSuccess) return h->cuda_fail(e, "mask allocation");
       h->device_bytes += h->n;
     }
-    int* d_count = reinterpret_cast<int*>(h->moments);
+    // the solid-site counter lives in the last 256 bytes of the staging buffer
+    const size_t usable = h->staging_bytes - 256;
+    int* d_count = reinterpret_cast<int*>(reinterpret_cast<char*>(h->staging) + usable);
     cudaMemsetAsync(d_count, 0, sizeof(int), h->stream);
     const size_t plane_m = size_t(h->nyh) * h->nzh;
-    const int ppc = int(std::max<size_t>(1, h->staging_bytes / (plane_m * sizeof(int32_t))));
+    const int ppc = int(std::max<size_t>(1, usable / (plane_m * sizeof(int32_t))));
     for (int xh0 = 0; xh0 < h->nxh; xh0 += ppc) {
       const int np = std::min(ppc, h->nxh - xh0);
       if (xh0 + np <= kHalo || xh0 >= h->nx + kHalo) continue;
@@ -704,6 +696,7 @@ int lbgpu_moments(lbgpu_handle* h, double* const* density, double* const* veloci
   if (!h) return LBGPU_E_INVALID;
   if (!h->uploaded) return h->fail(LBGPU_E_NOTREADY, "lbgpu_moments before lbgpu_upload");
   cudaSetDevice(h->cfg.device);
+  if (int rc = lb_ensure_moments(h)) return rc;
   // the staging buffer holds C*N*d doubles of velocity when large enough,
   // else velocities go one component at a time through the moments buffer
   cudaError_t e;
@@ -800,6 +793,7 @@ int lbgpu_reduce(lbgpu_handle* h, double* mass, double* momentum) {
   if (!h) return LBGPU_E_INVALID;
   if (!h->uploaded) return h->fail(LBGPU_E_NOTREADY, "lbgpu_reduce before lbgpu_upload");
   cudaSetDevice(h->cfg.device);
+  if (int rc = lb_ensure_moments(h)) return rc;
   const int nblocks = int(std::min<int64_t>(1024, ceil_div(h->n, kRedThreads)));
   const int64_t per_block = ceil_div(h->n, nblocks);
   double* partial = h->moments;             // nblocks*8 doubles <= C*N doubles

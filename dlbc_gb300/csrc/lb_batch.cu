@@ -1,0 +1,441 @@
+// Batches: many independent D3Q19 two-component lattices (FP32 or FP16
+// offset storage) advanced together, one persistent launch per timestep.
+//
+// Members are lattice handles (lb_handle.h) that own only their population
+// buffers and mask; the batch owns the stream and a shared staging buffer for
+// host transfers, and admits members against a fixed device-memory budget.
+// A device table of FusedSim descriptors (one per member, in admission order)
+// drives k_fused_batch; it is rebuilt when members join or leave.  Steps are
+// replayed as a captured CUDA graph of two launches (the two buffer
+// parities).  The launch shape (tile height 4 or 8, resident CTAs per SM) is
+// chosen by timing the candidates on the batch itself: every candidate
+// computes the same per-site arithmetic, so tuning steps are ordinary steps.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/lbgpu.h"
+#include "lb_fused.cuh"
+#include "lb_handle.h"
+
+namespace {
+
+constexpr size_t kBatchStaging = size_t(256) << 20;
+
+struct Shape {
+  int ty;
+  int ctas_per_sm;
+};
+
+const Shape kCandidates[] = {{8, 2}, {8, 1}, {4, 4}, {4, 2}};
+
+std::mutex g_tune_mu;
+std::map<std::string, Shape> g_tuned;  // member-size signature -> best shape
+
+thread_local std::string g_batch_create_error;
+
+}  // namespace
+
+struct lbgpu_batch {
+  int device = 0;
+  int precision = LBGPU_FP16;
+  int64_t budget = 0;
+  int64_t used = 0;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  double* staging = nullptr;
+  std::vector<lbgpu_handle*> sims;   // by member id; nullptr once removed
+  std::vector<int64_t> bytes;
+  // descriptor table
+  lbk::FusedSim* d_table = nullptr;
+  int table_cap = 0;
+  int table_n = 0;
+  int64_t total_work = 0;
+  bool walls = false;
+  bool dirty = true;
+  int64_t steps_since_build = 0;
+  std::vector<int> table_ids;
+  std::vector<int> table_phase;
+  // launch shape
+  Shape shape{8, 0};
+  int autotune = 1;
+  bool shape_fixed = false;
+  int use_graph = 1;
+  cudaGraphExec_t graph = nullptr;
+  int64_t launches = 0;
+  std::string err;
+
+  int fail(int code, const std::string& m) {
+    err = m;
+    return code;
+  }
+  int cuda_fail(cudaError_t e, const char* what) {
+    err = std::string(what) + ": " + cudaGetErrorString(e);
+    return LBGPU_E_CUDA;
+  }
+};
+
+namespace {
+
+void drop_graph(lbgpu_batch* b) {
+  if (b->graph) {
+    cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+  }
+}
+
+std::string signature(const lbgpu_batch* b) {
+  std::string s = std::to_string(b->precision);
+  for (auto* h : b->sims)
+    if (h) s += "|" + std::to_string(h->nx) + "x" + std::to_string(h->ny) + "x" + std::to_string(h->nz);
+  return s;
+}
+
+// (re)build the descriptor table for tile height ty, with every member's
+// current input buffer as parity 0
+int build_table(lbgpu_batch* b, int ty) {
+  std::vector<lbk::FusedSim> tab;
+  b->table_ids.clear();
+  b->table_phase.clear();
+  b->total_work = 0;
+  b->walls = false;
+  for (size_t id = 0; id < b->sims.size(); ++id) {
+    lbgpu_handle* h = b->sims[id];
+    if (!h) continue;
+    lbk::FusedSim fs;
+    memset(&fs, 0, sizeof fs);
+    fs.P = lbk::make_fused_params(h->P, ty);
+    fs.f[0] = h->f[0];
+    fs.f[1] = h->f[1];
+    fs.mask = h->mask;
+    fs.force_out = nullptr;
+    fs.work_begin = b->total_work;
+    fs.phase = h->cur;
+    b->total_work += fs.P.work;
+    b->walls = b->walls || h->mask != nullptr;
+    tab.push_back(fs);
+    b->table_ids.push_back(int(id));
+    b->table_phase.push_back(h->cur);
+  }
+  b->table_n = int(tab.size());
+  if (b->table_n > b->table_cap) {
+    if (b->d_table) cudaFree(b->d_table);
+    b->d_table = nullptr;
+    const int cap = b->table_n * 2;
+    cudaError_t e = cudaMalloc(&b->d_table, sizeof(lbk::FusedSim) * size_t(cap));
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      b->table_cap = 0;
+      return b->fail(LBGPU_E_NOMEM, "batch descriptor table allocation failed");
+    }
+    b->table_cap = cap;
+  }
+  if (b->table_n) {
+    cudaError_t e = cudaMemcpyAsync(b->d_table, tab.data(), sizeof(lbk::FusedSim) * tab.size(),
+                                    cudaMemcpyHostToDevice, b->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+    if (e != cudaSuccess) return b->cuda_fail(e, "batch table upload");
+  }
+  b->steps_since_build = 0;
+  b->dirty = false;
+  drop_graph(b);
+  return LBGPU_OK;
+}
+
+// members' current-buffer index after the steps since the last build
+void sync_members(lbgpu_batch* b) {
+  for (size_t i = 0; i < b->table_ids.size(); ++i) {
+    lbgpu_handle* h = b->sims[b->table_ids[i]];
+    if (h) h->cur = int((b->table_phase[i] + b->steps_since_build) & 1);
+  }
+}
+
+cudaError_t launch_one(lbgpu_batch* b, int parity) {
+  b->launches++;
+  return lbk::launch_fused_batch(b->precision == LBGPU_FP16, b->shape.ty, b->walls, b->d_table, b->table_n,
+                                 b->total_work, parity, b->shape.ctas_per_sm, b->stream, b->device);
+}
+
+// advance n steps with the current table and shape
+int run_steps(lbgpu_batch* b, int n) {
+  if (b->table_n == 0 || n <= 0) return LBGPU_OK;
+  cudaError_t e;
+  int done = 0;
+  // a direct launch first: it makes the parity even for the graph and sets
+  // up the kernel (attributes, occupancy) outside any capture
+  if ((b->steps_since_build & 1) || !b->graph || !b->use_graph) {
+    e = launch_one(b, int(b->steps_since_build & 1));
+    if (e != cudaSuccess) return b->cuda_fail(e, "batch step launch");
+    b->steps_since_build++;
+    done++;
+  }
+  if (b->use_graph && n - done >= 2) {
+    if ((b->steps_since_build & 1) == 1) {
+      e = launch_one(b, 1);
+      if (e != cudaSuccess) return b->cuda_fail(e, "batch step launch");
+      b->steps_since_build++;
+      done++;
+    }
+    if (!b->graph) {
+      cudaGraph_t g = nullptr;
+      e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
+      if (e == cudaSuccess) {
+        cudaError_t e0 = launch_one(b, 0);
+        cudaError_t e1 = launch_one(b, 1);
+        b->launches -= 2;  // counted when replayed
+        e = cudaStreamEndCapture(b->stream, &g);
+        if (e == cudaSuccess && e0 == cudaSuccess && e1 == cudaSuccess)
+          e = cudaGraphInstantiate(&b->graph, g, 0);
+        else if (e == cudaSuccess)
+          e = e0 != cudaSuccess ? e0 : e1;
+        if (g) cudaGraphDestroy(g);
+      }
+      if (e != cudaSuccess) {
+        cudaGetLastError();
+        b->graph = nullptr;
+        b->use_graph = 0;  // fall back to direct launches
+      }
+    }
+    while (b->graph && n - done >= 2) {
+      e = cudaGraphLaunch(b->graph, b->stream);
+      if (e != cudaSuccess) return b->cuda_fail(e, "batch graph launch");
+      b->launches += 2;
+      b->steps_since_build += 2;
+      done += 2;
+    }
+  }
+  while (done < n) {
+    e = launch_one(b, int(b->steps_since_build & 1));
+    if (e != cudaSuccess) return b->cuda_fail(e, "batch step launch");
+    b->steps_since_build++;
+    done++;
+  }
+  return LBGPU_OK;
+}
+
+// time 2 steps of each candidate shape (real steps), keep the fastest;
+// returns the number of steps taken
+int autotune(lbgpu_batch* b, int budget_steps, int* rc) {
+  *rc = LBGPU_OK;
+  const std::string sig = signature(b);
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    auto it = g_tuned.find(sig);
+    if (it != g_tuned.end()) {
+      if (it->second.ty != b->shape.ty || it->second.ctas_per_sm != b->shape.ctas_per_sm) {
+        sync_members(b);
+        b->shape = it->second;
+        *rc = build_table(b, b->shape.ty);
+      }
+      return 0;
+    }
+  }
+  const int per = 2;
+  const int ncand = int(sizeof(kCandidates) / sizeof(kCandidates[0]));
+  if (budget_steps < per * ncand) return 0;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 1e30f;
+  Shape best_shape = b->shape;
+  int taken = 0;
+  const int use_graph = b->use_graph;
+  b->use_graph = 0;
+  for (int i = 0; i < ncand; ++i) {
+    sync_members(b);
+    b->shape = kCandidates[i];
+    if ((*rc = build_table(b, b->shape.ty))) break;
+    cudaEventRecord(e0, b->stream);
+    if ((*rc = run_steps(b, per))) break;
+    cudaEventRecord(e1, b->stream);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    taken += per;
+    if (ms < best) {
+      best = ms;
+      best_shape = kCandidates[i];
+    }
+  }
+  b->use_graph = use_graph;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (*rc) return taken;
+  sync_members(b);
+  b->shape = best_shape;
+  *rc = build_table(b, b->shape.ty);
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  g_tuned[sig] = best_shape;
+  return taken;
+}
+
+}  // namespace
+
+extern "C" {
+
+int lbgpu_batch_create(int32_t device, int32_t precision, int64_t hbm_budget_bytes, lbgpu_batch** out) {
+  if (!out) return LBGPU_E_INVALID;
+  *out = nullptr;
+  if (precision != LBGPU_FP32 && precision != LBGPU_FP16) {
+    g_batch_create_error = "batches run the FP32 or FP16 forms";
+    return LBGPU_E_INVALID;
+  }
+  cudaError_t e = cudaSetDevice(device);
+  if (e != cudaSuccess) {
+    g_batch_create_error = std::string("cudaSetDevice: ") + cudaGetErrorString(e);
+    return LBGPU_E_CUDA;
+  }
+  lbgpu_batch* b = new lbgpu_batch;
+  b->device = device;
+  b->precision = precision;
+  b->budget = hbm_budget_bytes > 0 ? hbm_budget_bytes : INT64_MAX;
+  e = cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMalloc(&b->staging, kBatchStaging);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    if (b->own_stream) cudaStreamDestroy(b->own_stream);
+    g_batch_create_error = std::string("batch set-up failed: ") + cudaGetErrorString(e);
+    delete b;
+    return LBGPU_E_NOMEM;
+  }
+  b->stream = b->own_stream;
+  *out = b;
+  return LBGPU_OK;
+}
+
+void lbgpu_batch_destroy(lbgpu_batch* b) {
+  if (!b) return;
+  cudaSetDevice(b->device);
+  cudaStreamSynchronize(b->stream);
+  for (auto* h : b->sims)
+    if (h) lbgpu_destroy(h);
+  drop_graph(b);
+  if (b->d_table) cudaFree(b->d_table);
+  cudaFree(b->staging);
+  if (b->own_stream) cudaStreamDestroy(b->own_stream);
+  delete b;
+}
+
+const char* lbgpu_batch_last_error(const lbgpu_batch* b) { return b ? b->err.c_str() : g_batch_create_error.c_str(); }
+
+int lbgpu_batch_add(lbgpu_batch* b, const lbgpu_config* cfg, const double* const* fluids, const int32_t* mask,
+                    int32_t* sim_id) {
+  if (!b || !cfg || !fluids || !sim_id) return LBGPU_E_INVALID;
+  if (cfg->precision != b->precision) return b->fail(LBGPU_E_INVALID, "member precision differs from the batch's");
+  if (cfg->q != 19 || cfg->components != 2)
+    return b->fail(LBGPU_E_INVALID, "batch members are two-component D3Q19 lattices");
+  if (cfg->device != b->device) return b->fail(LBGPU_E_INVALID, "member device differs from the batch's");
+  const int64_t need = lb_member_bytes(cfg);
+  if (b->used + need > b->budget)
+    return b->fail(LBGPU_E_BUDGET, "admission refused: " + std::to_string(need) + " bytes over the budget (" +
+                                       std::to_string(b->budget - b->used) + " left)");
+  cudaSetDevice(b->device);
+  std::string why;
+  lbgpu_handle* h = nullptr;
+  int rc = lb_handle_create(cfg, true, b->staging, kBatchStaging, b->stream, &h, &why);
+  if (rc) return b->fail(rc, why);
+  rc = lbgpu_upload(h, fluids, mask);
+  if (rc) {
+    b->err = lbgpu_last_error(h);
+    lbgpu_destroy(h);
+    return rc;
+  }
+  sync_members(b);
+  b->sims.push_back(h);
+  b->bytes.push_back(h->device_bytes);
+  b->used += b->bytes.back();
+  b->dirty = true;
+  *sim_id = int32_t(b->sims.size() - 1);
+  return LBGPU_OK;
+}
+
+int lbgpu_batch_remove(lbgpu_batch* b, int32_t sim_id) {
+  if (!b || sim_id < 0 || size_t(sim_id) >= b->sims.size() || !b->sims[sim_id]) return LBGPU_E_INVALID;
+  cudaSetDevice(b->device);
+  sync_members(b);
+  cudaStreamSynchronize(b->stream);
+  lbgpu_destroy(b->sims[sim_id]);
+  b->sims[sim_id] = nullptr;
+  b->used -= b->bytes[sim_id];
+  b->dirty = true;
+  return LBGPU_OK;
+}
+
+int lbgpu_batch_step(lbgpu_batch* b, int32_t nsteps) {
+  if (!b || nsteps < 0) return LBGPU_E_INVALID;
+  cudaSetDevice(b->device);
+  if (b->dirty) {
+    sync_members(b);
+    int rc = build_table(b, b->shape.ty);
+    if (rc) return rc;
+  }
+  int remaining = nsteps;
+  if (b->autotune && !b->shape_fixed) {
+    int rc = LBGPU_OK;
+    remaining -= autotune(b, remaining, &rc);
+    if (rc) return rc;
+  }
+  int rc = run_steps(b, remaining);
+  sync_members(b);
+  return rc;
+}
+
+lbgpu_handle* lbgpu_batch_member(lbgpu_batch* b, int32_t sim_id) {
+  if (!b || sim_id < 0 || size_t(sim_id) >= b->sims.size()) return nullptr;
+  return b->sims[sim_id];
+}
+
+int lbgpu_batch_set_stream(lbgpu_batch* b, void* stream) {
+  if (!b) return LBGPU_E_INVALID;
+  cudaSetDevice(b->device);
+  cudaStreamSynchronize(b->stream);
+  b->stream = stream ? static_cast<cudaStream_t>(stream) : b->own_stream;
+  for (auto* h : b->sims)
+    if (h) h->stream = b->stream;
+  drop_graph(b);
+  return LBGPU_OK;
+}
+
+int lbgpu_batch_synchronize(lbgpu_batch* b) {
+  if (!b) return LBGPU_E_INVALID;
+  cudaSetDevice(b->device);
+  cudaError_t e = cudaStreamSynchronize(b->stream);
+  if (e != cudaSuccess) return b->cuda_fail(e, "batch synchronize");
+  return LBGPU_OK;
+}
+
+int64_t lbgpu_batch_device_bytes(const lbgpu_batch* b) { return b ? b->used : 0; }
+
+int64_t lbgpu_batch_launch_count(const lbgpu_batch* b) { return b ? b->launches : 0; }
+
+int lbgpu_batch_set_tuning(lbgpu_batch* b, int32_t autotune, int32_t tile_height, int32_t ctas_per_sm,
+                           int32_t use_graph) {
+  if (!b) return LBGPU_E_INVALID;
+  if (tile_height != 0 && tile_height != 4 && tile_height != 8) return b->fail(LBGPU_E_INVALID, "tile height 4 or 8");
+  b->autotune = autotune;
+  b->use_graph = use_graph;
+  if (tile_height) {
+    sync_members(b);
+    b->shape = Shape{tile_height, ctas_per_sm};
+    b->shape_fixed = true;
+    b->dirty = true;
+  } else {
+    b->shape_fixed = false;
+  }
+  drop_graph(b);
+  return LBGPU_OK;
+}
+
+int lbgpu_batch_launch_shape(const lbgpu_batch* b, int32_t* tile_height, int32_t* ctas_per_sm) {
+  if (!b) return LBGPU_E_INVALID;
+  if (tile_height) *tile_height = b->shape.ty;
+  if (ctas_per_sm) *ctas_per_sm = b->shape.ctas_per_sm;
+  return LBGPU_OK;
+}
+
+}  // extern "C"

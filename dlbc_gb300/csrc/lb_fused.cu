@@ -1,4 +1,5 @@
-// Launcher of the fused single-pass step (lb_fused.cuh).
+// Launchers of the fused single-pass step (lb_fused.cuh): one lattice, or a
+// batch of lattices in one persistent launch.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -8,15 +9,13 @@
 
 namespace lbk {
 
-namespace {
-
-FusedParams to_fused(const StepParams& P) {
+FusedParams make_fused_params(const StepParams& P, int ty) {
   FusedParams F{};
   F.nx = P.nx;
   F.ny = P.ny;
   F.nz = P.nz;
   F.n = P.n;
-  F.tiles_y = (P.ny + kFusedTY - 1) / kFusedTY;
+  F.tiles_y = (P.ny + ty - 1) / ty;
   F.tiles_z = (P.nz + kFusedTZ - 1) / kFusedTZ;
   F.work = int64_t(F.tiles_y) * F.tiles_z * P.nx;
   F.shan_chen = P.shan_chen;
@@ -42,31 +41,70 @@ FusedParams to_fused(const StepParams& P) {
   return F;
 }
 
-template <typename T, int C, bool W>
-cudaError_t go(const StepBuffers& b, const FusedParams& F, cudaStream_t st, int device) {
-  auto kern = k_fused<T, C, W>;
-  const int smem = int(sizeof(FusedShared));
-  static std::mutex mu;
-  static int configured[64] = {0};
-  static int grid_for[64] = {0};
-  int grid;
-  {
-    std::lock_guard<std::mutex> lock(mu);
-    if (!configured[device & 63]) {
-      cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-      if (e != cudaSuccess) return e;
-      int per_sm = 0, sms = 0;
-      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kFusedThreads, smem);
-      if (e != cudaSuccess) return e;
-      e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-      if (e != cudaSuccess) return e;
-      grid_for[device & 63] = (per_sm > 0 ? per_sm : 1) * sms;
-      configured[device & 63] = 1;
-    }
-    grid = grid_for[device & 63];
+size_t fused_smem_bytes(int ty) { return ty == 4 ? sizeof(FusedShared<4>) : sizeof(FusedShared<8>); }
+
+namespace {
+
+// per (kernel, device): shared-memory opt-in done and resident CTAs per SM
+struct KernelInfo {
+  std::mutex mu;
+  int per_sm[64] = {0};
+};
+
+template <typename K>
+cudaError_t kernel_setup(K kern, int smem, int threads, int device, KernelInfo& info, int* per_sm) {
+  std::lock_guard<std::mutex> lock(info.mu);
+  if (!info.per_sm[device & 63]) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    int n = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, threads, smem);
+    if (e != cudaSuccess) return e;
+    info.per_sm[device & 63] = n > 0 ? n : 1;
   }
-  if (int64_t(grid) > F.work) grid = int(F.work);
-  kern<<<grid, kFusedThreads, smem, st>>>(static_cast<const T*>(b.f), static_cast<T*>(b.fout), b.mask, b.force, F);
+  *per_sm = info.per_sm[device & 63];
+  return cudaSuccess;
+}
+
+int sm_count(int device) {
+  static int cache[64] = {0};
+  if (!cache[device & 63]) {
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    cache[device & 63] = sms > 0 ? sms : 1;
+  }
+  return cache[device & 63];
+}
+
+template <typename T, int C, bool W, int TY>
+cudaError_t go_single(const StepBuffers& b, const FusedParams& F, cudaStream_t st, int device) {
+  static KernelInfo info;
+  auto kern = k_fused<T, C, W, TY>;
+  const int smem = int(sizeof(FusedShared<TY>));
+  int per_sm = 0;
+  cudaError_t e = kernel_setup(kern, smem, TY * kFusedTZ, device, info, &per_sm);
+  if (e != cudaSuccess) return e;
+  int64_t grid = int64_t(per_sm) * sm_count(device);
+  if (grid > F.work) grid = F.work;
+  kern<<<unsigned(grid), TY * kFusedTZ, smem, st>>>(static_cast<const T*>(b.f), static_cast<T*>(b.fout), b.mask,
+                                                    b.force, F);
+  return cudaGetLastError();
+}
+
+template <typename T, bool W, int TY>
+cudaError_t go_batch(const FusedSim* sims, int nsims, int64_t total, int parity, int ctas_per_sm, cudaStream_t st,
+                     int device) {
+  static KernelInfo info;
+  auto kern = k_fused_batch<T, 2, W, TY>;
+  const int smem = int(sizeof(FusedShared<TY>));
+  int per_sm = 0;
+  cudaError_t e = kernel_setup(kern, smem, TY * kFusedTZ, device, info, &per_sm);
+  if (e != cudaSuccess) return e;
+  if (ctas_per_sm > 0 && ctas_per_sm < per_sm) per_sm = ctas_per_sm;
+  int64_t grid = int64_t(per_sm) * sm_count(device);
+  if (grid > total) grid = total;
+  if (grid < 1) return cudaSuccess;
+  kern<<<unsigned(grid), TY * kFusedTZ, smem, st>>>(sims, nsims, total, parity);
   return cudaGetLastError();
 }
 
@@ -74,7 +112,7 @@ cudaError_t go(const StepBuffers& b, const FusedParams& F, cudaStream_t st, int 
 
 cudaError_t launch_fused(bool half_storage, int c, const StepBuffers& b, const StepParams& P, cudaStream_t st,
                          int64_t* launches, const StepEvents* ev, int device) {
-  const FusedParams F = to_fused(P);
+  const FusedParams F = make_fused_params(P, 8);
   const bool w = b.mask != nullptr;
   if (ev) {
     cudaEventRecord(ev->ev[0], st);
@@ -83,18 +121,30 @@ cudaError_t launch_fused(bool half_storage, int c, const StepBuffers& b, const S
   cudaError_t e;
   if (half_storage) {
     if (c == 2)
-      e = w ? go<__half, 2, true>(b, F, st, device) : go<__half, 2, false>(b, F, st, device);
+      e = w ? go_single<__half, 2, true, 8>(b, F, st, device) : go_single<__half, 2, false, 8>(b, F, st, device);
     else
-      e = w ? go<__half, 1, true>(b, F, st, device) : go<__half, 1, false>(b, F, st, device);
+      e = w ? go_single<__half, 1, true, 8>(b, F, st, device) : go_single<__half, 1, false, 8>(b, F, st, device);
   } else {
     if (c == 2)
-      e = w ? go<float, 2, true>(b, F, st, device) : go<float, 2, false>(b, F, st, device);
+      e = w ? go_single<float, 2, true, 8>(b, F, st, device) : go_single<float, 2, false, 8>(b, F, st, device);
     else
-      e = w ? go<float, 1, true>(b, F, st, device) : go<float, 1, false>(b, F, st, device);
+      e = w ? go_single<float, 1, true, 8>(b, F, st, device) : go_single<float, 1, false, 8>(b, F, st, device);
   }
   if (ev) cudaEventRecord(ev->ev[2], st);
   *launches += 1;
   return e;
+}
+
+cudaError_t launch_fused_batch(bool half_storage, int ty, bool walls, const FusedSim* sims, int nsims,
+                               int64_t total_work, int parity, int ctas_per_sm, cudaStream_t st, int device) {
+#define LB_BATCH(T, W, TYV) go_batch<T, W, TYV>(sims, nsims, total_work, parity, ctas_per_sm, st, device)
+  if (half_storage) {
+    if (ty == 4) return walls ? LB_BATCH(__half, true, 4) : LB_BATCH(__half, false, 4);
+    return walls ? LB_BATCH(__half, true, 8) : LB_BATCH(__half, false, 8);
+  }
+  if (ty == 4) return walls ? LB_BATCH(float, true, 4) : LB_BATCH(float, false, 4);
+  return walls ? LB_BATCH(float, true, 8) : LB_BATCH(float, false, 8);
+#undef LB_BATCH
 }
 
 }  // namespace lbk

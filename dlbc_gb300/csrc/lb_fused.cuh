@@ -35,13 +35,11 @@
 
 namespace lbk {
 
-constexpr int kFusedTY = 8;
+// Tiles are TY x 32 sites (TY = 4 or 8, a template parameter; 32 = one warp
+// along the contiguous z axis), one thread per site.
 constexpr int kFusedTZ = 32;
-constexpr int kFusedThreads = kFusedTY * kFusedTZ;
-constexpr int kFusedRY = kFusedTY + 2;   // tile + one-site ring
-constexpr int kFusedRZ = kFusedTZ + 2;
-constexpr int kFusedMY = kFusedTY + 4;   // tile + two-site border (mask)
-constexpr int kFusedMZ = kFusedTZ + 4;
+constexpr int kFusedRZ = kFusedTZ + 2;   // tile + one-site ring
+constexpr int kFusedMZ = kFusedTZ + 4;   // tile + two-site border (mask)
 
 // float copies of the step parameters (no double arithmetic in the kernel)
 struct FusedParams {
@@ -82,11 +80,12 @@ struct FStore<__half> {
   }
 };
 
+template <int TY>
 struct FusedShared {
-  float pops[2][2][19][kFusedThreads];   // [buffer][c][q][site in tile]
-  float psi[3][2][kFusedRY][kFusedRZ];   // [plane slot][c][y+1][z+1]
-  float rho[3][2][kFusedRY][kFusedRZ];
-  uint8_t solid[5][kFusedMY][kFusedMZ];  // mask, [plane slot][y+2][z+2]
+  float pops[2][2][19][TY * kFusedTZ];  // [buffer][c][q][site in tile]
+  float psi[3][2][TY + 2][kFusedRZ];    // [plane slot][c][y+1][z+1]
+  float rho[3][2][TY + 2][kFusedRZ];
+  uint8_t solid[5][TY + 4][kFusedMZ];   // mask, [plane slot][y+2][z+2]
 };
 
 __device__ __forceinline__ int wrap(int v, int n) { return v < 0 ? v + n : (v >= n ? v - n : v); }
@@ -119,8 +118,8 @@ __device__ __forceinline__ YZ make_yz(int y, int z, const FusedParams& P) {
 
 // Pull-gather one site; planes[0..2] are the offsets of planes xg-1, xg,
 // xg+1 of the gathered plane xg; (my, mz) locate the site in the mask ring.
-template <typename T, bool WALLS, int C>
-__device__ __forceinline__ void fused_gather(const T* const (&fc)[2], const FusedShared& sh, const FusedParams& P,
+template <typename T, bool WALLS, int C, int TY>
+__device__ __forceinline__ void fused_gather(const T* const (&fc)[2], const FusedShared<TY>& sh, const FusedParams& P,
                                              const uint32_t (&planes)[3], const YZ& yz, const int (&mslot)[3],
                                              int my, int mz, bool solid, float (&pop)[C][19]) {
   const uint32_t s = planes[1] + uint32_t(yz.off[1][1]);
@@ -140,19 +139,21 @@ __device__ __forceinline__ void fused_gather(const T* const (&fc)[2], const Fuse
   }
 }
 
-template <typename T, int C, bool WALLS>
-__global__ void __launch_bounds__(kFusedThreads, 2)
-    k_fused(const T* __restrict__ f, T* __restrict__ fout, const uint8_t* __restrict__ mask,
-            double* __restrict__ force_out, FusedParams P) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  FusedShared& sh = *reinterpret_cast<FusedShared*>(smem_raw);
+// Process plane-tiles [w0, w1) of one lattice (tile-major: w = tile*nx + x).
+// P may live in the constant bank (single lattice) or in shared memory
+// (batches); every thread of the CTA calls this with the same range.
+template <typename T, int C, bool WALLS, int TY>
+__device__ __forceinline__ void fused_body(const FusedParams& P, const T* __restrict__ f, T* __restrict__ fout,
+                                           const uint8_t* __restrict__ mask, double* __restrict__ force_out,
+                                           int64_t w0, int64_t w1, FusedShared<TY>& sh) {
+  constexpr int kFusedTY = TY;
+  constexpr int kFusedThreads = TY * kFusedTZ;
+  constexpr int kFusedMY = TY + 4;
   const int t = threadIdx.x;
   const int ty = t / kFusedTZ, tz = t % kFusedTZ;
   const uint32_t plane_sz = uint32_t(P.ny) * uint32_t(P.nz);
   const T* const fc[2] = {f, f + size_t(19) * size_t(P.n)};
   T* const fo[2] = {fout, fout + size_t(19) * size_t(P.n)};
-  const int64_t w0 = P.work * blockIdx.x / gridDim.x;
-  const int64_t w1 = P.work * (blockIdx.x + 1) / gridDim.x;
   int64_t w = w0;
   while (w < w1) {
     const int tile = int(w / P.nx);
@@ -183,7 +184,7 @@ __global__ void __launch_bounds__(kFusedThreads, 2)
 
     // mask ring loader: plane x into slot ms, tile + two-site border
     auto load_mask = [&](int ms, int x) {
-      if (!WALLS) return;
+      if (!WALLS || mask == nullptr) return;
       const size_t base = size_t(x) * plane_sz;
       for (int i = t; i < kFusedMY * kFusedMZ; i += kFusedThreads) {
         const int my = i / kFusedMZ, mz = i % kFusedMZ;
@@ -201,7 +202,7 @@ __global__ void __launch_bounds__(kFusedThreads, 2)
       if (active) {
         const bool solid = WALLS && sh.solid[mslot[1]][ty + 2][tz + 2];
         float pop[C][19];
-        fused_gather<T, WALLS, C>(fc, sh, P, planes, yz_in, mslot, ty + 2, tz + 2, solid, pop);
+        fused_gather<T, WALLS, C, TY>(fc, sh, P, planes, yz_in, mslot, ty + 2, tz + 2, solid, pop);
 #pragma unroll
         for (int c = 0; c < C; ++c) {
           const float den = density<19, float>(pop[c]);
@@ -216,7 +217,7 @@ __global__ void __launch_bounds__(kFusedThreads, 2)
       if (has_ring) {
         const bool solid = WALLS && sh.solid[mslot[1]][rry + 2][rrz + 2];
         float pop[C][19];
-        fused_gather<T, WALLS, C>(fc, sh, P, planes, yz_ring, mslot, rry + 2, rrz + 2, solid, pop);
+        fused_gather<T, WALLS, C, TY>(fc, sh, P, planes, yz_ring, mslot, rry + 2, rrz + 2, solid, pop);
 #pragma unroll
         for (int c = 0; c < C; ++c) {
           const float den = density<19, float>(pop[c]);
@@ -376,6 +377,73 @@ __global__ void __launch_bounds__(kFusedThreads, 2)
       cur = 1 - cur;
     }
     w += run;
+  }
+}
+
+template <typename T, int C, bool WALLS, int TY>
+__global__ void __launch_bounds__(TY * kFusedTZ, 8 / TY * 2 > 4 ? 4 : 8 / TY * 2)
+    k_fused(const T* __restrict__ f, T* __restrict__ fout, const uint8_t* __restrict__ mask,
+            double* __restrict__ force_out, FusedParams P) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  FusedShared<TY>& sh = *reinterpret_cast<FusedShared<TY>*>(smem_raw);
+  const int64_t w0 = P.work * blockIdx.x / gridDim.x;
+  const int64_t w1 = P.work * (blockIdx.x + 1) / gridDim.x;
+  fused_body<T, C, WALLS, TY>(P, f, fout, mask, force_out, w0, w1, sh);
+}
+
+// One simulation of a batch.  The step reads populations f[(parity + phase)
+// & 1] and writes the other buffer.
+struct FusedSim {
+  FusedParams P;
+  const void* f[2];
+  const uint8_t* mask;     // nullptr: no solid site
+  double* force_out;       // nullptr unless recording
+  int64_t work_begin;      // first plane-tile of this simulation in the batch
+  int32_t phase;
+  int32_t pad;
+};
+
+// Many independent lattices of any sizes in one persistent launch: the
+// concatenated plane-tile work of all simulations is split into equal
+// contiguous ranges, one per CTA.
+template <typename T, int C, bool WALLS, int TY>
+__global__ void __launch_bounds__(TY * kFusedTZ, 8 / TY * 2 > 4 ? 4 : 8 / TY * 2)
+    k_fused_batch(const FusedSim* __restrict__ sims, int nsims, int64_t total_work, int parity) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  FusedShared<TY>& sh = *reinterpret_cast<FusedShared<TY>*>(smem_raw);
+  __shared__ FusedParams Ps;
+  __shared__ int s_idx;
+  const int64_t w0 = total_work * blockIdx.x / gridDim.x;
+  const int64_t w1 = total_work * (blockIdx.x + 1) / gridDim.x;
+  int64_t w = w0;
+  while (w < w1) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int lo = 0, hi = nsims - 1;  // last simulation with work_begin <= w
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (sims[mid].work_begin <= w)
+          lo = mid;
+        else
+          hi = mid - 1;
+      }
+      s_idx = lo;
+    }
+    __syncthreads();
+    const int i = s_idx;
+    // stage this simulation's parameters (FusedParams is a multiple of 4 bytes)
+    const int* src = reinterpret_cast<const int*>(&sims[i].P);
+    int* dst = reinterpret_cast<int*>(&Ps);
+    for (int k = threadIdx.x; k < int(sizeof(FusedParams) / 4); k += blockDim.x) dst[k] = src[k];
+    const int64_t wb = sims[i].work_begin;
+    const int64_t we = wb + sims[i].P.work;
+    const int64_t end = min(w1, we);
+    const int par = (parity + sims[i].phase) & 1;
+    const T* fin = static_cast<const T*>(sims[i].f[par]);
+    T* fout = const_cast<T*>(static_cast<const T*>(sims[i].f[1 - par]));
+    __syncthreads();
+    fused_body<T, C, WALLS, TY>(Ps, fin, fout, sims[i].mask, sims[i].force_out, w - wb, end - wb, sh);
+    w = end;
   }
 }
 

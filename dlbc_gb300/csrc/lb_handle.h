@@ -1,0 +1,72 @@
+// Internal definition of the lattice handle behind include/lbgpu.h, shared
+// by the single-lattice entry points (lb_api.cu) and batches (lb_batch.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/lbgpu.h"
+#include "lb_launch.h"
+
+constexpr int kHalo = 2;
+using lbk::StepParams;
+
+struct lbgpu_handle {
+  lbgpu_config cfg;
+  int d = 3, Q = 19, C = 2;
+  int nx = 1, ny = 1, nz = 1;       // kernel extents (nz = 1 for D2Q9)
+  int nxh = 1, nyh = 1, nzh = 1;    // haloed host extents
+  int hz = kHalo;                   // halo in z (0 for D2Q9)
+  int64_t n = 0;
+  cudaStream_t stream = nullptr;       // where work is queued
+  cudaStream_t own_stream = nullptr;   // created with the handle
+  void* f[2] = {nullptr, nullptr};
+  int cur = 0;
+  uint8_t* mask = nullptr;
+  void* rho = nullptr;
+  void* psi = nullptr;
+  double* force = nullptr;
+  int record_force = 0;
+  int force_valid = 0;
+  double* staging = nullptr;
+  size_t staging_bytes = 0;
+  bool owns_staging = true;         // false: borrowed from a batch
+  bool lite = false;                // batch member: no rho/psi scratch (fused step only)
+  double* moments = nullptr;        // device scratch for lbgpu_moments / lbgpu_reduce
+  size_t moments_bytes = 0;
+  StepParams P{};
+  bool uploaded = false;
+  // FP32/FP16 D3Q19 run the fused single-pass kernel; LBGPU_TWO_KERNEL=1 in
+  // the environment at lbgpu_create selects the two-kernel step instead
+  bool fused = false;
+  // per-kernel event timing (lbgpu_profile)
+  bool profiling = false;
+  std::vector<lbk::StepEvents> ev_pending, ev_pool;
+  double kernel_ms[2] = {0.0, 0.0};
+  int64_t kernel_n[2] = {0, 0};
+  int64_t launches = 0;
+  int64_t device_bytes = 0;
+  std::string err;
+
+  int fail(int code, const std::string& msg) {
+    err = msg;
+    return code;
+  }
+  int cuda_fail(cudaError_t e, const char* what) {
+    err = std::string(what) + ": " + cudaGetErrorString(e);
+    return LBGPU_E_CUDA;
+  }
+};
+
+// Create a handle.  lite: allocate only the two population buffers, borrow
+// `staging` (staging_bytes) for host transfers and queue work on `stream`
+// (batch members); otherwise own everything.
+int lb_handle_create(const lbgpu_config* cfg, bool lite, double* staging, size_t staging_bytes,
+                     cudaStream_t stream, lbgpu_handle** out, std::string* err);
+// bytes of device memory a lattice of this configuration needs as a batch member
+int64_t lb_member_bytes(const lbgpu_config* cfg);
+// scratch for lbgpu_moments / lbgpu_reduce, allocated on first use
+int lb_ensure_moments(lbgpu_handle* h);

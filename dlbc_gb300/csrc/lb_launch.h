@@ -43,3 +43,19 @@ cudaError_t launch_fused(bool half_storage, int c, const StepBuffers& b, const S
                          int64_t* launches, const StepEvents* ev, int device);
 
 }  // namespace lbk
+
+namespace lbk {
+
+struct FusedParams;
+struct FusedSim;
+
+// float parameters of the fused kernel for tiles of height ty (4 or 8)
+FusedParams make_fused_params(const StepParams& P, int ty);
+size_t fused_smem_bytes(int ty);
+
+// One timestep of every simulation in `sims` (device array, two-component,
+// D3Q19) in one persistent launch.  ctas_per_sm <= 0: as many as fit.
+cudaError_t launch_fused_batch(bool half_storage, int ty, bool walls, const FusedSim* sims, int nsims,
+                               int64_t total_work, int parity, int ctas_per_sm, cudaStream_t stream, int device);
+
+}  // namespace lbk

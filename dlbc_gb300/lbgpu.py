@@ -240,3 +240,143 @@ class GPULattice:
     @property
     def device_bytes(self) -> int:
         return int(lib().lbgpu_device_bytes(self.h))
+
+
+# ---------------------------------------------------------------------------
+# batches (lbgpu_batch_* in include/lbgpu.h)
+# ---------------------------------------------------------------------------
+EXPORTED += ["lbgpu_batch_create", "lbgpu_batch_destroy", "lbgpu_batch_add", "lbgpu_batch_remove",
+             "lbgpu_batch_step", "lbgpu_batch_member", "lbgpu_batch_set_stream", "lbgpu_batch_synchronize",
+             "lbgpu_batch_device_bytes", "lbgpu_batch_launch_count", "lbgpu_batch_set_tuning",
+             "lbgpu_batch_launch_shape", "lbgpu_batch_last_error", "lbgpu_step_noalloc"]
+
+_batch_ready = False
+
+
+def _batch_lib() -> C.CDLL:
+    global _batch_ready
+    L = lib()
+    if not _batch_ready:
+        H = C.c_void_p
+        L.lbgpu_batch_create.argtypes = [C.c_int32, C.c_int32, C.c_int64, C.POINTER(H)]
+        L.lbgpu_batch_destroy.argtypes = [H]
+        L.lbgpu_batch_destroy.restype = None
+        L.lbgpu_batch_add.argtypes = [H, C.POINTER(LbgpuConfig), C.POINTER(C.c_void_p), C.c_void_p,
+                                      C.POINTER(C.c_int32)]
+        L.lbgpu_batch_remove.argtypes = [H, C.c_int32]
+        L.lbgpu_batch_step.argtypes = [H, C.c_int32]
+        L.lbgpu_batch_member.argtypes = [H, C.c_int32]
+        L.lbgpu_batch_member.restype = H
+        L.lbgpu_batch_set_stream.argtypes = [H, C.c_void_p]
+        L.lbgpu_batch_synchronize.argtypes = [H]
+        L.lbgpu_batch_device_bytes.argtypes = [H]
+        L.lbgpu_batch_device_bytes.restype = C.c_int64
+        L.lbgpu_batch_launch_count.argtypes = [H]
+        L.lbgpu_batch_launch_count.restype = C.c_int64
+        L.lbgpu_batch_set_tuning.argtypes = [H, C.c_int32, C.c_int32, C.c_int32, C.c_int32]
+        L.lbgpu_batch_launch_shape.argtypes = [H, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
+        L.lbgpu_batch_last_error.argtypes = [H]
+        L.lbgpu_batch_last_error.restype = C.c_char_p
+        _batch_ready = True
+    return L
+
+
+class BudgetExceeded(LbgpuError):
+    """lbgpu_batch_add refused a lattice that does not fit the HBM budget."""
+
+
+class _MemberView(GPULattice):
+    """A batch member's handle (owned by the batch)."""
+
+    def __init__(self, p, precision, h):
+        self.p = p
+        self.precision = precision
+        self.h = C.c_void_p(h)
+        self.n = tuple(int(x) for x in p.gn[: p.d])
+        self.nH = tuple(x + 4 for x in self.n)
+
+    def close(self):
+        self.h = C.c_void_p()
+
+    def step(self, n: int = 1) -> None:
+        raise LbgpuError("batch members advance with Batch.step")
+
+
+class Batch:
+    """Independent lattices advanced together (lbgpu_batch_*)."""
+
+    def __init__(self, precision: int = FP16, device: int = 0, hbm_budget_bytes: int = 0):
+        self.L = _batch_lib()
+        self.precision = precision
+        self.device = device
+        self.h = C.c_void_p()
+        rc = self.L.lbgpu_batch_create(device, precision, int(hbm_budget_bytes), C.byref(self.h))
+        if rc != 0:
+            raise LbgpuError(f"lbgpu_batch_create: {ERRORS.get(rc, rc)}: "
+                             f"{self.L.lbgpu_batch_last_error(None).decode()}")
+        self.params = {}
+
+    def _check(self, rc, what):
+        if rc == -4:
+            raise BudgetExceeded(f"{what}: {self.L.lbgpu_batch_last_error(self.h).decode()}")
+        if rc != 0:
+            raise LbgpuError(f"{what}: {ERRORS.get(rc, rc)}: {self.L.lbgpu_batch_last_error(self.h).decode()}")
+
+    def add(self, p, fluids, mask=None, rho0=(0.0, 0.0)) -> int:
+        cfg = make_config(p, self.precision, self.device, rho0)
+        ptrs = (C.c_void_p * MAXC)()
+        for i, a in enumerate(fluids):
+            ptrs[i] = _ptr_of(a)
+        sid = C.c_int32()
+        self._check(self.L.lbgpu_batch_add(self.h, C.byref(cfg), ptrs, _ptr_of(mask), C.byref(sid)),
+                    "lbgpu_batch_add")
+        self.params[sid.value] = p
+        return sid.value
+
+    def remove(self, sid: int) -> None:
+        self._check(self.L.lbgpu_batch_remove(self.h, sid), "lbgpu_batch_remove")
+        self.params.pop(sid, None)
+
+    def step(self, n: int = 1) -> None:
+        self._check(self.L.lbgpu_batch_step(self.h, int(n)), "lbgpu_batch_step")
+
+    def member(self, sid: int) -> GPULattice:
+        h = self.L.lbgpu_batch_member(self.h, sid)
+        if not h:
+            raise LbgpuError(f"no batch member {sid}")
+        return _MemberView(self.params[sid], self.precision, h)
+
+    def set_stream(self, stream_handle) -> None:
+        self._check(self.L.lbgpu_batch_set_stream(self.h, stream_handle), "lbgpu_batch_set_stream")
+
+    def synchronize(self) -> None:
+        self._check(self.L.lbgpu_batch_synchronize(self.h), "lbgpu_batch_synchronize")
+
+    def set_tuning(self, autotune=True, tile_height=0, ctas_per_sm=0, use_graph=True) -> None:
+        self._check(self.L.lbgpu_batch_set_tuning(self.h, int(autotune), int(tile_height), int(ctas_per_sm),
+                                                  int(use_graph)), "lbgpu_batch_set_tuning")
+
+    def launch_shape(self):
+        ty = C.c_int32()
+        cps = C.c_int32()
+        self._check(self.L.lbgpu_batch_launch_shape(self.h, C.byref(ty), C.byref(cps)), "lbgpu_batch_launch_shape")
+        return ty.value, cps.value
+
+    @property
+    def device_bytes(self) -> int:
+        return int(self.L.lbgpu_batch_device_bytes(self.h))
+
+    @property
+    def launch_count(self) -> int:
+        return int(self.L.lbgpu_batch_launch_count(self.h))
+
+    def close(self):
+        if self.h:
+            self.L.lbgpu_batch_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -156,6 +156,43 @@ int lbgpu_kernel_time(lbgpu_handle* h, int32_t which, double* total_ms, int64_t*
 int lbgpu_step_noalloc(const lbgpu_config* cfg, const void* f_in, void* f_out, const uint8_t* mask,
                        void* stream, char* errbuf, size_t errbuf_len);
 
+/* ------------------------------------------------------------------------
+ * Batches: many independent two-component D3Q19 lattices (LBGPU_FP32 or
+ * LBGPU_FP16, any sizes) advanced together, one persistent launch per
+ * timestep over all members, replayed as a CUDA graph.  No counterpart in the
+ * reference (one lattice per process there): each member is exactly the
+ * lattice lbgpu_create would hold and steps bit-identically to it.  A batch
+ * is used from one host thread; its members are owned by it.
+ * ---------------------------------------------------------------------- */
+typedef struct lbgpu_batch lbgpu_batch;
+
+/* hbm_budget_bytes <= 0: no budget.  Members are admitted while the device
+ * memory they need (lbgpu_batch_add) fits in the budget. */
+int lbgpu_batch_create(int32_t device, int32_t precision, int64_t hbm_budget_bytes, lbgpu_batch** out);
+void lbgpu_batch_destroy(lbgpu_batch* b);
+/* Admit a lattice (same arguments as lbgpu_create + lbgpu_upload); returns
+ * LBGPU_E_BUDGET, leaving the batch unchanged, when it does not fit. */
+int lbgpu_batch_add(lbgpu_batch* b, const lbgpu_config* cfg, const double* const* fluids, const int32_t* mask,
+                    int32_t* sim_id);
+int lbgpu_batch_remove(lbgpu_batch* b, int32_t sim_id);
+/* Advance every member nsteps timesteps. */
+int lbgpu_batch_step(lbgpu_batch* b, int32_t nsteps);
+/* The member's handle, for lbgpu_download / lbgpu_moments / lbgpu_reduce /
+ * lbgpu_force (do not destroy or step it directly); NULL if removed. */
+lbgpu_handle* lbgpu_batch_member(lbgpu_batch* b, int32_t sim_id);
+int lbgpu_batch_set_stream(lbgpu_batch* b, void* stream);
+int lbgpu_batch_synchronize(lbgpu_batch* b);
+int64_t lbgpu_batch_device_bytes(const lbgpu_batch* b);
+int64_t lbgpu_batch_launch_count(const lbgpu_batch* b);
+/* Launch shape: autotune (1: time the candidate shapes on the batch's first
+ * steps and cache the choice per set of member sizes), or a fixed tile height
+ * (4 or 8 sites along y; 0 = keep tuning) and resident CTAs per SM (0 = as
+ * many as fit); use_graph 0 launches every step directly. */
+int lbgpu_batch_set_tuning(lbgpu_batch* b, int32_t autotune, int32_t tile_height, int32_t ctas_per_sm,
+                           int32_t use_graph);
+int lbgpu_batch_launch_shape(const lbgpu_batch* b, int32_t* tile_height, int32_t* ctas_per_sm);
+const char* lbgpu_batch_last_error(const lbgpu_batch* b);
+
 /* Number of kernel launches issued by this handle since creation. */
 int64_t lbgpu_launch_count(const lbgpu_handle* h);
 
