@@ -184,13 +184,14 @@ __device__ __forceinline__ void fused_body(const FusedParams& P, const T* __rest
 
     // mask ring loader: plane x into slot ms, tile + two-site border
     auto load_mask = [&](int ms, int x) {
-      if (!WALLS || mask == nullptr) return;
+      if (!WALLS) return;
       const size_t base = size_t(x) * plane_sz;
       for (int i = t; i < kFusedMY * kFusedMZ; i += kFusedThreads) {
         const int my = i / kFusedMZ, mz = i % kFusedMZ;
         if (my > tyv + 3 || mz > tzv + 3) continue;
         const int y = wrap(y0 + my - 2, P.ny), z = wrap(z0 + mz - 2, P.nz);
-        sh.solid[ms][my][mz] = __ldg(mask + base + size_t(y) * P.nz + z);
+        // a batch member without walls inside a walled batch: all fluid
+        sh.solid[ms][my][mz] = mask ? __ldg(mask + base + size_t(y) * P.nz + z) : uint8_t(0);
       }
     };
     // rho/psi of plane xg into psi slot ps (and the tile's populations into
