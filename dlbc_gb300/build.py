@@ -26,6 +26,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
 UNITS = {
     "lb_step_f64.cu": ["-fmad=false"],
     "lb_api.cu": ["-fmad=false"],
+    "lb_init.cu": ["-fmad=false"],
     "lb_step_lp.cu": [],
     "lb_fused.cu": [],
     "lb_batch.cu": [],

@@ -57,7 +57,7 @@ __device__ __forceinline__ float wq(int Q, int q) {
 }
 template <>
 __device__ __forceinline__ __half to_storage<__half>(double v, int q, int c, const StepParams& P, int Q) {
-  return __float2half_rn((float(v) - wq(Q, q) * P.rho0[c]) * P.inv_scale[c]);
+  return __float2half_rn((float(v) * (1.0f / wq(Q, q)) - P.rho0[c]) * P.inv_scale[c]);
 }
 
 template <typename T>
@@ -72,7 +72,7 @@ __device__ __forceinline__ double from_storage<float>(float v, int, int, const S
 }
 template <>
 __device__ __forceinline__ double from_storage<__half>(__half v, int q, int c, const StepParams& P, int Q) {
-  return double(wq(Q, q) * P.rho0[c] + P.scale[c] * __half2float(v));
+  return double(wq(Q, q) * fmaf(P.scale[c], __half2float(v), P.rho0[c]));
 }
 
 struct Geo {
@@ -503,7 +503,7 @@ int lbgpu_upload(lbgpu_handle* h, const double* const* fluids, const int32_t* ma
       double rho0 = h->cfg.rho0[c];
       double maxdev = 0.0;
       const double* a = fluids[c];
-      // mean density and the largest |f_q - w_q rho0| over physical sites
+      // mean density and the largest |f_q / w_q - rho0| over physical sites
       double sum = 0.0;
       int64_t cnt = 0;
       for (int x = kHalo; x < h->nx + kHalo; ++x)
@@ -522,11 +522,12 @@ int lbgpu_upload(lbgpu_handle* h, const double* const* fluids, const int32_t* ma
             const double* p = a + ((int64_t(x) * h->nyh + y) * h->nzh + z) * h->Q;
             for (int q = 0; q < h->Q; ++q) {
               const double w = h->Q == 19 ? lbk::weight<19, double>(q) : lbk::weight<9, double>(q);
-              maxdev = std::max(maxdev, fabs(p[q] - w * rho0));
+              maxdev = std::max(maxdev, fabs(p[q] / w - rho0));
             }
           }
-      // offsets of up to 4x the initial spread stay inside half's normal range
-      // with ~11 significant bits; the scale maps that spread to 2^12
+      // the initial spread maps to |h| <= 1024: deviations may grow 64-fold
+      // before they leave half's range, and every direction keeps ~11
+      // significant bits of its own weight-normalised offset
       double scale = maxdev > 0.0 ? (4.0 * maxdev) / 4096.0 : 1.0 / 4096.0;
       h->P.rho0[c] = float(rho0);
       h->P.scale[c] = float(scale);

@@ -323,9 +323,13 @@ void lbgpu_batch_destroy(lbgpu_batch* b) {
 
 const char* lbgpu_batch_last_error(const lbgpu_batch* b) { return b ? b->err.c_str() : g_batch_create_error.c_str(); }
 
-int lbgpu_batch_add(lbgpu_batch* b, const lbgpu_config* cfg, const double* const* fluids, const int32_t* mask,
-                    int32_t* sim_id) {
-  if (!b || !cfg || !fluids || !sim_id) return LBGPU_E_INVALID;
+}  // extern "C"
+
+namespace {
+
+// admit a member whose fields are filled by `fill` (upload or device init)
+template <typename Fill>
+int batch_admit(lbgpu_batch* b, const lbgpu_config* cfg, int32_t* sim_id, Fill fill) {
   if (cfg->precision != b->precision) return b->fail(LBGPU_E_INVALID, "member precision differs from the batch's");
   if (cfg->q != 19 || cfg->components != 2)
     return b->fail(LBGPU_E_INVALID, "batch members are two-component D3Q19 lattices");
@@ -339,7 +343,7 @@ int lbgpu_batch_add(lbgpu_batch* b, const lbgpu_config* cfg, const double* const
   lbgpu_handle* h = nullptr;
   int rc = lb_handle_create(cfg, true, b->staging, kBatchStaging, b->stream, &h, &why);
   if (rc) return b->fail(rc, why);
-  rc = lbgpu_upload(h, fluids, mask);
+  rc = fill(h);
   if (rc) {
     b->err = lbgpu_last_error(h);
     lbgpu_destroy(h);
@@ -352,6 +356,21 @@ int lbgpu_batch_add(lbgpu_batch* b, const lbgpu_config* cfg, const double* const
   b->dirty = true;
   *sim_id = int32_t(b->sims.size() - 1);
   return LBGPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int lbgpu_batch_add(lbgpu_batch* b, const lbgpu_config* cfg, const double* const* fluids, const int32_t* mask,
+                    int32_t* sim_id) {
+  if (!b || !cfg || !fluids || !sim_id) return LBGPU_E_INVALID;
+  return batch_admit(b, cfg, sim_id, [&](lbgpu_handle* h) { return lbgpu_upload(h, fluids, mask); });
+}
+
+int lbgpu_batch_add_init(lbgpu_batch* b, const lbgpu_config* cfg, const lbgpu_init* ini, int32_t* sim_id) {
+  if (!b || !cfg || !ini || !sim_id) return LBGPU_E_INVALID;
+  return batch_admit(b, cfg, sim_id, [&](lbgpu_handle* h) { return lbgpu_init_fields(h, ini); });
 }
 
 int lbgpu_batch_remove(lbgpu_batch* b, int32_t sim_id) {

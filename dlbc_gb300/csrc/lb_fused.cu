@@ -36,7 +36,11 @@ FusedParams make_fused_params(const StepParams& P, int ty) {
   for (int i = 0; i < 3; ++i) F.acc[i] = float(P.acc[i]);
   for (int q = 0; q < 19; ++q) {
     F.qn[q] = uint32_t(int64_t(q) * P.n);
-    for (int c = 0; c < 2; ++c) F.wrho[c][q] = weight<19, float>(q) * P.rho0[c];
+    for (int c = 0; c < 2; ++c) {
+      F.wrho[c][q] = weight<19, float>(q) * P.rho0[c];
+      F.wscale[c][q] = weight<19, float>(q) * P.scale[c];
+      F.inv_wscale[c][q] = 1.0f / F.wscale[c][q];
+    }
   }
   return F;
 }

@@ -52,7 +52,9 @@ struct FusedParams {
   float gcc[2][2], gwc[2], acc[3];
   float rho0[2], scale[2], inv_scale[2];
   uint32_t qn[19];         // q * n: population q's offset inside a component (19 n < 2^32)
-  float wrho[2][19];       // w_q * rho0_c (half-offset storage)
+  float wrho[2][19];       // w_q * rho0_c (half storage: f_q = w_q rho0_c + w_q scale_c h)
+  float wscale[2][19];     // w_q * scale_c
+  float inv_wscale[2][19]; // 1 / (w_q * scale_c)
 };
 
 template <typename T>
@@ -69,14 +71,14 @@ struct FStore<float> {
 template <>
 struct FStore<__half> {
   __device__ static __forceinline__ float load(const __half* p, int c, int q, const FusedParams& P) {
-    return fmaf(P.scale[c], __half2float(__ldg(p)), P.wrho[c][q]);
+    return fmaf(P.wscale[c][q], __half2float(__ldg(p)), P.wrho[c][q]);
   }
   __device__ static __forceinline__ float load2(const __half* p, int c, int q, int b, bool bb,
                                                 const FusedParams& P) {
-    return fmaf(P.scale[c], __half2float(__ldg(p)), bb ? P.wrho[c][b] : P.wrho[c][q]);
+    return fmaf(bb ? P.wscale[c][b] : P.wscale[c][q], __half2float(__ldg(p)), bb ? P.wrho[c][b] : P.wrho[c][q]);
   }
   __device__ static __forceinline__ void store(__half* p, float v, int c, int q, const FusedParams& P) {
-    *p = __float2half_rn((v - P.wrho[c][q]) * P.inv_scale[c]);
+    *p = __float2half_rn((v - P.wrho[c][q]) * P.inv_wscale[c][q]);
   }
 };
 

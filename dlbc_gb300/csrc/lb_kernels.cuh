@@ -40,7 +40,7 @@ struct StepParams {
   double gcc[2][2];
   double gwc[2];
   double acc[3];
-  // FP16 offset storage: f = w_q*rho0 + scale*h
+  // FP16 storage of weight-normalised offsets: f_q = w_q * (rho0 + scale*h)
   float rho0[2];
   float scale[2];
   float inv_scale[2];
@@ -68,10 +68,10 @@ template <typename R, int Q>
 struct Store<__half, R, Q> {
   __device__ static __forceinline__ R load(const __half* p, int c, int q, const StepParams& P) {
     const float h = __half2float(__ldg(p));
-    return R(weight<Q, float>(q) * P.rho0[c] + P.scale[c] * h);
+    return R(weight<Q, float>(q) * fmaf(P.scale[c], h, P.rho0[c]));
   }
   __device__ static __forceinline__ void store(__half* p, R v, int c, int q, const StepParams& P) {
-    *p = __float2half_rn((float(v) - weight<Q, float>(q) * P.rho0[c]) * P.inv_scale[c]);
+    *p = __float2half_rn((float(v) * (1.0f / weight<Q, float>(q)) - P.rho0[c]) * P.inv_scale[c]);
   }
 };
 

@@ -380,3 +380,82 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+# ---------------------------------------------------------------------------
+# device-side initial fields (lbgpu_init_fields / lbgpu_batch_add_init)
+# ---------------------------------------------------------------------------
+EXPORTED += ["lbgpu_init_fields", "lbgpu_batch_add_init"]
+
+
+class LbgpuInit(C.Structure):
+    _fields_ = [
+        ("fluid_init", C.c_int32 * MAXC), ("n_densities", C.c_int32 * MAXC),
+        ("densities", (C.c_double * 8) * MAXC), ("perturb", C.c_double * MAXC), ("seed", C.c_uint64),
+        ("init_radius", C.c_double), ("init_offset", C.c_double * 3), ("init_separation", C.c_double * 3),
+        ("init_axis", C.c_int32), ("interface_thickness", C.c_double), ("n_lamellae", C.c_int32),
+        ("lamellae_widths", C.c_double * 8), ("mask_init", C.c_int32), ("mask_axis", C.c_int32),
+        ("wall_offset", C.c_int32), ("wall_thickness", C.c_int32), ("dimension_has_wall", (C.c_int32 * 2) * 3),
+    ]
+
+
+def make_init(p, seed: int = 0) -> LbgpuInit:
+    """Device initialiser description from :class:`dlbc_gb300.params.LBParams`."""
+    ini = LbgpuInit()
+    for f in range(p.components):
+        ini.fluid_init[f] = p.fluid_init[f]
+        dens = p.fluid_densities[f]
+        ini.n_densities[f] = len(dens)
+        for j, v in enumerate(dens[:8]):
+            ini.densities[f][j] = v
+        ini.perturb[f] = p.fluid_perturb[f]
+    ini.seed = seed & 0xFFFFFFFFFFFFFFFF
+    ini.init_radius = p.init_radius
+    for i in range(p.d):
+        ini.init_offset[i] = p.init_offset[i]
+        ini.init_separation[i] = p.init_separation[i]
+        ini.dimension_has_wall[i][0] = int(p.dimension_has_wall[i][0])
+        ini.dimension_has_wall[i][1] = int(p.dimension_has_wall[i][1])
+    ini.init_axis = p.init_axis
+    ini.interface_thickness = p.interface_thickness
+    ini.n_lamellae = len(p.lamellae_widths)
+    for j, w in enumerate(p.lamellae_widths[:8]):
+        ini.lamellae_widths[j] = w
+    ini.mask_init = p.mask_init
+    ini.mask_axis = p.mask_axis
+    ini.wall_offset = p.wall_offset
+    ini.wall_thickness = p.wall_thickness
+    return ini
+
+
+def _init_lib():
+    L = _batch_lib()
+    if not getattr(L, "_init_ready", False):
+        L.lbgpu_init_fields.argtypes = [C.c_void_p, C.POINTER(LbgpuInit)]
+        L.lbgpu_batch_add_init.argtypes = [C.c_void_p, C.POINTER(LbgpuConfig), C.POINTER(LbgpuInit),
+                                           C.POINTER(C.c_int32)]
+        L._init_ready = True
+    return L
+
+
+def _gpulattice_init_device(self, seed: int = 0) -> None:
+    """Fill the lattice on the device from its parameters (lbgpu_init_fields)."""
+    ini = make_init(self.p, seed)
+    self._check(_init_lib().lbgpu_init_fields(self.h, C.byref(ini)), "lbgpu_init_fields")
+
+
+GPULattice.init_device = _gpulattice_init_device
+
+
+def _batch_add_device(self, p, seed: int = 0, rho0=(0.0, 0.0)) -> int:
+    """Admit a lattice whose initial fields are computed on the device."""
+    cfg = make_config(p, self.precision, self.device, rho0)
+    ini = make_init(p, seed)
+    sid = C.c_int32()
+    self._check(_init_lib().lbgpu_batch_add_init(self.h, C.byref(cfg), C.byref(ini), C.byref(sid)),
+                "lbgpu_batch_add_init")
+    self.params[sid.value] = p
+    return sid.value
+
+
+Batch.add_device = _batch_add_device

@@ -95,6 +95,44 @@ int lbgpu_upload(lbgpu_handle* h, const double* const* fluids, const int32_t* ma
  * body, src/main.d:175-199, without dumpData). */
 int lbgpu_step(lbgpu_handle* h, int32_t nsteps);
 
+/* Initial fields computed on the device (no host arrays cross the bus): the
+ * deterministic initialisers of initFluids/initMask (src/dlbc/lb/init.d:139-339,
+ * src/dlbc/fields/init.d) for one process.  Sphere, cylinder, two-sphere and
+ * lamellae initialisers (and their Frac forms), EqDist, Const and every mask
+ * but File give exactly the values the reference computes.  The random
+ * initialisers (EqDistPerturb, EqDistPerturbFrac, EqDistRandom, ConstRandom)
+ * draw from a counter-based generator keyed by `seed`, component and site,
+ * not from the reference's sequential Mt19937 stream: same distribution,
+ * different numbers (use lbgpu_upload with host-generated fields to
+ * reproduce a reference run exactly).  FluidInit/MaskInit codes are the
+ * reference's enum orders (FluidInit: None 0, File 1, Const 2, EqDist 3,
+ * EqDistPerturb 4, EqDistPerturbFrac 5, ConstRandom 6, EqDistRandom 7,
+ * EqDistSphere 8, EqDistSphereFrac 9, EqDistCylinder 10, EqDistCylinderFrac 11,
+ * EqDistTwoSpheres 12, EqDistTwoSpheresFrac 13, EqDistLamellae 14,
+ * EqDistLamellaeFrac 15; MaskInit: None 0, File 1, Plates 2, Tube 3, Box 4,
+ * Walls 5). */
+typedef struct lbgpu_init {
+  int32_t fluid_init[LBGPU_MAX_COMPONENTS];      /* lb.init.fluidInit */
+  int32_t n_densities[LBGPU_MAX_COMPONENTS];
+  double densities[LBGPU_MAX_COMPONENTS][8];     /* lb.init.fluidDensities */
+  double perturb[LBGPU_MAX_COMPONENTS];          /* lb.init.fluidPerturb */
+  uint64_t seed;
+  double init_radius;                            /* lb.init.initRadius */
+  double init_offset[3];                         /* lb.init.initOffset */
+  double init_separation[3];                     /* lb.init.initSeparation */
+  int32_t init_axis;                             /* lb.init.initAxis (0 X, 1 Y, 2 Z) */
+  double interface_thickness;                    /* lb.init.interfaceThickness */
+  int32_t n_lamellae;
+  double lamellae_widths[8];                     /* lb.init.lamellaeWidths */
+  int32_t mask_init;                             /* lb.mask.maskInit */
+  int32_t mask_axis;                             /* lb.mask.initAxis */
+  int32_t wall_offset;                           /* lb.mask.wallOffset */
+  int32_t wall_thickness;                        /* lb.mask.wallThickness */
+  int32_t dimension_has_wall[3][2];              /* lb.mask.dimensionHasWall */
+} lbgpu_init;
+
+int lbgpu_init_fields(lbgpu_handle* h, const lbgpu_init* ini);
+
 /* Copy the current populations back into haloed AoS host arrays (halo sites
  * are filled with their periodic images, as after exchangeHalo). */
 int lbgpu_download(lbgpu_handle* h, double* const* fluids);
@@ -174,6 +212,8 @@ void lbgpu_batch_destroy(lbgpu_batch* b);
  * LBGPU_E_BUDGET, leaving the batch unchanged, when it does not fit. */
 int lbgpu_batch_add(lbgpu_batch* b, const lbgpu_config* cfg, const double* const* fluids, const int32_t* mask,
                     int32_t* sim_id);
+/* lbgpu_batch_add with device-side initial fields (lbgpu_init_fields) */
+int lbgpu_batch_add_init(lbgpu_batch* b, const lbgpu_config* cfg, const lbgpu_init* ini, int32_t* sim_id);
 int lbgpu_batch_remove(lbgpu_batch* b, int32_t sim_id);
 /* Advance every member nsteps timesteps. */
 int lbgpu_batch_step(lbgpu_batch* b, int32_t nsteps);
