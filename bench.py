@@ -184,6 +184,108 @@ def cpu_baseline(p, budget_s=12.0, threads=None):
                       f"step (FP64 oracle, OpenMP over x-slabs)"}
 
 
+def batched_params(n_sims=256, seed=3):
+    """The batched workload: cubic periodic lattices, L in {32, 48, 64, 80, 96}, two red
+    spheres of radius L/6 with a 2-site gap along x in a blue bath, tau ~
+    U[0.8, 1.2] (both components), g ~ U[3.2, 4.0]."""
+    import numpy as np
+    from dlbc_gb300 import params
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n_sims):
+        L = int(rng.choice([32, 48, 64, 80, 96]))
+        tau = float(rng.uniform(0.8, 1.2))
+        g = float(rng.uniform(3.2, 4.0))
+        r = L / 6.0
+        lines = [
+            "[lattice]", f"gn = [{L}, {L}, {L}]",
+            "[lb]", "components = 2", 'fieldNames = ["red", "blue"]', f"tau = [{tau!r}, {tau!r}]",
+            "eqdist.eqDistForm = BDist2", "force.enableShanChen = true",
+            f"force.gcc = [[0.0, {g!r}], [{g!r}, 0.0]]", "force.psiForm = Exponential",
+            "force.globalAcc = [0.0, 0.0, 0.0]",
+            "init.fluidInit = [EqDistTwoSpheres, EqDistTwoSpheres]",
+            "init.fluidDensities = [[1.0, 0.05], [0.05, 1.0]]",
+            f"init.initRadius = {r!r}", f"init.initSeparation = [{2 * r + 2!r}, 0.0, 0.0]",
+            "init.interfaceThickness = 0.0",
+        ]
+        out.append(params.LBParams.from_dict(params.parse_lines(lines), "d3q19"))
+    return out
+
+
+def run_batched(device, torch, n_sims=256, steps=2000, baseline_steps=20):
+    """The batched workload in one batch (FP16 offset storage, FP32 arithmetic), timed with
+    CUDA events on the batch's stream; the sequential baseline runs each size
+    class alone in the plain FP64 form for a few steps and extrapolates."""
+    from dlbc_gb300 import lbgpu
+    ps = batched_params(n_sims)
+    b = lbgpu.Batch(precision=lbgpu.FP16, device=device)
+    for p in ps:
+        b.add_device(p)
+    stream = torch.cuda.Stream(device=device)
+    b.set_stream(stream.cuda_stream)
+    b.step(12)  # autotune (8 steps) + graph capture, untimed
+    b.synchronize()
+    shape = b.launch_shape()
+    start = torch.cuda.Event(enable_timing=True)
+    stop = torch.cuda.Event(enable_timing=True)
+    n0 = b.launch_count
+    start.record(stream)
+    b.step(steps)
+    stop.record(stream)
+    stop.synchronize()
+    ms = start.elapsed_time(stop)
+    launches = b.launch_count - n0
+    sites = sum(p.gn[0] * p.gn[1] * p.gn[2] for p in ps)
+    dev_bytes = b.device_bytes
+    b.close()
+    # sequential plain-form baseline per size class
+    per_step = {}
+    for L in sorted({p.gn[0] for p in ps}):
+        p = next(q for q in ps if q.gn[0] == L)
+        g = lbgpu.GPULattice(p, precision=lbgpu.FP64, device=device)
+        g.init_device()
+        g.step(3)
+        g.synchronize()
+        t0 = time.perf_counter()
+        g.step(baseline_steps)
+        g.synchronize()
+        per_step[L] = (time.perf_counter() - t0) / baseline_steps
+        g.close()
+    seq_s = sum(per_step[p.gn[0]] * steps for p in ps)
+    return {
+        "workload": f"{n_sims} periodic D3Q19 two-sphere lattices, L in {{32,48,64,80,96}}, {steps} steps, "
+                    f"tau~U[0.8,1.2], g~U[3.2,4.0]",
+        "form": "fp16 offset storage, fp32 arithmetic", "sims": n_sims, "steps": steps,
+        "total_sites": int(sites), "time_s": round(ms / 1e3, 3), "sims_per_s": round(n_sims / (ms / 1e3), 3),
+        "aggregate_mlups": round(sites * steps / (ms / 1e3) / 1e6, 1), "launch_shape": list(shape),
+        "kernel_launches": launches, "device_bytes": int(dev_bytes),
+        "sequential_fp64_baseline": {"sims_per_s": round(n_sims / seq_s, 4), "time_s": round(seq_s, 1),
+                                     "how": f"each size class alone, plain FP64 form, {baseline_steps} timed "
+                                            f"steps, extrapolated to {steps} steps x {n_sims} sims"},
+        "speedup_vs_sequential_fp64": round(seq_s / (ms / 1e3), 1),
+    }
+
+
+def run_served(device, n_requests=32, step_scale=0.1, rate=50.0, budget_gb=120.0):
+    """The served workload (request steps scaled by step_scale to keep the run short):
+    Poisson arrivals, admission by an HBM budget, continuous batching."""
+    import numpy as np
+    from dlbc_gb300 import lbgpu, serve
+    reqs = serve.request_stream(n_requests, rate=rate, seed=2024, step_scale=step_scale)
+    srv = serve.Server(precision=lbgpu.FP16, budget_bytes=budget_gb * 1e9, device=device)
+    out = srv.run(reqs)
+    out.pop("results")
+    mean_work = float(np.mean([r.sites * r.steps for r in reqs]))
+    out["sustainable_rate_per_s"] = round(out["aggregate_mlups"] * 1e6 / mean_work, 3)
+    out["sustainable_rate_per_s_full_length"] = round(out["aggregate_mlups"] * 1e6 / (mean_work / step_scale), 4)
+    out["workload"] = (f"{n_requests} droplet-channel requests, Poisson {rate}/s, x~U[48,256], y=z~U[32,128], "
+                       f"radius~U[6,y/4], steps~U[2000,20000] x {step_scale}, acc~U[0,1e-5], "
+                       f"budget {budget_gb} GB, fp16 storage")
+    for k in ("p50_latency_s", "p99_latency_s", "makespan_s", "aggregate_mlups"):
+        out[k] = round(out[k], 3)
+    return out
+
+
 def run_reference(args):
     """--impl reference: the reference's CPU algorithm (the oracle) on all host threads."""
     rank = int(os.environ.get("RANK", "0"))
@@ -224,6 +326,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-forms", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--form", default="fp64", choices=["fp64", "fp32", "fp16"],
                     help="headline form (the others are reported under 'forms')")
     ap.add_argument("--lattice", default=None,
@@ -322,6 +426,9 @@ def main():
                            "step_roofline_frac": round(bytes_per_site(prec) * sites / (f_ms * 1e-3) / 1e9 / peak,
                                                        4)}
 
+    batched = None if args.no_batched else run_batched(device, torch)
+    served = None if args.no_served else run_served(device)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(p)
@@ -343,6 +450,8 @@ def main():
             "gpu_launches": launches,
             "clocks": clk.summary(),
             "forms": forms,
+            "batched": batched,
+            "served": served,
         }
         print(json.dumps(line), flush=True)
     if dist is not None:
