@@ -1,0 +1,94 @@
+"""Precision study: FP32 and FP16-offset storage against FP64 on a large
+spinodal decomposition.
+
+Two-component D3Q19 Shan-Chen, periodic, rho = 0.7 +- `perturb` per site and
+component (device-side counter-based noise, the same initial state for every
+form up to the storage rounding), tau = 1, g = 3.6, psi = 1 - exp(-rho),
+BDist2.  Every form runs the same number of steps from the same initial
+fields; the FP64 form is the reference for the errors (it is bit-identical to
+the CPU restatement of the reference, checked at small sizes by the tests).
+
+Reported per form: time and MLUPS, relative L2 error of each component's
+density and velocity against FP64 at checkpoints, and the fraction of sites
+whose phase (sign of rho_red - rho_blue) differs from FP64's (the interface
+position error).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import time
+
+import numpy as np
+
+from . import lbgpu, params
+
+
+def spinodal_params(n: int, perturb: float) -> params.LBParams:
+    lines = [
+        "[lattice]", f"gn = [{n}, {n}, {n}]",
+        "[lb]", "components = 2", 'fieldNames = ["red", "blue"]', "tau = [1.0, 1.0]",
+        "eqdist.eqDistForm = BDist2", "force.enableShanChen = true",
+        "force.gcc = [[0.0, 3.6], [3.6, 0.0]]", "force.psiForm = Exponential",
+        "force.globalAcc = [0.0, 0.0, 0.0]",
+        "init.fluidInit = [EqDistPerturb, EqDistPerturb]", "init.fluidDensities = [[0.7], [0.7]]",
+        f"init.fluidPerturb = [{perturb}, {perturb}]",
+    ]
+    return params.LBParams.from_dict(params.parse_lines(lines), "d3q19")
+
+
+def run_form(p, precision, steps, checkpoints, seed, device=0):
+    g = lbgpu.GPULattice(p, precision=precision, device=device)
+    g.init_device(seed)
+    out = {}
+    done = 0
+    t_total = 0.0
+    for cp in checkpoints:
+        g.synchronize()
+        t0 = time.perf_counter()
+        g.step(cp - done)
+        g.synchronize()
+        t_total += time.perf_counter() - t0
+        done = cp
+        dens = g.density()
+        vel = g.velocity()
+        out[cp] = ([d.astype(np.float64) for d in dens], [v.astype(np.float64) for v in vel])
+    g.close()
+    return out, t_total
+
+
+def rel_l2(a, b):
+    return float(np.linalg.norm((a - b).ravel()) / np.linalg.norm(b.ravel()))
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--n", type=int, default=512)
+    ap.add_argument("--steps", type=int, default=5000)
+    ap.add_argument("--perturb", type=float, default=0.02)
+    ap.add_argument("--seed", type=int, default=11)
+    ap.add_argument("--checkpoints", default="500,1000,2000,5000")
+    args = ap.parse_args()
+    cps = sorted({int(c) for c in args.checkpoints.split(",") if int(c) <= args.steps} | {args.steps})
+    p = spinodal_params(args.n, args.perturb)
+    sites = args.n ** 3
+    ref, t64 = run_form(p, lbgpu.FP64, args.steps, cps, args.seed)
+    report = {"workload": f"{args.n}^3 periodic spinodal decomposition, rho 0.7 +- {args.perturb}, "
+                          f"{args.steps} steps, BDist2, g 3.6",
+              "fp64": {"time_s": round(t64, 2), "mlups": round(sites * args.steps / t64 / 1e6, 1)}}
+    for name, prec in (("fp32", lbgpu.FP32), ("fp16", lbgpu.FP16)):
+        res, t = run_form(p, prec, args.steps, cps, args.seed)
+        errs = {}
+        for cp in cps:
+            (d, v), (d64, v64) = res[cp], ref[cp]
+            phase = np.mean(np.sign(d[0] - d[1]) != np.sign(d64[0] - d64[1]))
+            errs[cp] = {"rho_l2": [rel_l2(d[c], d64[c]) for c in range(2)],
+                        "u_l2": [rel_l2(v[c], v64[c]) for c in range(2)],
+                        "phase_mismatch_fraction": float(phase)}
+        report[name] = {"time_s": round(t, 2), "mlups": round(sites * args.steps / t / 1e6, 1), "errors": errs}
+        del res
+    print(json.dumps(report))
+
+
+if __name__ == "__main__":
+    main()
