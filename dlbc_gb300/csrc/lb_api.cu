@@ -615,9 +615,46 @@ int lbgpu_set_record_force(lbgpu_handle* h, int32_t enable) {
   return LBGPU_OK;
 }
 
+static int run_phase(lbgpu_handle* h, int phase) {
+  if (!h) return LBGPU_E_INVALID;
+  if (!h->uploaded) return h->fail(LBGPU_E_NOTREADY, "timestep phase before lbgpu_upload");
+  if (h->lite || !h->rho) return h->fail(LBGPU_E_INVALID, "batch members step with their batch");
+  if (phase == lbk::kPhaseAdvect && h->advected)
+    return h->fail(LBGPU_E_NOTREADY, "lbgpu_advect twice: lbgpu_collide completes the timestep");
+  if (phase == lbk::kPhaseCollide && !h->advected)
+    return h->fail(LBGPU_E_NOTREADY, "lbgpu_collide without lbgpu_advect");
+  cudaSetDevice(h->cfg.device);
+  lbk::StepBuffers b;
+  b.f = h->f[h->cur];
+  b.fout = h->f[1 - h->cur];
+  b.mask = h->mask;
+  b.rho = h->rho;
+  b.psi = h->psi;
+  b.force = h->force;
+  StepParams P = h->P;
+  P.record_force = (h->record_force && phase == lbk::kPhaseCollide) ? 1 : 0;
+  cudaError_t e;
+  if (h->cfg.precision == LBGPU_FP64)
+    e = lbk::launch_phase_f64(phase, h->Q, h->C, b, P, h->stream, &h->launches);
+  else if (h->cfg.precision == LBGPU_FP32)
+    e = lbk::launch_phase_f32(phase, h->Q, h->C, b, P, h->stream, &h->launches);
+  else
+    e = lbk::launch_phase_f16(phase, h->Q, h->C, b, P, h->stream, &h->launches);
+  if (e != cudaSuccess) return h->cuda_fail(e, "phase launch");
+  h->cur = 1 - h->cur;
+  h->advected = phase == lbk::kPhaseAdvect;
+  if (P.record_force) h->force_valid = 1;
+  return LBGPU_OK;
+}
+
+int lbgpu_advect(lbgpu_handle* h) { return run_phase(h, lbk::kPhaseAdvect); }
+
+int lbgpu_collide(lbgpu_handle* h) { return run_phase(h, lbk::kPhaseCollide); }
+
 int lbgpu_step(lbgpu_handle* h, int32_t nsteps) {
   if (!h || nsteps < 0) return LBGPU_E_INVALID;
   if (!h->uploaded) return h->fail(LBGPU_E_NOTREADY, "lbgpu_step before lbgpu_upload");
+  if (h->advected) return h->fail(LBGPU_E_NOTREADY, "lbgpu_step between lbgpu_advect and lbgpu_collide");
   cudaSetDevice(h->cfg.device);
   for (int t = 0; t < nsteps; ++t) {
     lbk::StepBuffers b;
@@ -813,10 +850,10 @@ int lbgpu_reduce(lbgpu_handle* h, double* mass, double* momentum) {
   e = cudaMemcpyAsync(res, out, sizeof res, cudaMemcpyDeviceToHost, h->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
   if (e != cudaSuccess) return h->cuda_fail(e, "reduce");
-  for (int c = 0; c < h->C; ++c) {
+  for (int c = 0; c < h->C && c < 2; ++c) {
     if (mass) mass[c] = res[c * 4];
     if (momentum)
-      for (int vd = 0; vd < h->d; ++vd) momentum[c * h->d + vd] = res[c * 4 + 1 + vd];
+      for (int vd = 0; vd < h->d && vd < 3; ++vd) momentum[c * h->d + vd] = res[c * 4 + 1 + vd];
   }
   return LBGPU_OK;
 }

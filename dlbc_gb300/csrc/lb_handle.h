@@ -39,6 +39,7 @@ struct lbgpu_handle {
   size_t moments_bytes = 0;
   StepParams P{};
   bool uploaded = false;
+  bool advected = false;            // between lbgpu_advect and lbgpu_collide
   // FP32/FP16 D3Q19 run the fused single-pass kernel; LBGPU_TWO_KERNEL=1 in
   // the environment at lbgpu_create selects the two-kernel step instead
   bool fused = false;

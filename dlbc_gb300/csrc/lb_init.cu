@@ -450,6 +450,7 @@ extern "C" int lbgpu_init_fields(lbgpu_handle* h, const lbgpu_init* ini) {
     h->mask = nullptr;
   }
   h->uploaded = true;
+  h->advected = false;
   h->force_valid = 0;
   return LBGPU_OK;
 }

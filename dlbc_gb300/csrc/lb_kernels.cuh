@@ -136,7 +136,7 @@ __device__ __forceinline__ void load_local(const T* __restrict__ f, int64_t s, i
 // ---------------------------------------------------------------------------
 // kernel 1: densities and psi after streaming, at every site
 // ---------------------------------------------------------------------------
-template <typename T, typename R, int Q, int C, bool WALLS>
+template <typename T, typename R, int Q, int C, bool WALLS, bool STREAM = true>
 __global__ void __launch_bounds__(128) k_density_psi(const T* __restrict__ f, const uint8_t* __restrict__ mask,
                                                      R* __restrict__ rho, R* __restrict__ psi, StepParams P) {
   const int64_t s = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -146,7 +146,7 @@ __global__ void __launch_bounds__(128) k_density_psi(const T* __restrict__ f, co
 #pragma unroll
   for (int c = 0; c < C; ++c) {
     R pop[Q];
-    if (solid)
+    if (solid || !STREAM)
       load_local<T, R, Q>(f, s, c, P, pop);
     else
       gather<T, R, Q, WALLS>(f, mask, S, s, c, P, pop);
@@ -160,7 +160,7 @@ __global__ void __launch_bounds__(128) k_density_psi(const T* __restrict__ f, co
 // ---------------------------------------------------------------------------
 // kernel 2: force + collision, writes the new populations
 // ---------------------------------------------------------------------------
-template <typename T, typename R, int Q, int C, bool WALLS>
+template <typename T, typename R, int Q, int C, bool WALLS, bool STREAM = true>
 __global__ void __launch_bounds__(128) k_collide(const T* __restrict__ f, T* __restrict__ fout,
                                                  const uint8_t* __restrict__ mask, const R* __restrict__ rho,
                                                  const R* __restrict__ psi, double* __restrict__ force_out,
@@ -268,7 +268,12 @@ __global__ void __launch_bounds__(128) k_collide(const T* __restrict__ f, T* __r
   // --- populations after streaming
   R pop[C][Q];
 #pragma unroll
-  for (int c = 0; c < C; ++c) gather<T, R, Q, WALLS>(f, mask, S, s, c, P, pop[c]);
+  for (int c = 0; c < C; ++c) {
+    if (STREAM)
+      gather<T, R, Q, WALLS>(f, mask, S, s, c, P, pop[c]);
+    else
+      load_local<T, R, Q>(f, s, c, P, pop[c]);
+  }
 
   // --- BDist2 weighted velocity (collision.d:256-296)
   R wv[3] = {R(0), R(0), R(0)};
@@ -312,6 +317,42 @@ __global__ void __launch_bounds__(128) k_collide(const T* __restrict__ f, T* __r
 #pragma unroll
       for (int q = 0; q < Q; ++q)
         Store<T, R, Q>::store(oc + int64_t(q) * P.n + s, pop[c][q] * omo + omega * eq[q], c, q, P);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// advection alone (advectFieldsKernel src/dlbc/lb/advection.d:61-89), for the
+// phase-split timestep: fout = pull-streamed f at fluid sites (bounce-back
+// from solid neighbours), f copied at solid sites.  The stored values move
+// unconverted, so advection followed by k_density_psi/k_collide with
+// STREAM = false is bit for bit the streamed two-kernel step.
+// ---------------------------------------------------------------------------
+template <typename T, int Q, int C, bool WALLS>
+__global__ void __launch_bounds__(128) k_advect(const T* __restrict__ f, T* __restrict__ fout,
+                                                const uint8_t* __restrict__ mask, StepParams P) {
+  const int64_t s = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (s >= P.n) return;
+  const bool solid = WALLS && mask[s];
+  const Site S = make_site(s, P);
+#pragma unroll
+  for (int c = 0; c < C; ++c) {
+    const T* fc = f + int64_t(c) * Q * P.n;
+    T* oc = fout + int64_t(c) * Q * P.n;
+    oc[s] = fc[s];
+#pragma unroll
+    for (int q = 1; q < Q; ++q) {
+      T v;
+      if (solid) {
+        v = fc[int64_t(q) * P.n + s];
+      } else {
+        const int64_t nb = nb_index<Q>(S, q, -1, P);
+        if (WALLS && __ldg(mask + nb))
+          v = fc[int64_t(Conn<Q>::bounce(q)) * P.n + s];
+        else
+          v = fc[int64_t(q) * P.n + nb];
+      }
+      oc[int64_t(q) * P.n + s] = v;
     }
   }
 }

@@ -33,6 +33,17 @@ cudaError_t launch_step_f32(int q, int c, const StepBuffers& b, const StepParams
 cudaError_t launch_step_f16(int q, int c, const StepBuffers& b, const StepParams& P, cudaStream_t stream,
                             int64_t* launches, const StepEvents* ev);
 
+// The timestep split at the reference's hook points (advection, then
+// density/force/collision), for host code that runs hooks in between.
+constexpr int kPhaseAdvect = 1;
+constexpr int kPhaseCollide = 2;
+cudaError_t launch_phase_f64(int phase, int q, int c, const StepBuffers& b, const StepParams& P,
+                             cudaStream_t stream, int64_t* launches);
+cudaError_t launch_phase_f32(int phase, int q, int c, const StepBuffers& b, const StepParams& P,
+                             cudaStream_t stream, int64_t* launches);
+cudaError_t launch_phase_f16(int phase, int q, int c, const StepBuffers& b, const StepParams& P,
+                             cudaStream_t stream, int64_t* launches);
+
 }  // namespace lbk
 
 namespace lbk {

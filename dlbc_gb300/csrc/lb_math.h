@@ -15,11 +15,17 @@
 //   R  = (x - N*L1) - N*L2,  |R| <= ln2/64   (L1 + L2 = ln2/32, L1 has
 //        32 significant bits so N*L1 is exact)
 //   exp(x) = 2^M * 2^(J/32) * exp(R)
-//   exp(R) - 1 ~= R + R^2 (1/2 + R (1/6 + R (1/24 + R (1/120 + R/720))))
+//   exp(R) - 1 = R + R^2/2 + ... + R^8/8!  (truncation below 2^-76)
 //   2^(J/32) = S_lead[J] + S_trail[J]  (S_lead has 46 significant bits)
 // The table entries are the mathematical values 2^(J/32) rounded to the
-// stated number of bits (computed with 200-bit arithmetic).  Measured error
-// is below 0.54 ulp, as in Tang's paper.
+// stated number of bits (computed with 200-bit arithmetic).  Unlike Tang's
+// single-double evaluation (error up to ~0.54 ulp), R is carried as a
+// double-double and the leading products and sums are formed exactly with
+// fma and error-free additions (Dekker/Knuth TwoSum), so that the value
+// before the final rounding is within about 2^-72 relative of exp(x): the
+// result is the correctly rounded exp(x) except for arguments within that
+// distance of a rounding boundary (a few in a million).  The reduction
+// constants keep R's error below that bound for |x| < 2^10.
 #pragma once
 
 #include <stdint.h>
@@ -98,8 +104,18 @@ LB_EXP_TABLE_QUAL double kExpTable[32][2] = {
     {0x1.f50765b6e4580p+0, -0x1.fcc583da44ebdp-47},
 };
 
+// fused multiply-add with one rounding (IEEE fma on both sides)
+LB_HD double fma_(double a, double b, double c) {
+#if defined(__CUDA_ARCH__)
+  return __fma_rn(a, b, c);
+#else
+  return __builtin_fma(a, b, c);
+#endif
+}
+
 // exp(x) in IEEE double, identical on host (compiled with
-// -ffp-contract=off) and device (compiled with -fmad=false).
+// -ffp-contract=off) and device (compiled with -fmad=false; the explicit
+// fma_ calls are the only fused operations).
 LB_HD double lb_exp(double x) {
   const double kInvL = 0x1.71547652b82fep+5;   // 32/ln2
   const double kL1 = 0x1.62e42ff000000p-6;     // ln2/32, leading 32 bits
@@ -114,16 +130,47 @@ LB_HD double lb_exp(double x) {
   const int N = (int)Nd;
   const int J = N & 31;
   const int M = (N - J) / 32;
-  const double R1 = x - Nd * kL1;
-  const double R2 = -(Nd * kL2);
-  const double R = R1 + R2;
-  const double Q = R * R * (0.5 + R * (0x1.5555555555555p-3 + R * (0x1.5555555555555p-5 +
-                   R * (0x1.1111111111111p-7 + R * 0x1.6c16c16c16c17p-10))));
-  const double P = R1 + (R2 + Q);
+  // R = Rh + Rl: Rh is the rounded reduced argument, Rl its rounding error
+  // plus the rounding error of Nd*kL2 (both exact through fma / Fast2Sum)
+  const double R1 = x - Nd * kL1;               // exact
+  const double T = Nd * kL2;
+  const double Tl = fma_(Nd, kL2, -T);
+  const double Rh = R1 - T;
+  const double Rl = ((R1 - Rh) - T) - Tl;
+  // exp(R) - 1 = Rh + H + small, with H = Rh^2/2 exact and small holding
+  // the low part of Rh^2/2, the Rl cross term and R^3/6 + ... + R^8/8!
+  const double R2h = Rh * Rh;
+  const double R2l = fma_(Rh, Rh, -R2h);
+  const double H = 0.5 * R2h;
+  const double c3 = R2h * Rh * (0x1.5555555555555p-3 + Rh * (0x1.5555555555555p-5 +
+                    Rh * (0x1.1111111111111p-7 + Rh * (0x1.6c16c16c16c17p-10 +
+                    Rh * (0x1.a01a01a01a01ap-13 + Rh * 0x1.a01a01a01a01ap-16)))));
+  const double small = (0.5 * R2l + Rh * Rl) + (Rl + c3);
+  // 2^(J/32) * exp(R) = (Sl + St)(1 + Rh + H + small), summed so that only
+  // the last addition rounds at the result's precision
   const double Sl = kExpTable[J][0];
   const double St = kExpTable[J][1];
-  const double S = Sl + St;
-  const double y = Sl + (St + S * P);
+  const double Ah = Sl * Rh;
+  const double Al = fma_(Sl, Rh, -Ah);
+  const double Bh = Sl * H;
+  const double Bl = fma_(Sl, H, -Bh);
+  const double s1 = Ah + Bh;                    // TwoSum(Ah, Bh)
+  const double bv = s1 - Ah;
+  const double e1 = (Ah - (s1 - bv)) + (Bh - bv);
+  const double s = Sl + s1;                     // Fast2Sum: |Sl| >= 1 > |s1|
+  const double e2 = (Sl - s) + s1;
+  const double tail = e2 + (e1 + (Al + (Bl + (Sl * small + (St + St * ((Rh + H) + small))))));
+  double y = s + tail;
+  // The reference rounds twice: its exp works in the x87 80-bit format (64
+  // significant bits) and the result is stored as a double.  RN53(RN64(v))
+  // differs from RN53(v) = y only when RN64(v) is the midpoint between y and
+  // its neighbour, i.e. when v lies within half a 64-bit ulp of that midpoint;
+  // the midpoint then rounds to the even one of the two.
+  const double rr = tail - (y - s);            // v = y + rr (Fast2Sum residual)
+  const uint64_t yb = double_to_bits(y);
+  const double ulp = bits_to_double(((yb >> 52) - 52) << 52);   // y in [0.98, 2.03]
+  const double gap = 0.5 * ulp - (rr < 0.0 ? -rr : rr);
+  if ((yb & 1) && gap <= ulp * 0x1p-12) y = bits_to_double(rr > 0.0 ? yb + 1 : yb - 1);
   if (M >= -1021) {
     if (M <= 1023) return y * pow2i(M);
     return (y * pow2i(M - 1)) * 2.0;

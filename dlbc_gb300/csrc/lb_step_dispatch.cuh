@@ -39,4 +39,42 @@ cudaError_t dispatch_step(int q, int c, const StepBuffers& b, const StepParams& 
   return cudaErrorInvalidValue;
 }
 
+// One phase of the split timestep: kPhaseAdvect queues k_advect (f -> fout),
+// kPhaseCollide the two kernels without streaming (f is already advected).
+template <typename T, typename R, int Q, int C, bool W>
+cudaError_t launch_phase_t(int phase, const StepBuffers& b, const StepParams& P, cudaStream_t st,
+                           int64_t* launches) {
+  const unsigned blocks = unsigned((P.n + kStepThreads - 1) / kStepThreads);
+  if (phase == kPhaseAdvect) {
+    k_advect<T, Q, C, W><<<blocks, kStepThreads, 0, st>>>(static_cast<const T*>(b.f), static_cast<T*>(b.fout),
+                                                          b.mask, P);
+    *launches += 1;
+  } else {
+    k_density_psi<T, R, Q, C, W, false><<<blocks, kStepThreads, 0, st>>>(
+        static_cast<const T*>(b.f), b.mask, static_cast<R*>(b.rho), static_cast<R*>(b.psi), P);
+    k_collide<T, R, Q, C, W, false><<<blocks, kStepThreads, 0, st>>>(
+        static_cast<const T*>(b.f), static_cast<T*>(b.fout), b.mask, static_cast<const R*>(b.rho),
+        static_cast<const R*>(b.psi), b.force, P);
+    *launches += 2;
+  }
+  return cudaGetLastError();
+}
+
+template <typename T, typename R>
+cudaError_t dispatch_phase(int phase, int q, int c, const StepBuffers& b, const StepParams& P, cudaStream_t st,
+                           int64_t* launches) {
+  if (phase != kPhaseAdvect && phase != kPhaseCollide) return cudaErrorInvalidValue;
+  const bool w = b.mask != nullptr;
+#define LB_CASE(QQ, CC)                                                      \
+  if (q == QQ && c == CC)                                                    \
+    return w ? launch_phase_t<T, R, QQ, CC, true>(phase, b, P, st, launches) \
+             : launch_phase_t<T, R, QQ, CC, false>(phase, b, P, st, launches);
+  LB_CASE(19, 2)
+  LB_CASE(19, 1)
+  LB_CASE(9, 2)
+  LB_CASE(9, 1)
+#undef LB_CASE
+  return cudaErrorInvalidValue;
+}
+
 }  // namespace lbk

@@ -7,4 +7,8 @@ cudaError_t launch_step_f64(int q, int c, const StepBuffers& b, const StepParams
                             int64_t* launches, const StepEvents* ev) {
   return dispatch_step<double, double>(q, c, b, P, st, launches, ev);
 }
+cudaError_t launch_phase_f64(int phase, int q, int c, const StepBuffers& b, const StepParams& P, cudaStream_t st,
+                             int64_t* launches) {
+  return dispatch_phase<double, double>(phase, q, c, b, P, st, launches);
+}
 }  // namespace lbk

@@ -11,4 +11,12 @@ cudaError_t launch_step_f16(int q, int c, const StepBuffers& b, const StepParams
                             int64_t* launches, const StepEvents* ev) {
   return dispatch_step<__half, float>(q, c, b, P, st, launches, ev);
 }
+cudaError_t launch_phase_f32(int phase, int q, int c, const StepBuffers& b, const StepParams& P, cudaStream_t st,
+                             int64_t* launches) {
+  return dispatch_phase<float, float>(phase, q, c, b, P, st, launches);
+}
+cudaError_t launch_phase_f16(int phase, int q, int c, const StepBuffers& b, const StepParams& P, cudaStream_t st,
+                             int64_t* launches) {
+  return dispatch_phase<__half, float>(phase, q, c, b, P, st, launches);
+}
 }  // namespace lbk

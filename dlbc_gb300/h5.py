@@ -14,9 +14,13 @@ module implements exactly the subset those files use:
   layout v3 (contiguous, chunked with a v1 B-tree), filter pipeline v1/v2
   with deflate (1) and shuffle (2);
 
-and a writer that emits a contiguous, unfiltered ``/OutArray`` plus the
-``input`` string-array attribute, readable by h5py/h5dump and by this
-reader.  Everything is little-endian only (both machines this runs on are).
+attribute messages (numbers, fixed- and variable-length strings, the latter
+through the global heap), and a writer that emits a contiguous, unfiltered
+``/OutArray`` plus the reference's attributes: ``input`` at the root and the
+``metadata`` / ``globals`` groups.  The writer follows the published HDF5
+file-format specification (superblock 0); it is checked against this
+reader, as no libhdf5 is installed.  Everything is little-endian only (both
+machines this runs on are).
 """
 from __future__ import annotations
 
@@ -273,6 +277,84 @@ def read_field(path: str, name: str = "OutArray") -> np.ndarray:
 
 
 # ---------------------------------------------------------------------------
+# attributes
+# ---------------------------------------------------------------------------
+
+def _global_heap_object(d: bytes, coll: int, index: int) -> bytes:
+    """Object ``index`` of the global heap collection at ``coll``."""
+    if d[coll : coll + 4] != b"GCOL":
+        raise H5Error("bad global heap signature")
+    size = struct.unpack_from("<Q", d, coll + 8)[0]
+    p = coll + 16
+    end = coll + size
+    while p + 16 <= end:
+        idx, _refc, _res, osize = struct.unpack_from("<HHIQ", d, p)
+        if idx == 0:
+            break
+        if idx == index:
+            return d[p + 16 : p + 16 + osize]
+        p += 16 + osize + ((-osize) % 8)
+    raise H5Error(f"global heap object {index} not found")
+
+
+def _decode_attr(d: bytes, body: bytes):
+    ver = body[0]
+    if ver != 1:
+        raise H5Error(f"attribute message version {ver} unsupported")
+    _r, nlen, dtlen, dslen = struct.unpack_from("<BHHH", body, 1)
+    p = 8
+    name = body[p : p + nlen - 1].decode()
+    p += (nlen + 7) // 8 * 8
+    dtb = body[p : p + dtlen]
+    p += (dtlen + 7) // 8 * 8
+    dsb = body[p : p + dslen]
+    p += (dslen + 7) // 8 * 8
+    shape = _Reader._dataspace(dsb)
+    n = int(np.prod(shape)) if shape else 1
+    cls = dtb[0] & 0x0F
+    size = struct.unpack_from("<I", dtb, 4)[0]
+    if cls == 3:  # fixed-length string
+        val = [body[p + i * size : p + (i + 1) * size].split(b"\x00")[0].decode() for i in range(n)]
+    elif cls == 9:  # variable-length: (length, global heap collection, index) per element
+        val = []
+        for i in range(n):
+            ln, coll, idx = struct.unpack_from("<IQI", body, p + 16 * i)
+            val.append(_global_heap_object(d, coll, idx)[:ln].decode())
+    else:
+        dt = _Reader._datatype(dtb)
+        val = np.frombuffer(body[p : p + n * dt.itemsize], dt).copy()
+    return name, val
+
+
+def read_attrs(path: str, group: str = "") -> Dict[str, object]:
+    """All attributes of the root group (``group=""``) or of the child group
+    ``/group``: numbers as 1-D arrays, strings as lists of str (fixed-length
+    or variable-length, as libhdf5 writes the reference's ``input`` and
+    ``metadata`` strings)."""
+    with open(path, "rb") as fh:
+        data = fh.read()
+    r = _Reader(data)
+    addr = r.root_ohdr
+    if group:
+        links = r.root_links()
+        if group not in links:
+            raise H5Error(f"group /{group} not found in {path}")
+        addr = links[group]
+    out: Dict[str, object] = {}
+    for mtype, body in r.messages(addr):
+        if mtype == 0x0C:
+            name, val = _decode_attr(data, body)
+            out[name] = val
+    return out
+
+
+def list_links(path: str) -> List[str]:
+    """Names linked from the root group."""
+    with open(path, "rb") as fh:
+        return sorted(_Reader(fh.read()).root_links())
+
+
+# ---------------------------------------------------------------------------
 # writer
 # ---------------------------------------------------------------------------
 
@@ -289,9 +371,9 @@ def _dtype_msg(dt: np.dtype) -> bytes:
     dt = np.dtype(dt)
     if dt.kind == "f":
         if dt.itemsize == 8:
-            # class 1 version 1; bit fields: little endian, mantissa norm = 2 (implied msb),
-            # sign bit location 63; properties: bit offset 0, precision 64, exp loc 52,
-            # exp size 11, mantissa loc 0, mantissa size 52, exp bias 1023
+            # class 1 version 1; bit fields: little endian, mantissa normalisation 2 (implied
+            # msb), sign bit at 63; properties: offset 0, precision 64, exponent at 52 (11 bits),
+            # mantissa at 0 (52 bits), exponent bias 1023
             return struct.pack("<B3BI", 0x11, 0x20, 63, 0, 8) + struct.pack(
                 "<HHBBBBI", 0, 64, 52, 11, 0, 52, 1023)
         if dt.itemsize == 4:
@@ -305,137 +387,201 @@ def _dtype_msg(dt: np.dtype) -> bytes:
     raise H5Error(f"unsupported dtype {dt}")
 
 
-def write_field(path: str, arr: np.ndarray, input_lines: Optional[List[str]] = None,
-                attrs_f64: Optional[Dict[str, float]] = None,
-                attrs_i32: Optional[Dict[str, int]] = None) -> None:
-    """Write ``arr`` as ``/OutArray`` (contiguous, unfiltered), like
-    ``dumpFieldHDF5`` (``src/dlbc/io/hdf5.d:125``).
+def _dataspace(dims) -> bytes:
+    # version 1, no maximum dimensions
+    return struct.pack("<BBB5x", 1, len(dims), 0) + b"".join(struct.pack("<Q", x) for x in dims)
 
-    ``input_lines`` become the root attribute ``input`` as a 1-D array of
-    fixed-length strings (the reference stores the parameter file lines
-    there, ``src/dlbc/io/hdf5.d:529-548``).  ``attrs_f64``/``attrs_i32``
-    add scalar root attributes (used for checkpoint globals such as the
-    ``timestep``).
-    """
-    arr = np.ascontiguousarray(arr)
-    if arr.dtype == np.float64:
-        pass
-    elif arr.dtype.kind in "iu":
-        arr = arr.astype(np.int32)
+
+def _attr_msg(name: str, value) -> bytes:
+    """Attribute message (version 1).  int -> 32-bit signed scalar [1],
+    float -> double [1], str / list of str -> fixed-length null-terminated
+    ASCII strings, numpy array -> its dtype and shape."""
+    if isinstance(value, str):
+        value = [value]
+    if isinstance(value, (list, tuple)) and all(isinstance(v, str) for v in value):
+        enc = [v.encode() for v in value]
+        width = max(1, max(len(e) for e in enc) + 1)
+        dt_body = struct.pack("<B3BI", 0x13, 0x00, 0, 0, width)
+        ds_body = _dataspace([len(enc)])
+        data = b"".join(e.ljust(width, b"\x00") for e in enc)
     else:
-        arr = arr.astype(np.float64)
-    shape = arr.shape
+        if isinstance(value, bool):
+            arr = np.array([int(value)], np.int32)
+        elif isinstance(value, int):
+            arr = np.array([value], np.int32)
+        elif isinstance(value, float):
+            arr = np.array([value], np.float64)
+        else:
+            arr = np.ascontiguousarray(value)
+            if arr.ndim == 0:
+                arr = arr.reshape(1)
+        dt_body = _dtype_msg(arr.dtype)
+        ds_body = _dataspace(list(arr.shape))
+        data = arr.tobytes()
+    nm = name.encode() + b"\x00"
+    body = struct.pack("<BBHHH", 1, 0, len(nm), len(dt_body), len(ds_body))
+    body += _pad8(nm) + _pad8(dt_body) + _pad8(ds_body) + data
+    return _msg(0x0C, body)
 
-    # Layout of the file we emit:
-    #   superblock (96 bytes incl. root symbol table entry)
-    #   root object header (symbol table message + attributes)
-    #   group B-tree, local heap (+ data), symbol node
-    #   dataset object header, raw data
+
+# superblock parameters: group leaf node K (symbols per node / 2) and internal node K
+_K_LEAF = 4
+_K_INTERNAL = 16
+_BTREE_SIZE = 24 + (2 * _K_INTERNAL + 1) * 8 + 2 * _K_INTERNAL * 8
+_SNOD_SIZE = 8 + 2 * _K_LEAF * 40
+
+
+def write_file(path: str, datasets: Dict[str, np.ndarray], root_attrs: Optional[Dict[str, object]] = None,
+               groups: Optional[Dict[str, Dict[str, object]]] = None) -> None:
+    """Write an HDF5 file: ``datasets`` (contiguous, unfiltered, little
+    endian) and attribute-only child ``groups`` below the root group, which
+    carries ``root_attrs``.
+
+    File layout (superblock version 0, version-1 object headers, symbol-table
+    groups, as libhdf5 writes with its default file-creation properties):
+    superblock, then per group its object header, B-tree node, local heap and
+    symbol node, then per dataset its object header and raw data.
+    """
+    datasets = {k: np.ascontiguousarray(v) for k, v in datasets.items()}
+    groups = dict(groups or {})
+    root_attrs = dict(root_attrs or {})
+    if len(datasets) + len(groups) > 2 * _K_LEAF:
+        raise H5Error("too many links for one symbol node")
+
+    def heap_of(names):
+        blob = bytearray(b"\x00" * 8)  # offset 0: the empty name
+        offs = {}
+        for nm in names:
+            offs[nm] = len(blob)
+            blob += _pad8(nm.encode() + b"\x00")
+        return bytes(blob), offs
+
+    # sizes first (every address is 8 bytes, so no size depends on an address)
+    root_names = sorted(list(datasets) + list(groups), key=lambda s: s.encode())
+    root_heap, root_offs = heap_of(root_names)
+    root_attr_msgs = b"".join(_attr_msg(k, v) for k, v in root_attrs.items())
+    root_msgs_len = len(_msg(0x11, b"\x00" * 16)) + len(root_attr_msgs)
+
+    addr = 96
+    root_ohdr = addr
+    addr += 16 + root_msgs_len
+    root_btree = addr
+    addr += _BTREE_SIZE
+    root_heap_hdr = addr
+    addr += 32
+    root_heap_data = addr
+    addr += len(root_heap)
+    root_snod = addr
+    addr += _SNOD_SIZE
+
+    gmeta = {}
+    for g in sorted(groups, key=lambda s: s.encode()):
+        msgs = b"".join(_attr_msg(k, v) for k, v in groups[g].items())
+        heap, _ = heap_of([])
+        ent = {"attrs": msgs, "ohdr": addr}
+        addr += 16 + len(_msg(0x11, b"\x00" * 16)) + len(msgs)
+        ent["btree"] = addr
+        addr += _BTREE_SIZE
+        ent["heap_hdr"] = addr
+        addr += 32
+        ent["heap_data"] = addr
+        ent["heap"] = heap
+        addr += len(heap)
+        gmeta[g] = ent
+
+    dmeta = {}
+    for nm in sorted(datasets, key=lambda s: s.encode()):
+        arr = datasets[nm]
+        if arr.dtype.byteorder == ">":
+            raise H5Error("big-endian arrays unsupported")
+        msgs_wo_layout = _msg(0x01, _dataspace(list(arr.shape)), 1) + _msg(0x03, _dtype_msg(arr.dtype), 1)
+        layout_len = len(_msg(0x08, struct.pack("<BBQQ", 3, 1, 0, 0)))
+        ent = {"ohdr": addr, "msgs": msgs_wo_layout}
+        addr += 16 + len(msgs_wo_layout) + layout_len
+        addr += (-addr) % 8
+        ent["data"] = addr
+        addr += arr.nbytes
+        addr += (-addr) % 8
+        dmeta[nm] = ent
+    eof = addr
+
     out = bytearray()
 
-    def attr_msg(name: str, dt_body: bytes, ds_body: bytes, data: bytes) -> bytes:
-        nm = name.encode() + b"\x00"
-        body = struct.pack("<BBHHH", 1, 0, len(nm), len(dt_body), len(ds_body))
-        body += _pad8(nm) + _pad8(dt_body) + _pad8(ds_body) + data
-        return _msg(0x0C, body)
+    def ohdr(msgs: bytes, nmsgs: int) -> bytes:
+        return struct.pack("<BBHII4x", 1, 0, nmsgs, 1, len(msgs)) + msgs
 
-    def dataspace(dims) -> bytes:
-        return struct.pack("<BBB5x", 1, len(dims), 0) + b"".join(struct.pack("<Q", x) for x in dims)
+    def btree(snod: Optional[int], last_key: int) -> bytes:
+        if snod is None:  # empty group: a leaf with no entries
+            bt = b"TREE" + struct.pack("<BBHQQ", 0, 0, 0, _UNDEF, _UNDEF) + struct.pack("<Q", 0)
+        else:
+            bt = b"TREE" + struct.pack("<BBHQQ", 0, 0, 1, _UNDEF, _UNDEF)
+            bt += struct.pack("<QQQ", 0, snod, last_key)
+        return bt.ljust(_BTREE_SIZE, b"\x00")
 
-    root_attrs = b""
-    if input_lines:
-        enc = [ln.encode() for ln in input_lines]
-        width = max(1, max(len(e) for e in enc) + 1)
-        # string datatype: class 3, version 1, null-terminated ascii
-        dt = struct.pack("<B3BI", 0x13, 0x00, 0, 0, width)
-        data = b"".join(e.ljust(width, b"\x00") for e in enc)
-        root_attrs += attr_msg("input", dt, dataspace([len(enc)]), data)
-    for k, v in (attrs_f64 or {}).items():
-        root_attrs += attr_msg(k, _dtype_msg(np.float64), dataspace([1]), struct.pack("<d", v))
-    for k, v in (attrs_i32 or {}).items():
-        root_attrs += attr_msg(k, _dtype_msg(np.int32), dataspace([1]), struct.pack("<i", v))
+    def heap_hdr(size: int, data_addr: int) -> bytes:
+        return b"HEAP" + struct.pack("<B3xQQQ", 0, size, _UNDEF, data_addr)
 
-    SB = 96
-    # root object header: 16-byte prefix + symbol table msg (16 body) + attrs
-    root_msgs = _msg(0x11, struct.pack("<QQ", 0, 0)) + root_attrs
-    root_ohdr = SB
-    root_size = 16 + len(root_msgs)
-    btree_addr = root_ohdr + root_size
-    # group B-tree with one child (K=16 leaf -> room for 2K+1 keys, 2K children)
-    K_internal = 16
-    btree_size = 24 + (2 * K_internal + 1) * 8 + 2 * K_internal * 8
-    heap_addr = btree_addr + btree_size
-    heap_data = _pad8(b"\x00" * 8 + b"OutArray\x00")
-    heap_data_addr = heap_addr + 32
-    snod_addr = heap_data_addr + len(heap_data)
-    K_leaf = 4
-    snod_size = 8 + 2 * K_leaf * 40
-    ds_ohdr = snod_addr + snod_size
-    ds_msgs = _msg(0x01, dataspace(shape), 1) + _msg(0x03, _dtype_msg(arr.dtype), 1)
-    ds_msgs_len_guess = len(ds_msgs) + 8 + 24  # layout message (v3 contiguous: 18 bytes -> 24)
-    data_addr = ds_ohdr + 16 + ds_msgs_len_guess
-    data_addr += (-data_addr) % 8
-    ds_msgs += _msg(0x08, struct.pack("<BBQQ", 3, 1, data_addr, arr.nbytes))
-    assert 16 + len(ds_msgs) == ds_msgs_len_guess + 16
-    eof = data_addr + arr.nbytes
-
-    # superblock v0
+    # superblock v0 and the root group's symbol table entry (cache type 1)
     out += _SIG
     out += struct.pack("<BBBBBBBB", 0, 0, 0, 0, 0, 8, 8, 0)
-    out += struct.pack("<HHI", K_leaf, K_internal, 0)
+    out += struct.pack("<HHI", _K_LEAF, _K_INTERNAL, 0)
     out += struct.pack("<QQQQ", 0, _UNDEF, eof, _UNDEF)
-    # root symbol table entry (cache type 1 -> B-tree + heap)
-    out += struct.pack("<QQII", 0, root_ohdr, 1, 0) + struct.pack("<QQ", btree_addr, heap_addr)
-    assert len(out) == SB
-    # root object header: fix up the symbol table message body
-    root_msgs = _msg(0x11, struct.pack("<QQ", btree_addr, heap_addr)) + root_attrs
-    nmsgs = 1 + (1 if input_lines else 0) + len(attrs_f64 or {}) + len(attrs_i32 or {})
-    out += struct.pack("<BBHII4x", 1, 0, nmsgs, 1, len(root_msgs)) + root_msgs
-    assert len(out) == btree_addr
-    # group B-tree node: type 0, level 0, one entry; keys are heap offsets
-    bt = b"TREE" + struct.pack("<BBHQQ", 0, 0, 1, _UNDEF, _UNDEF)
-    bt += struct.pack("<Q", 0) + struct.pack("<Q", snod_addr) + struct.pack("<Q", 8)
-    out += bt.ljust(btree_size, b"\x00")
-    # local heap
-    out += b"HEAP" + struct.pack("<B3xQQQ", 0, len(heap_data), _UNDEF, heap_data_addr)
-    out += heap_data
-    # symbol table node with one entry
-    sn = b"SNOD" + struct.pack("<BBH", 1, 0, 1)
-    sn += struct.pack("<QQII", 8, ds_ohdr, 0, 0) + b"\x00" * 16
-    out += sn.ljust(snod_size, b"\x00")
-    assert len(out) == ds_ohdr
-    out += struct.pack("<BBHII4x", 1, 0, 3, 1, len(ds_msgs)) + ds_msgs
-    out += b"\x00" * (data_addr - len(out))
-    out += arr.tobytes()
+    out += struct.pack("<QQII", 0, root_ohdr, 1, 0) + struct.pack("<QQ", root_btree, root_heap_hdr)
+    assert len(out) == root_ohdr
+    out += ohdr(_msg(0x11, struct.pack("<QQ", root_btree, root_heap_hdr)) + root_attr_msgs, 1 + len(root_attrs))
+    out += btree(root_snod if root_names else None, root_offs[root_names[-1]] if root_names else 0)
+    out += heap_hdr(len(root_heap), root_heap_data) + root_heap
+    sn = b"SNOD" + struct.pack("<BBH", 1, 0, len(root_names))
+    for nm in root_names:
+        if nm in gmeta:
+            g = gmeta[nm]
+            sn += struct.pack("<QQII", root_offs[nm], g["ohdr"], 1, 0) + struct.pack("<QQ", g["btree"], g["heap_hdr"])
+        else:
+            sn += struct.pack("<QQII", root_offs[nm], dmeta[nm]["ohdr"], 0, 0) + b"\x00" * 16
+    out += sn.ljust(_SNOD_SIZE, b"\x00")
+    for nm in sorted(groups, key=lambda s: s.encode()):
+        g = gmeta[nm]
+        assert len(out) == g["ohdr"]
+        out += ohdr(_msg(0x11, struct.pack("<QQ", g["btree"], g["heap_hdr"])) + g["attrs"], 1 + len(groups[nm]))
+        out += btree(None, 0)
+        out += heap_hdr(len(g["heap"]), g["heap_data"]) + g["heap"]
+    for nm in sorted(datasets, key=lambda s: s.encode()):
+        arr, ent = datasets[nm], dmeta[nm]
+        assert len(out) == ent["ohdr"]
+        msgs = ent["msgs"] + _msg(0x08, struct.pack("<BBQQ", 3, 1, ent["data"], arr.nbytes))
+        out += ohdr(msgs, 3)
+        out += b"\x00" * (ent["data"] - len(out))
+        out += arr.tobytes()
+        out += b"\x00" * ((-len(out)) % 8)
+    assert len(out) == eof
     with open(path, "wb") as fh:
         fh.write(bytes(out))
 
 
-def read_root_attr(path: str, name: str):
-    """Read a scalar/1-D root attribute written by :func:`write_field`
-    (numeric or fixed-length string)."""
-    with open(path, "rb") as fh:
-        data = fh.read()
-    r = _Reader(data)
-    for mtype, body in r.messages(r.root_ohdr):
-        if mtype != 0x0C:
-            continue
-        ver, _r, nlen, dtlen, dslen = struct.unpack_from("<BBHHH", body, 0)
-        p = 8
-        aname = body[p : p + nlen - 1].decode()
-        p += (nlen + 7) // 8 * 8
-        dtb = body[p : p + dtlen]
-        p += (dtlen + 7) // 8 * 8
-        dsb = body[p : p + dslen]
-        p += (dslen + 7) // 8 * 8
-        if aname != name:
-            continue
-        shape = _Reader._dataspace(dsb)
-        n = int(np.prod(shape)) if shape else 1
-        cls = dtb[0] & 0x0F
-        size = struct.unpack_from("<I", dtb, 4)[0]
-        if cls == 3:
-            return [body[p + i * size : p + (i + 1) * size].rstrip(b"\x00").decode() for i in range(n)]
-        dt = _Reader._datatype(dtb)
-        return np.frombuffer(body[p : p + n * dt.itemsize], dt).copy()
-    raise H5Error(f"attribute {name} not found")
+def write_field(path: str, arr: np.ndarray, input_lines: Optional[List[str]] = None,
+                metadata: Optional[Dict[str, object]] = None,
+                globals_: Optional[Dict[str, object]] = None) -> None:
+    """Write ``arr`` as ``/OutArray`` the way ``dumpFieldHDF5`` lays a field
+    out (``src/dlbc/io/hdf5.d:125-285``): native double (or 32-bit int for
+    the mask), global dims with the vector/population component fastest.
+
+    ``input_lines`` become the root attribute ``input`` (the parameter file
+    lines, ``hdf5.d:529-548``), ``metadata`` the attributes of group
+    ``/metadata`` (``hdf5.d:290-299``) and ``globals_`` those of group
+    ``/globals`` (checkpoint files only, ``src/dlbc/io/checkpoint.d:248-313``,
+    e.g. ``{"dlbc.lb.lb.timestep": t}``).
+    """
+    arr = np.ascontiguousarray(arr)
+    if arr.dtype.kind in "iub":
+        arr = arr.astype(np.int32)
+    elif arr.dtype != np.float64:
+        arr = arr.astype(np.float64)
+    root = {"input": list(input_lines)} if input_lines else {}
+    groups: Dict[str, Dict[str, object]] = {}
+    if metadata is not None:
+        groups["metadata"] = metadata
+    if globals_ is not None:
+        groups["globals"] = globals_
+    write_file(path, {"OutArray": arr}, root, groups)
+
+

@@ -25,6 +25,7 @@ ERRORS = {0: "OK", -1: "LBGPU_E_INVALID", -2: "LBGPU_E_NOMEM", -3: "LBGPU_E_CUDA
           -5: "LBGPU_E_NOTREADY", -6: "LBGPU_E_NONFINITE"}
 
 EXPORTED = ["lbgpu_abi_version", "lbgpu_create", "lbgpu_destroy", "lbgpu_upload", "lbgpu_step",
+            "lbgpu_advect", "lbgpu_collide",
             "lbgpu_download", "lbgpu_moments", "lbgpu_set_record_force", "lbgpu_force", "lbgpu_reduce",
             "lbgpu_synchronize", "lbgpu_set_stream", "lbgpu_profile", "lbgpu_kernel_time",
             "lbgpu_launch_count", "lbgpu_device_bytes", "lbgpu_last_error"]
@@ -62,6 +63,8 @@ def lib() -> C.CDLL:
         L.lbgpu_destroy.restype = None
         L.lbgpu_upload.argtypes = [H, PP, C.c_void_p]
         L.lbgpu_step.argtypes = [H, C.c_int32]
+        L.lbgpu_advect.argtypes = [H]
+        L.lbgpu_collide.argtypes = [H]
         L.lbgpu_download.argtypes = [H, PP]
         L.lbgpu_moments.argtypes = [H, PP, PP, C.c_void_p]
         L.lbgpu_set_record_force.argtypes = [H, C.c_int32]
@@ -177,6 +180,14 @@ class GPULattice:
 
     def step(self, n: int = 1) -> None:
         self._check(lib().lbgpu_step(self.h, int(n)), "lbgpu_step")
+
+    def advect(self) -> None:
+        """First phase of a timestep (streaming); :meth:`collide` completes it."""
+        self._check(lib().lbgpu_advect(self.h), "lbgpu_advect")
+
+    def collide(self) -> None:
+        """Second phase: densities, psi, forces and collision of the advected state."""
+        self._check(lib().lbgpu_collide(self.h), "lbgpu_collide")
 
     def synchronize(self) -> None:
         self._check(lib().lbgpu_synchronize(self.h), "lbgpu_synchronize")

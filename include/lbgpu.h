@@ -95,6 +95,22 @@ int lbgpu_upload(lbgpu_handle* h, const double* const* fluids, const int32_t* ma
  * body, src/main.d:175-199, without dumpData). */
 int lbgpu_step(lbgpu_handle* h, int32_t nsteps);
 
+/* One timestep in two phases, for a host that runs hooks between advection
+ * and collision (postAdvectionHooks / preCollisionHooks, executed by
+ * src/dlbc/lb/advection.d:53 and src/dlbc/lb/collision.d:70 and registered
+ * through src/dlbc/hooks.d:57-118).  lbgpu_advect streams the populations
+ * (advectFields, src/dlbc/lb/advection.d:35-55); lbgpu_collide does the
+ * densities, psi, forces and collision without streaming
+ * (src/dlbc/lb/force.d:165-309, src/dlbc/lb/collision.d:60-119).  Between
+ * the two, lbgpu_download returns the advected populations and lbgpu_upload
+ * may replace them.  lbgpu_advect then lbgpu_collide compute bit for bit
+ * what lbgpu_step(h, 1) computes in the FP64 form; the FP32 and FP16 D3Q19
+ * forms of lbgpu_step use the fused single-pass kernel, which rounds
+ * differently (within the forms' documented error).  Calling lbgpu_collide
+ * twice in a row, or lbgpu_step between the phases, is LBGPU_E_NOTREADY. */
+int lbgpu_advect(lbgpu_handle* h);
+int lbgpu_collide(lbgpu_handle* h);
+
 /* Initial fields computed on the device (no host arrays cross the bus): the
  * deterministic initialisers of initFluids/initMask (src/dlbc/lb/init.d:139-339,
  * src/dlbc/fields/init.d) for one process.  Sphere, cylinder, two-sphere and

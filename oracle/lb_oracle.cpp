@@ -793,4 +793,8 @@ double or_uniform_sequence(uint32_t seed, double a, double b, int n, double* out
   return n > 0 ? out[n - 1] : 0.0;
 }
 
+void or_exp(int mode, int n, const double* x, double* out) {
+  for (int i = 0; i < n; ++i) out[i] = mode == 1 ? lbmath::lb_exp(x[i]) : (double)expl((long double)x[i]);
+}
+
 }  // extern "C"

@@ -27,8 +27,11 @@ typedef struct {
   int32_t shan_chen;       /* lb.force.enableShanChen */
   int32_t psi_form;        /* lb.force.psiForm: 0 Linear, 1 Exponential */
   int32_t eq_form;         /* lb.eqdist.eqDistForm: 0 SecondOrder, 1 ThirdOrder, 2 BDist2 */
-  int32_t exp_mode;        /* 0: exp in extended precision rounded to double (as Phobos
-                              std.math.exp); 1: lbmath::lb_exp (the kernels' exp) */
+  int32_t exp_mode;        /* 0: expl in long double rounded to double (as Phobos
+                              std.math.exp on x86-64, where long double is the x87
+                              80-bit format; other hosts' long double differs);
+                              1: lbmath::lb_exp (the kernels' exp, which emulates
+                              that double rounding on every host) */
   int32_t sum_mode;        /* density(): 0 Phobos pairwise (recursive halving), 1 sequential (negative control) */
   int32_t threads;         /* OpenMP threads for the sweeps (<= 1: serial) */
   double tau[OR_MAXC];
@@ -93,6 +96,9 @@ double or_total_mass(const or_lattice* L, int c);               /* fluid sites, 
 
 /* Mt19937 uniform(a, b) as Phobos std.random (src/dlbc/random.d:55-89) */
 double or_uniform_sequence(uint32_t seed, double a, double b, int n, double* out);
+
+/* exp of n arguments with exp_mode `mode` (see or_config) */
+void or_exp(int mode, int n, const double* x, double* out);
 
 #ifdef __cplusplus
 }

@@ -77,8 +77,19 @@ def lib() -> C.CDLL:
         L.or_total_mass.restype = C.c_double
         L.or_uniform_sequence.argtypes = [C.c_uint32, C.c_double, C.c_double, C.c_int, dp]
         L.or_uniform_sequence.restype = C.c_double
+        L.or_exp.argtypes = [C.c_int, C.c_int, dp, dp]
+        L.or_exp.restype = None
         _lib = L
     return _lib
+
+
+def exp(x, mode: int = 1):
+    """exp of a float64 array: mode 1 the kernels' lbmath::lb_exp, mode 0
+    long double expl rounded to double."""
+    x = np.ascontiguousarray(x, np.float64)
+    out = np.empty_like(x)
+    lib().or_exp(mode, x.size, x, out)
+    return out
 
 
 def make_config(p, exp_mode: int = 0, sum_mode: int = 0, threads: int = 1) -> OrConfig:

@@ -40,6 +40,15 @@ CASES = [
      "reference-data/*-t%08d.h5", {0: 0.0, 1000: 0.0}),
     ("laplace-quasi-1d-d2q9", "lb/laplace-quasi-1d", "laplace-quasi-1d-d2q9.in", "d2q9",
      "reference-data/d2q9/*-t%08d.h5", {0: 0.0, 1000: 1e-15}),
+    # restored from the t = 0 checkpoint, 5 steps; the test compares without a tolerance
+    ("checkpoint-3d", "technical/checkpoint-3d", "checkpoint-3d.in.source", "d3q19",
+     "reference-data/*-t%08d.h5", {0: 0.0, 5: 0.0}),
+]
+
+# checkpoint files stored whole (case, directory, file stem, checkpoint name)
+CHECKPOINTS = [
+    ("checkpoint-3d", "technical/checkpoint-3d/reference-data/cp", ["cp-fluids0", "cp-fluids1", "cp-mask"],
+     "checkpoint-3d-t00000000"),
 ]
 
 # init-2d: every initialiser and mask at t = 0 (exact goldens)
@@ -107,6 +116,15 @@ def main(ref: str):
                 out[key + "/tol"] = np.array(tol)
                 keys.append(key)
         out["keys"] = np.array(keys)
+        for cname, cdir, stems, cpname in CHECKPOINTS:
+            if cname != name:
+                continue
+            out["checkpoint/name"] = np.array(cpname)
+            for stem in stems:
+                f = os.path.join(tests, cdir, f"{stem}-{cpname}.h5")
+                out[f"checkpoint/{stem}"] = h5.read_field(f)
+                out[f"checkpoint/{stem}/timestep"] = np.array(
+                    h5.read_attrs(f, "globals")["dlbc.lb.lb.timestep"]).ravel()
         path = os.path.join(HERE, name + ".npz")
         np.savez_compressed(path, **out)
         print(f"{path}: {len(keys)} arrays, {os.path.getsize(path)} bytes")

@@ -40,3 +40,9 @@ def droplet_channel(n=(32, 16, 16), radius=5.0, acc=1e-6, gwc=(0.0, 0.0), eq="BD
         "mask.wallThickness = 1",
     ]
     return params.LBParams.from_dict(params.parse_lines(lines), "d3q19")
+
+
+# D3Q19 velocities in the reference's order (src/dlbc/lb/connectivity.d:401-418)
+D3Q19_VELOCITIES = [(0, 0, 0), (1, 0, 0), (-1, 0, 0), (0, 1, 0), (0, -1, 0), (0, 0, 1), (0, 0, -1),
+                    (1, 1, 0), (-1, 1, 0), (0, 1, 1), (0, -1, 1), (1, 0, 1), (1, 0, -1), (1, -1, 0),
+                    (-1, -1, 0), (0, 1, -1), (0, -1, -1), (-1, 0, 1), (-1, 0, -1)]

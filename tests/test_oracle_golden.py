@@ -5,6 +5,9 @@ by tests/golden/make_fixtures.py.  Tolerances are the reference's own
 (the "accuracy" of each comparison in its JSON test specs); t = 0 files are
 compared bitwise, as the reference does.
 """
+import decimal
+import platform
+
 import numpy as np
 import pytest
 
@@ -20,7 +23,12 @@ from oracle import oracle as orc
 KNOWN_DEVIATIONS = {("poiseuille-2d", 1000): 2.5e-15, ("laplace-quasi-1d-d2q9", 1000): 2.5e-15}
 
 CASES = ["merging-droplets-3d", "bdist2-sc-3d", "laplace-droplet-3d", "merging-droplets-2d",
-         "bdist2-sc-2d", "poiseuille-2d", "laplace-quasi-1d-d2q9"]
+         "bdist2-sc-2d", "poiseuille-2d", "laplace-quasi-1d-d2q9", "checkpoint-3d"]
+
+# D3Q19 BDist2 Shan-Chen cases whose every golden file (t = 0 to the last
+# dump) the oracle reproduces bit for bit with either exp, including the
+# kernels' double-rounding exp
+BITWISE_CASES = ["bdist2-sc-3d", "checkpoint-3d"]
 LONG = {("merging-droplets-3d", 1000), ("merging-droplets-2d", 1000)}
 
 
@@ -67,6 +75,44 @@ def test_oracle_long_runs(name):
     o.run(1000)
     for key, kind in golden_arrays(z, 1000):
         assert compare(z, key, oracle_output(o, p, kind), float(z[key + "/tol"])), key
+
+
+@pytest.mark.parametrize("exp_mode", [0, 1])
+@pytest.mark.parametrize("name", BITWISE_CASES)
+def test_goldens_bitwise(name, exp_mode):
+    if exp_mode == 0 and platform.machine() not in ("x86_64", "AMD64"):
+        pytest.skip("exp_mode 0 is the x87 extended-precision exp of x86-64")
+    z, p = load_case(name)
+    o = orc.Oracle(p, exp_mode=exp_mode, threads=8)
+    t_now = 0
+    for t in times(z):
+        o.run(t - t_now)
+        t_now = t
+        for key, kind in golden_arrays(z, t):
+            assert compare(z, key, oracle_output(o, p, kind), 0.0), key
+
+
+def test_kernel_exp_is_the_double_rounded_exp():
+    """lbmath::lb_exp against Python's correctly rounded decimal exp: equal,
+    or (where the 80-bit intermediate rounding of the reference's exp
+    decides a tie) one ulp away with the exact value within 2^-11 ulp of the
+    midpoint; and on x86-64 against the x87 expl rounded to double."""
+    rng = np.random.default_rng(5)
+    x = np.concatenate([rng.uniform(-3.0, 0.0, 20000), rng.uniform(-700.0, 700.0, 2000),
+                        rng.uniform(-1e-3, 1e-3, 2000)])
+    got = orc.exp(x, mode=1)
+    decimal.getcontext().prec = 60
+    for xi, gi in zip(x, got):
+        e = decimal.Decimal(float(xi)).exp()
+        cr = float(e)
+        if gi != cr:
+            ulp = np.spacing(cr)
+            assert abs(gi - cr) == ulp, xi
+            mid = decimal.Decimal(float(cr)) + decimal.Decimal(float(gi - cr)) / 2
+            assert abs(e - mid) <= decimal.Decimal(float(ulp)) * decimal.Decimal(2) ** -11, xi
+    if platform.machine() in ("x86_64", "AMD64"):
+        xs = rng.uniform(-3.0, 0.0, 2_000_000)
+        assert np.mean(orc.exp(xs, mode=1) != orc.exp(xs, mode=0)) < 2e-4
 
 
 def test_bdist2_populations_bitwise_at_t10():
