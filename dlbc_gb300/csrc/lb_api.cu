@@ -440,7 +440,55 @@ int lb_handle_create(const lbgpu_config* cfg, bool lite, double* staging, size_t
 int64_t lb_member_bytes(const lbgpu_config* cfg) {
   int64_t n = 1;
   for (int i = 0; i < cfg->d; ++i) n *= cfg->gn[i];
-  return 2 * int64_t(cfg->components) * cfg->q * n * int64_t(storage_size(cfg->precision)) + n;
+  // populations (two buffers), mask byte and 32-bit neighbour mask
+  return 2 * int64_t(cfg->components) * cfg->q * n * int64_t(storage_size(cfg->precision)) + 5 * n;
+}
+
+// Neighbour mask of every site: bit 0 the site's own solid flag, bit q the
+// solid flag of x + c_q (periodic), for the fused step's bounce-back, stencil
+// and wall-force tests.
+__global__ void k_nbmask(const uint8_t* __restrict__ mask, uint32_t* __restrict__ nbm, Geo g) {
+  const int64_t s = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (s >= g.n) return;
+  const int64_t yz = int64_t(g.ny) * g.nz;
+  const int x = int(s / yz);
+  const int64_t r = s - int64_t(x) * yz;
+  const int y = int(r / g.nz), z = int(r - int64_t(y) * g.nz);
+  uint32_t bits = mask[s] ? 1u : 0u;
+#pragma unroll
+  for (int q = 1; q < 19; ++q) {
+    const int xn = (x + lbk::Conn<19>::cx(q) + g.nx) % g.nx;
+    const int yn = (y + lbk::Conn<19>::cy(q) + g.ny) % g.ny;
+    const int zn = (z + lbk::Conn<19>::cz(q) + g.nz) % g.nz;
+    if (mask[(int64_t(xn) * g.ny + yn) * g.nz + zn]) bits |= 1u << q;
+  }
+  nbm[s] = bits;
+}
+
+int lb_update_nbmask(lbgpu_handle* h) {
+  const bool want = h->mask && (h->fused || h->lite) && h->Q == 19;
+  if (!want) {
+    if (h->nbmask) {
+      cudaFree(h->nbmask);
+      h->device_bytes -= 4 * h->n;
+      h->nbmask = nullptr;
+    }
+    return LBGPU_OK;
+  }
+  if (!h->nbmask) {
+    cudaError_t e = cudaMalloc(&h->nbmask, size_t(h->n) * sizeof(uint32_t));
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      h->nbmask = nullptr;
+      return h->fail(LBGPU_E_NOMEM, "neighbour mask allocation failed");
+    }
+    h->device_bytes += 4 * h->n;
+  }
+  k_nbmask<<<unsigned(ceil_div(h->n, 256)), 256, 0, h->stream>>>(h->mask, h->nbmask, geo_of(h));
+  h->launches++;
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return h->cuda_fail(e, "neighbour mask kernel");
+  return LBGPU_OK;
 }
 
 int lb_ensure_moments(lbgpu_handle* h) {
@@ -479,6 +527,7 @@ void lbgpu_destroy(lbgpu_handle* h) {
   if (h->owns_staging && h->staging) cudaFree(h->staging);
   if (h->moments) cudaFree(h->moments);
   if (h->mask) cudaFree(h->mask);
+  if (h->nbmask) cudaFree(h->nbmask);
   if (h->force) cudaFree(h->force);
   for (auto& e : h->ev_pending)
     for (auto ev : e.ev) cudaEventDestroy(ev);
@@ -525,10 +574,13 @@ int lbgpu_upload(lbgpu_handle* h, const double* const* fluids, const int32_t* ma
               maxdev = std::max(maxdev, fabs(p[q] / w - rho0));
             }
           }
-      // the initial spread maps to |h| <= 1024: deviations may grow 64-fold
-      // before they leave half's range, and every direction keeps ~11
-      // significant bits of its own weight-normalised offset
-      double scale = maxdev > 0.0 ? (4.0 * maxdev) / 4096.0 : 1.0 / 4096.0;
+      // half is a floating-point format: every stored offset keeps 11
+      // significant bits whatever the scale, which therefore only sets the
+      // range.  Offsets up to 64 * max(rho0, 4 * initial spread) stay finite,
+      // so phase separation, which moves densities far beyond their initial
+      // spread, cannot overflow; offsets below 6e-8 of that lose precision.
+      const double span = std::max(fabs(rho0), 4.0 * maxdev);
+      const double scale = span > 0.0 ? span / 1024.0 : 1.0 / 4096.0;
       h->P.rho0[c] = float(rho0);
       h->P.scale[c] = float(scale);
       h->P.inv_scale[c] = float(1.0 / scale);
@@ -592,6 +644,7 @@ int lbgpu_upload(lbgpu_handle* h, const double* const* fluids, const int32_t* ma
     h->device_bytes -= h->n;
     h->mask = nullptr;
   }
+  if (int rc = lb_update_nbmask(h)) return rc;
   e = cudaStreamSynchronize(h->stream);
   if (e != cudaSuccess) return h->cuda_fail(e, "upload");
   h->uploaded = true;
@@ -661,6 +714,7 @@ int lbgpu_step(lbgpu_handle* h, int32_t nsteps) {
     b.f = h->f[h->cur];
     b.fout = h->f[1 - h->cur];
     b.mask = h->mask;
+    b.nbmask = h->nbmask;
     b.rho = h->rho;
     b.psi = h->psi;
     b.force = h->force;

@@ -112,7 +112,7 @@ int build_table(lbgpu_batch* b, int ty) {
     fs.P = lbk::make_fused_params(h->P, ty);
     fs.f[0] = h->f[0];
     fs.f[1] = h->f[1];
-    fs.mask = h->mask;
+    fs.nbmask = h->nbmask;
     fs.force_out = nullptr;
     fs.work_begin = b->total_work;
     fs.phase = h->cur;

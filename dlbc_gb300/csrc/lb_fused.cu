@@ -22,6 +22,7 @@ FusedParams make_fused_params(const StepParams& P, int ty) {
   F.psi_form = P.psi_form;
   F.eq_form = P.eq_form;
   F.record_force = P.record_force;
+  F.unit_tau = P.unit_tau;
   for (int c = 0; c < 2; ++c) {
     F.tau[c] = float(P.tau[c]);
     F.inv_tau[c] = float(1.0 / P.tau[c]);
@@ -40,6 +41,7 @@ FusedParams make_fused_params(const StepParams& P, int ty) {
       F.wrho[c][q] = weight<19, float>(q) * P.rho0[c];
       F.wscale[c][q] = weight<19, float>(q) * P.scale[c];
       F.inv_wscale[c][q] = 1.0f / F.wscale[c][q];
+      F.hoff[c][q] = -F.wrho[c][q] * F.inv_wscale[c][q];
     }
   }
   return F;
@@ -90,7 +92,7 @@ cudaError_t go_single(const StepBuffers& b, const FusedParams& F, cudaStream_t s
   if (e != cudaSuccess) return e;
   int64_t grid = int64_t(per_sm) * sm_count(device);
   if (grid > F.work) grid = F.work;
-  kern<<<unsigned(grid), TY * kFusedTZ, smem, st>>>(static_cast<const T*>(b.f), static_cast<T*>(b.fout), b.mask,
+  kern<<<unsigned(grid), TY * kFusedTZ, smem, st>>>(static_cast<const T*>(b.f), static_cast<T*>(b.fout), b.nbmask,
                                                     b.force, F);
   return cudaGetLastError();
 }
@@ -118,6 +120,7 @@ cudaError_t launch_fused(bool half_storage, int c, const StepBuffers& b, const S
                          int64_t* launches, const StepEvents* ev, int device) {
   const FusedParams F = make_fused_params(P, 8);
   const bool w = b.mask != nullptr;
+  if (w && !b.nbmask) return cudaErrorInvalidValue;  // walls need the neighbour masks
   if (ev) {
     cudaEventRecord(ev->ev[0], st);
     cudaEventRecord(ev->ev[1], st);

@@ -10,9 +10,12 @@
 // stay in shared memory until the next iteration, when plane x is collided
 // with the psi stencil of planes x-1, x, x+1 and written out.  Ring sites are
 // re-read by the neighbouring tile (from L2); the populations of a site are
-// read from HBM once and written once.  With walls, the mask of planes
-// x-1 .. x+3 over the tile and a two-site border is staged in shared memory
-// (one plane ahead) so the bounce-back tests never touch global memory.
+// read from HBM once and written once.  With walls, every site carries a
+// 32-bit neighbour mask (bit 0: the site is solid; bit q: the site x + c_q is
+// solid, periodic images included), built once when the mask is set: the
+// bounce-back choice of the gather (x - c_q = x + c_bounce(q)), the
+// stencil's wall substitution and the wall force all read it, one coalesced
+// 4-byte load per site instead of 37 mask lookups.
 //
 // Scheduling is persistent and balanced: the (tile, x) plane-tiles are laid
 // out tile-major and split into equal contiguous ranges, one per CTA; every
@@ -39,7 +42,6 @@ namespace lbk {
 // along the contiguous z axis), one thread per site.
 constexpr int kFusedTZ = 32;
 constexpr int kFusedRZ = kFusedTZ + 2;   // tile + one-site ring
-constexpr int kFusedMZ = kFusedTZ + 4;   // tile + two-site border (mask)
 
 // float copies of the step parameters (no double arithmetic in the kernel)
 struct FusedParams {
@@ -48,6 +50,7 @@ struct FusedParams {
   int32_t tiles_y, tiles_z;
   int64_t work;            // tiles * nx plane-tiles
   int32_t shan_chen, psi_form, eq_form, record_force;
+  int32_t unit_tau;        // every tau == 1: the relaxation is the equilibrium itself
   float tau[2], inv_tau[2], omega[2], one_minus_omega[2];
   float gcc[2][2], gwc[2], acc[3];
   float rho0[2], scale[2], inv_scale[2];
@@ -55,6 +58,7 @@ struct FusedParams {
   float wrho[2][19];       // w_q * rho0_c (half storage: f_q = w_q rho0_c + w_q scale_c h)
   float wscale[2][19];     // w_q * scale_c
   float inv_wscale[2][19]; // 1 / (w_q * scale_c)
+  float hoff[2][19];       // -w_q rho0_c / (w_q scale_c): half value = v / (w_q scale_c) + hoff
 };
 
 template <typename T>
@@ -78,7 +82,7 @@ struct FStore<__half> {
     return fmaf(bb ? P.wscale[c][b] : P.wscale[c][q], __half2float(__ldg(p)), bb ? P.wrho[c][b] : P.wrho[c][q]);
   }
   __device__ static __forceinline__ void store(__half* p, float v, int c, int q, const FusedParams& P) {
-    *p = __float2half_rn((v - P.wrho[c][q]) * P.inv_wscale[c][q]);
+    *p = __float2half_rn(fmaf(v, P.inv_wscale[c][q], P.hoff[c][q]));
   }
 };
 
@@ -87,7 +91,6 @@ struct FusedShared {
   float pops[2][2][19][TY * kFusedTZ];  // [buffer][c][q][site in tile]
   float psi[3][2][TY + 2][kFusedRZ];    // [plane slot][c][y+1][z+1]
   float rho[3][2][TY + 2][kFusedRZ];
-  uint8_t solid[5][TY + 4][kFusedMZ];   // mask, [plane slot][y+2][z+2]
 };
 
 __device__ __forceinline__ int wrap(int v, int n) { return v < 0 ? v + n : (v >= n ? v - n : v); }
@@ -119,12 +122,13 @@ __device__ __forceinline__ YZ make_yz(int y, int z, const FusedParams& P) {
 }
 
 // Pull-gather one site; planes[0..2] are the offsets of planes xg-1, xg,
-// xg+1 of the gathered plane xg; (my, mz) locate the site in the mask ring.
-template <typename T, bool WALLS, int C, int TY>
-__device__ __forceinline__ void fused_gather(const T* const (&fc)[2], const FusedShared<TY>& sh, const FusedParams& P,
-                                             const uint32_t (&planes)[3], const YZ& yz, const int (&mslot)[3],
-                                             int my, int mz, bool solid, float (&pop)[C][19]) {
+// xg+1 of the gathered plane xg; nbm is the site's neighbour mask.
+template <typename T, bool WALLS, int C>
+__device__ __forceinline__ void fused_gather(const T* const (&fc)[2], const FusedParams& P,
+                                             const uint32_t (&planes)[3], const YZ& yz, uint32_t nbm,
+                                             float (&pop)[C][19]) {
   const uint32_t s = planes[1] + uint32_t(yz.off[1][1]);
+  const bool solid = WALLS && (nbm & 1u);
   // branch-free (warps straddling a wall must not run two code paths):
   // a solid site keeps its own populations, a fluid site pulls from x - c_q
   // or, when that site is solid, bounces back its own opposite population
@@ -132,9 +136,9 @@ __device__ __forceinline__ void fused_gather(const T* const (&fc)[2], const Fuse
   for (int q = 0; q < 19; ++q) {
     const int cx = Conn<19>::cx(q), cy = Conn<19>::cy(q), cz = Conn<19>::cz(q);
     const uint32_t nb = planes[1 - cx] + uint32_t(yz.off[1 - cy][1 - cz]);
-    bool bb = false;
-    if (WALLS && q > 0) bb = sh.solid[mslot[1 - cx]][my - cy][mz - cz] && !solid;
     const int b = Conn<19>::bounce(q);
+    bool bb = false;
+    if (WALLS && q > 0) bb = ((nbm >> b) & 1u) && !solid;  // x - c_q = x + c_b is solid
     const uint32_t off = (bb ? P.qn[b] : P.qn[q]) + ((WALLS && (solid || bb)) ? s : nb);
 #pragma unroll
     for (int c = 0; c < C; ++c) pop[c][q] = FStore<T>::load2(fc[c] + off, c, q, b, bb, P);
@@ -146,16 +150,15 @@ __device__ __forceinline__ void fused_gather(const T* const (&fc)[2], const Fuse
 // (batches); every thread of the CTA calls this with the same range.
 template <typename T, int C, bool WALLS, int TY>
 __device__ __forceinline__ void fused_body(const FusedParams& P, const T* __restrict__ f, T* __restrict__ fout,
-                                           const uint8_t* __restrict__ mask, double* __restrict__ force_out,
+                                           const uint32_t* __restrict__ nbmask, double* __restrict__ force_out,
                                            int64_t w0, int64_t w1, FusedShared<TY>& sh) {
   constexpr int kFusedTY = TY;
-  constexpr int kFusedThreads = TY * kFusedTZ;
-  constexpr int kFusedMY = TY + 4;
   const int t = threadIdx.x;
   const int ty = t / kFusedTZ, tz = t % kFusedTZ;
   const uint32_t plane_sz = uint32_t(P.ny) * uint32_t(P.nz);
   const T* const fc[2] = {f, f + size_t(19) * size_t(P.n)};
   T* const fo[2] = {fout, fout + size_t(19) * size_t(P.n)};
+  const bool unit = P.unit_tau != 0;
   int64_t w = w0;
   while (w < w1) {
     const int tile = int(w / P.nx);
@@ -183,29 +186,20 @@ __device__ __forceinline__ void fused_body(const FusedParams& P, const T* __rest
       }
     }
     const YZ yz_ring = make_yz(wrap(y0 + rry, P.ny), wrap(z0 + rrz, P.nz), P);
+    // neighbour masks of this thread's interior site at the gathered plane
+    // (nbm_next) and at the plane being collided (nbm_cur)
+    uint32_t nbm_next = 0, nbm_cur = 0;
 
-    // mask ring loader: plane x into slot ms, tile + two-site border
-    auto load_mask = [&](int ms, int x) {
-      if (!WALLS) return;
-      const size_t base = size_t(x) * plane_sz;
-      for (int i = t; i < kFusedMY * kFusedMZ; i += kFusedThreads) {
-        const int my = i / kFusedMZ, mz = i % kFusedMZ;
-        if (my > tyv + 3 || mz > tzv + 3) continue;
-        const int y = wrap(y0 + my - 2, P.ny), z = wrap(z0 + mz - 2, P.nz);
-        // a batch member without walls inside a walled batch: all fluid
-        sh.solid[ms][my][mz] = mask ? __ldg(mask + base + size_t(y) * P.nz + z) : uint8_t(0);
-      }
-    };
     // rho/psi of plane xg into psi slot ps (and the tile's populations into
-    // buffer keep, unless keep < 0); the mask of planes xg-1..xg+1 must be in
-    // mask slots mslot[0..2]
-    auto gather_plane = [&](int ps, int xg, int keep, const int (&mslot)[3]) {
+    // buffer keep, unless keep < 0)
+    auto gather_plane = [&](int ps, int xg, int keep) {
       const uint32_t planes[3] = {uint32_t(wrap(xg - 1, P.nx)) * plane_sz, uint32_t(xg) * plane_sz,
                                   uint32_t(wrap(xg + 1, P.nx)) * plane_sz};
       if (active) {
-        const bool solid = WALLS && sh.solid[mslot[1]][ty + 2][tz + 2];
+        const uint32_t nbm = (WALLS && nbmask) ? __ldg(nbmask + planes[1] + uint32_t(yz_in.off[1][1])) : 0u;
+        nbm_next = nbm;
         float pop[C][19];
-        fused_gather<T, WALLS, C, TY>(fc, sh, P, planes, yz_in, mslot, ty + 2, tz + 2, solid, pop);
+        fused_gather<T, WALLS, C>(fc, P, planes, yz_in, nbm, pop);
 #pragma unroll
         for (int c = 0; c < C; ++c) {
           const float den = density<19, float>(pop[c]);
@@ -218,9 +212,9 @@ __device__ __forceinline__ void fused_body(const FusedParams& P, const T* __rest
         }
       }
       if (has_ring) {
-        const bool solid = WALLS && sh.solid[mslot[1]][rry + 2][rrz + 2];
+        const uint32_t nbm = (WALLS && nbmask) ? __ldg(nbmask + planes[1] + uint32_t(yz_ring.off[1][1])) : 0u;
         float pop[C][19];
-        fused_gather<T, WALLS, C, TY>(fc, sh, P, planes, yz_ring, mslot, rry + 2, rrz + 2, solid, pop);
+        fused_gather<T, WALLS, C>(fc, P, planes, yz_ring, nbm, pop);
 #pragma unroll
         for (int c = 0; c < C; ++c) {
           const float den = density<19, float>(pop[c]);
@@ -230,38 +224,28 @@ __device__ __forceinline__ void fused_body(const FusedParams& P, const T* __rest
       }
     };
 
-    // warm-up: mask of planes xs-2 .. xs+2 (plane p lives in mask slot
-    // (p - xs + 2) % 5); rho/psi of xs-1; rho/psi + populations of xs
+    // warm-up: rho/psi of xs-1; rho/psi + populations of xs
     __syncthreads();
-    for (int j = 0; j < 5; ++j) load_mask(j, wrap(xs - 2 + j, P.nx));
-    __syncthreads();
-    {
-      const int m0[3] = {0, 1, 2};
-      gather_plane(0, wrap(xs - 1, P.nx), -1, m0);
-      const int m1[3] = {1, 2, 3};
-      gather_plane(1, xs, 0, m1);
-    }
+    gather_plane(0, wrap(xs - 1, P.nx), -1);
+    gather_plane(1, xs, 0);
     int cur = 0;
     for (int k = 0; k < run; ++k) {
       const int x = xs + k;
       const int sm = k % 3, s0 = (k + 1) % 3, sp = (k + 2) % 3;  // psi slots of x-1, x, x+1
-      // mask slots of planes x-1, x, x+1, x+2: (k+1)%5 .. (k+4)%5
-      const int mg[3] = {(k + 2) % 5, (k + 3) % 5, (k + 4) % 5};  // planes x, x+1, x+2
-      __syncthreads();  // psi slot sp, pops buffer 1-cur and mask slot k%5 (plane x-2) are free
-      load_mask(k % 5, wrap(x + 3, P.nx));  // for the next iteration
-      gather_plane(sp, wrap(x + 1, P.nx), 1 - cur, mg);
+      nbm_cur = nbm_next;
+      __syncthreads();  // psi slot sp and pops buffer 1-cur are free
+      gather_plane(sp, wrap(x + 1, P.nx), 1 - cur);
       __syncthreads();
       if (active) {
         const uint32_t s = uint32_t(x) * plane_sz + uint32_t(yz_in.off[1][1]);
         const int c1y = ty + 1, c1z = tz + 1;
         // branch-free: solid sites compute like fluid ones and store their
         // own populations (warps straddling a wall run one code path)
-        const bool solid = WALLS && sh.solid[(k + 2) % 5][ty + 2][tz + 2];
+        const bool solid = WALLS && (nbm_cur & 1u);
         float den[C];
 #pragma unroll
         for (int c = 0; c < C; ++c) den[c] = sh.rho[s0][c][c1y][c1z];
-        const int pslot[3] = {sm, s0, sp};                              // by cx + 1
-        const int mslot[3] = {(k + 1) % 5, (k + 2) % 5, (k + 3) % 5};  // mask of x-1, x, x+1
+        const int pslot[3] = {sm, s0, sp};  // by cx + 1
         // --- Shan-Chen force: S_c = sum_q w_q psi_c(x + c_q) c_q, a solid
         // neighbour contributing the site's own psi (force.d:273)
         float F[C][3];
@@ -278,7 +262,7 @@ __device__ __forceinline__ void fused_body(const FusedParams& P, const T* __rest
             for (int q = 1; q < 19; ++q) {
               const int cx = Conn<19>::cx(q), cy = Conn<19>::cy(q), cz = Conn<19>::cz(q);
               float v = sh.psi[pslot[cx + 1]][c][c1y + cy][c1z + cz];
-              if (WALLS && sh.solid[mslot[cx + 1]][ty + 2 + cy][tz + 2 + cz]) v = own[c];
+              if (WALLS && ((nbm_cur >> q) & 1u)) v = own[c];
               if (Conn<19>::wclass(q) == 1)
                 stencil_acc(a, cx, cy, cz, v);
               else
@@ -305,9 +289,7 @@ __device__ __forceinline__ void fused_body(const FusedParams& P, const T* __rest
 #pragma unroll
                 for (int q = 1; q < 19; ++q) {
                   const int cx = Conn<19>::cx(q), cy = Conn<19>::cy(q), cz = Conn<19>::cz(q);
-                  const float v = sh.solid[mslot[cx + 1]][ty + 2 + cy][tz + 2 + cz]
-                                      ? sh.rho[pslot[cx + 1]][f1][c1y + cy][c1z + cz]
-                                      : 0.f;
+                  const float v = ((nbm_cur >> q) & 1u) ? sh.rho[pslot[cx + 1]][f1][c1y + cy][c1z + cz] : 0.f;
                   if (Conn<19>::wclass(q) == 1)
                     stencil_acc(a, cx, cy, cz, v);
                   else
@@ -345,14 +327,20 @@ __device__ __forceinline__ void fused_body(const FusedParams& P, const T* __rest
           for (int c = 0; c < C; ++c) {
 #pragma unroll
             for (int q = 0; q < 19; ++q) pop[q] = sh.pops[cur][c][q][t];
+            if (unit) {
 #pragma unroll
-            for (int vd = 0; vd < 3; ++vd) a[vd] = fmaf(moment<19, float>(pop, vd), P.inv_tau[c], a[vd]);
+              for (int vd = 0; vd < 3; ++vd) a[vd] += moment<19, float>(pop, vd);
+            } else {
+#pragma unroll
+              for (int vd = 0; vd < 3; ++vd) a[vd] = fmaf(moment<19, float>(pop, vd), P.inv_tau[c], a[vd]);
+            }
           }
           const float rtot = __frcp_rn(tot);
 #pragma unroll
           for (int vd = 0; vd < 3; ++vd) wv[vd] = a[vd] * rtot;
         }
-        // --- collision; solid sites store their populations unchanged
+        // --- collision; solid sites store their populations unchanged.  With
+        // tau == 1 the new populations are the equilibrium (pop*0 + 1*eq)
 #pragma unroll
         for (int cc = 0; cc < C; ++cc) {
           const int c = C - 1 - cc;  // last component first: its populations are loaded
@@ -362,8 +350,13 @@ __device__ __forceinline__ void fused_body(const FusedParams& P, const T* __rest
           }
           const float rden = __frcp_rn(den[c]);
           float dv[3];
+          if (unit) {
 #pragma unroll
-          for (int vd = 0; vd < 3; ++vd) dv[vd] = P.tau[c] * fmaf(F[c][vd], rden, P.acc[vd]) + wv[vd];
+            for (int vd = 0; vd < 3; ++vd) dv[vd] = fmaf(F[c][vd], rden, P.acc[vd]) + wv[vd];
+          } else {
+#pragma unroll
+            for (int vd = 0; vd < 3; ++vd) dv[vd] = P.tau[c] * fmaf(F[c][vd], rden, P.acc[vd]) + wv[vd];
+          }
           float eq[19];
           if (P.eq_form == 2)
             eq_bdist2<19, float>(dv, den[c], eq);
@@ -372,7 +365,7 @@ __device__ __forceinline__ void fused_body(const FusedParams& P, const T* __rest
           const float omega = P.omega[c], omo = P.one_minus_omega[c];
 #pragma unroll
           for (int q = 0; q < 19; ++q) {
-            const float v = pop[q] * omo + omega * eq[q];
+            const float v = unit ? eq[q] : pop[q] * omo + omega * eq[q];
             FStore<T>::store(fo[c] + (P.qn[q] + s), solid ? pop[q] : v, c, q, P);
           }
         }
@@ -385,13 +378,13 @@ __device__ __forceinline__ void fused_body(const FusedParams& P, const T* __rest
 
 template <typename T, int C, bool WALLS, int TY>
 __global__ void __launch_bounds__(TY * kFusedTZ, 8 / TY * 2 > 4 ? 4 : 8 / TY * 2)
-    k_fused(const T* __restrict__ f, T* __restrict__ fout, const uint8_t* __restrict__ mask,
+    k_fused(const T* __restrict__ f, T* __restrict__ fout, const uint32_t* __restrict__ nbmask,
             double* __restrict__ force_out, FusedParams P) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   FusedShared<TY>& sh = *reinterpret_cast<FusedShared<TY>*>(smem_raw);
   const int64_t w0 = P.work * blockIdx.x / gridDim.x;
   const int64_t w1 = P.work * (blockIdx.x + 1) / gridDim.x;
-  fused_body<T, C, WALLS, TY>(P, f, fout, mask, force_out, w0, w1, sh);
+  fused_body<T, C, WALLS, TY>(P, f, fout, nbmask, force_out, w0, w1, sh);
 }
 
 // One simulation of a batch.  The step reads populations f[(parity + phase)
@@ -399,7 +392,7 @@ __global__ void __launch_bounds__(TY * kFusedTZ, 8 / TY * 2 > 4 ? 4 : 8 / TY * 2
 struct FusedSim {
   FusedParams P;
   const void* f[2];
-  const uint8_t* mask;     // nullptr: no solid site
+  const uint32_t* nbmask;  // neighbour masks; nullptr: no solid site
   double* force_out;       // nullptr unless recording
   int64_t work_begin;      // first plane-tile of this simulation in the batch
   int32_t phase;
@@ -445,7 +438,7 @@ __global__ void __launch_bounds__(TY * kFusedTZ, 8 / TY * 2 > 4 ? 4 : 8 / TY * 2
     const T* fin = static_cast<const T*>(sims[i].f[par]);
     T* fout = const_cast<T*>(static_cast<const T*>(sims[i].f[1 - par]));
     __syncthreads();
-    fused_body<T, C, WALLS, TY>(Ps, fin, fout, sims[i].mask, sims[i].force_out, w - wb, end - wb, sh);
+    fused_body<T, C, WALLS, TY>(Ps, fin, fout, sims[i].nbmask, sims[i].force_out, w - wb, end - wb, sh);
     w = end;
   }
 }

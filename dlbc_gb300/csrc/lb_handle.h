@@ -26,6 +26,7 @@ struct lbgpu_handle {
   void* f[2] = {nullptr, nullptr};
   int cur = 0;
   uint8_t* mask = nullptr;
+  uint32_t* nbmask = nullptr;       // neighbour masks for the fused step (walls only)
   void* rho = nullptr;
   void* psi = nullptr;
   double* force = nullptr;
@@ -71,3 +72,5 @@ int lb_handle_create(const lbgpu_config* cfg, bool lite, double* staging, size_t
 int64_t lb_member_bytes(const lbgpu_config* cfg);
 // scratch for lbgpu_moments / lbgpu_reduce, allocated on first use
 int lb_ensure_moments(lbgpu_handle* h);
+// (re)build or drop the neighbour masks after the mask changed
+int lb_update_nbmask(lbgpu_handle* h);

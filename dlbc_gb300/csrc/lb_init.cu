@@ -409,8 +409,9 @@ extern "C" int lbgpu_init_fields(lbgpu_handle* h, const lbgpu_init* ini) {
     if (e != cudaSuccess) return h->cuda_fail(e, "init statistics");
     if (int rc = reduce_stats(h, I, 2, d_rho0, d_partial, nblocks, maxdev, true)) return rc;
     for (int c = 0; c < h->C; ++c) {
-      // same rule as lbgpu_upload: the initial spread maps to |h| <= 1024
-      const double scale = maxdev[c] > 0.0 ? (4.0 * maxdev[c]) / 4096.0 : 1.0 / 4096.0;
+      // same rule as lbgpu_upload: offsets up to 64 * max(rho0, 4 * spread)
+      const double span = std::max(fabs(rho0[c]), 4.0 * maxdev[c]);
+      const double scale = span > 0.0 ? span / 1024.0 : 1.0 / 4096.0;
       h->P.rho0[c] = float(rho0[c]);
       h->P.scale[c] = float(scale);
       h->P.inv_scale[c] = float(1.0 / scale);
@@ -449,6 +450,7 @@ extern "C" int lbgpu_init_fields(lbgpu_handle* h, const lbgpu_init* ini) {
     h->device_bytes -= h->n;
     h->mask = nullptr;
   }
+  if (int rc = lb_update_nbmask(h)) return rc;
   h->uploaded = true;
   h->advected = false;
   h->force_valid = 0;

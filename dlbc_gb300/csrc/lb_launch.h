@@ -19,6 +19,7 @@ struct StepBuffers {
   const void* f;        // populations in
   void* fout;           // populations out
   const uint8_t* mask;  // nullptr: no walls
+  const uint32_t* nbmask = nullptr;  // neighbour masks (fused step; set iff mask is)
   void* rho;            // C*N (double for FP64, float otherwise)
   void* psi;            // C*N
   double* force;        // C*N*D when P.record_force
