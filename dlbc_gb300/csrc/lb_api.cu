@@ -360,6 +360,10 @@ int lb_handle_create(const lbgpu_config* cfg, bool lite, double* staging, size_t
     // the fused kernel indexes a component's populations with 32-bit offsets
     h->fused = cfg->precision != LBGPU_FP64 && cfg->q == 19 && !(tk && tk[0] == '1' && !lite) &&
                19 * h->n < (int64_t(1) << 32);
+    // LBGPU_STAGED=1 puts the half form on the cp.async-staged kernel
+    // (bit-identical, slower on GB300: kept for comparison)
+    const char* sg = getenv("LBGPU_STAGED");
+    h->staged = h->fused && !lite && cfg->precision == LBGPU_FP16 && (sg && sg[0] == '1');
   }
   if (lite && !h->fused) {
     *err = "batch members must be FP32/FP16 D3Q19 lattices below 2^32/19 sites";
@@ -432,6 +436,15 @@ int lb_handle_create(const lbgpu_config* cfg, bool lite, double* staging, size_t
   h->f[1] = ptrs[1];
   h->rho = ptrs[2];
   h->psi = ptrs[3];
+  if (h->fused && !lite) {
+    e = cudaMalloc(&h->work_counter, sizeof(int));
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      h->work_counter = nullptr;  // static scheduling
+    } else {
+      h->device_bytes += sizeof(int);
+    }
+  }
   if (!lite) h->staging = static_cast<double*>(ptrs[4]);
   *out = h;
   return LBGPU_OK;
@@ -465,13 +478,43 @@ __global__ void k_nbmask(const uint8_t* __restrict__ mask, uint32_t* __restrict_
   nbm[s] = bits;
 }
 
+// Wall flag of every (x, tile) for the fused step's 8 x 32 tiles: 1 if a
+// site of the tile or of its one-site ring in plane x has a nonzero
+// neighbour mask.
+__global__ void k_tile_walls(const uint32_t* __restrict__ nbm, uint8_t* __restrict__ out, Geo g, int tiles_y,
+                             int tiles_z) {
+  const int tiles = tiles_y * tiles_z;
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= int64_t(g.nx) * tiles) return;
+  const int x = int(i / tiles);
+  const int tile = int(i - int64_t(x) * tiles);
+  const int y0 = (tile / tiles_z) * 8, z0 = (tile % tiles_z) * 32;
+  const int tyv = min(8, g.ny - y0), tzv = min(32, g.nz - z0);
+  uint32_t any = 0;
+  for (int yy = -1; yy <= tyv; ++yy) {
+    const int y = (y0 + yy + g.ny) % g.ny;
+    for (int zz = -1; zz <= tzv; ++zz) {
+      const int z = (z0 + zz + g.nz) % g.nz;
+      any |= nbm[(int64_t(x) * g.ny + y) * g.nz + z];
+    }
+  }
+  out[i] = any != 0;
+}
+
 int lb_update_nbmask(lbgpu_handle* h) {
   const bool want = h->mask && (h->fused || h->lite) && h->Q == 19;
+  const int tiles_y = (h->ny + 7) / 8, tiles_z = (h->nz + 31) / 32;
+  const int64_t nflags = int64_t(h->nx) * tiles_y * tiles_z;
   if (!want) {
     if (h->nbmask) {
       cudaFree(h->nbmask);
       h->device_bytes -= 4 * h->n;
       h->nbmask = nullptr;
+    }
+    if (h->tile_walls) {
+      cudaFree(h->tile_walls);
+      h->device_bytes -= nflags;
+      h->tile_walls = nullptr;
     }
     return LBGPU_OK;
   }
@@ -488,6 +531,21 @@ int lb_update_nbmask(lbgpu_handle* h) {
   h->launches++;
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return h->cuda_fail(e, "neighbour mask kernel");
+  if (h->lite) return LBGPU_OK;  // batch members use other tile shapes
+  if (!h->tile_walls) {
+    e = cudaMalloc(&h->tile_walls, size_t(nflags));
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      h->tile_walls = nullptr;
+      return h->fail(LBGPU_E_NOMEM, "tile wall flags allocation failed");
+    }
+    h->device_bytes += nflags;
+  }
+  k_tile_walls<<<unsigned(ceil_div(nflags, 128)), 128, 0, h->stream>>>(h->nbmask, h->tile_walls, geo_of(h), tiles_y,
+                                                                    tiles_z);
+  h->launches++;
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return h->cuda_fail(e, "tile wall flags kernel");
   return LBGPU_OK;
 }
 
@@ -528,6 +586,8 @@ void lbgpu_destroy(lbgpu_handle* h) {
   if (h->moments) cudaFree(h->moments);
   if (h->mask) cudaFree(h->mask);
   if (h->nbmask) cudaFree(h->nbmask);
+  if (h->tile_walls) cudaFree(h->tile_walls);
+  if (h->work_counter) cudaFree(h->work_counter);
   if (h->force) cudaFree(h->force);
   for (auto& e : h->ev_pending)
     for (auto ev : e.ev) cudaEventDestroy(ev);
@@ -715,6 +775,8 @@ int lbgpu_step(lbgpu_handle* h, int32_t nsteps) {
     b.fout = h->f[1 - h->cur];
     b.mask = h->mask;
     b.nbmask = h->nbmask;
+    b.tile_walls = h->tile_walls;
+    b.work_counter = h->work_counter;
     b.rho = h->rho;
     b.psi = h->psi;
     b.force = h->force;
@@ -744,7 +806,7 @@ int lbgpu_step(lbgpu_handle* h, int32_t nsteps) {
       e = lbk::launch_step_f64(h->Q, h->C, b, P, h->stream, &h->launches, evp);
     else if (h->fused)
       e = lbk::launch_fused(h->cfg.precision == LBGPU_FP16, h->C, b, P, h->stream, &h->launches, evp,
-                            h->cfg.device);
+                            h->cfg.device, h->staged);
     else if (h->cfg.precision == LBGPU_FP32)
       e = lbk::launch_step_f32(h->Q, h->C, b, P, h->stream, &h->launches, evp);
     else

@@ -6,6 +6,7 @@
 
 #include "lb_fused.cuh"
 #include "lb_launch.h"
+#include "lb_staged.cuh"
 
 namespace lbk {
 
@@ -23,6 +24,9 @@ FusedParams make_fused_params(const StepParams& P, int ty) {
   F.eq_form = P.eq_form;
   F.record_force = P.record_force;
   F.unit_tau = P.unit_tau;
+  F.tile_walls = nullptr;
+  F.work_counter = nullptr;
+  F.run_len = P.nx;
   for (int c = 0; c < 2; ++c) {
     F.tau[c] = float(P.tau[c]);
     F.inv_tau[c] = float(1.0 / P.tau[c]);
@@ -114,11 +118,44 @@ cudaError_t go_batch(const FusedSim* sims, int nsims, int64_t total, int parity,
   return cudaGetLastError();
 }
 
+template <int C, bool W>
+cudaError_t go_staged(const StepBuffers& b, const FusedParams& F, cudaStream_t st, int device) {
+  static KernelInfo info;
+  auto kern = k_staged<C, W, 8>;
+  const int smem = int(sizeof(StagedShared<8>));
+  int per_sm = 0;
+  cudaError_t e = kernel_setup(kern, smem, 8 * kFusedTZ, device, info, &per_sm);
+  if (e != cudaSuccess) return e;
+  // (tile, x-chunk) units: as many chunks per tile as keep every CTA slot
+  // busy in lockstep
+  const int64_t slots = int64_t(per_sm) * sm_count(device);
+  const int64_t tiles = int64_t(F.tiles_y) * F.tiles_z;
+  int chunks = tiles >= slots ? 1 : int(slots / tiles);
+  if (chunks > F.nx) chunks = F.nx;
+  const int64_t units = tiles * chunks;
+  const int64_t grid = units < slots ? units : slots;
+  kern<<<unsigned(grid), 8 * kFusedTZ, smem, st>>>(static_cast<const __half*>(b.f), static_cast<__half*>(b.fout),
+                                                   b.nbmask, b.force, F, chunks);
+  return cudaGetLastError();
+}
+
 }  // namespace
 
+bool staged_eligible(const StepParams& P, int c, bool half_storage) {
+  return half_storage && (c == 1 || c == 2) && P.nz % kStagedZH == 0 && P.nz >= kStagedZH &&
+         19 * P.n < (int64_t(1) << 32);
+}
+
 cudaError_t launch_fused(bool half_storage, int c, const StepBuffers& b, const StepParams& P, cudaStream_t st,
-                         int64_t* launches, const StepEvents* ev, int device) {
-  const FusedParams F = make_fused_params(P, 8);
+                         int64_t* launches, const StepEvents* ev, int device, bool staged) {
+  FusedParams F = make_fused_params(P, 8);
+  F.tile_walls = b.tile_walls;
+  if (b.work_counter && !(staged && staged_eligible(P, c, half_storage))) {
+    // runs of at most 32 planes (two of them gathered twice: warm-up)
+    F.work_counter = b.work_counter;
+    F.run_len = P.nx < 64 ? P.nx : 32;
+    cudaMemsetAsync(b.work_counter, 0, sizeof(int), st);
+  }
   const bool w = b.mask != nullptr;
   if (w && !b.nbmask) return cudaErrorInvalidValue;  // walls need the neighbour masks
   if (ev) {
@@ -126,7 +163,12 @@ cudaError_t launch_fused(bool half_storage, int c, const StepBuffers& b, const S
     cudaEventRecord(ev->ev[1], st);
   }
   cudaError_t e;
-  if (half_storage) {
+  if (staged && staged_eligible(P, c, half_storage)) {
+    if (c == 2)
+      e = w ? go_staged<2, true>(b, F, st, device) : go_staged<2, false>(b, F, st, device);
+    else
+      e = w ? go_staged<1, true>(b, F, st, device) : go_staged<1, false>(b, F, st, device);
+  } else if (half_storage) {
     if (c == 2)
       e = w ? go_single<__half, 2, true, 8>(b, F, st, device) : go_single<__half, 2, false, 8>(b, F, st, device);
     else

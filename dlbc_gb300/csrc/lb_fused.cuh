@@ -34,6 +34,8 @@
 #include <cuda_fp16.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 #include "lb_kernels.cuh"
 
 namespace lbk {
@@ -59,6 +61,14 @@ struct FusedParams {
   float wscale[2][19];     // w_q * scale_c
   float inv_wscale[2][19]; // 1 / (w_q * scale_c)
   float hoff[2][19];       // -w_q rho0_c / (w_q scale_c): half value = v / (w_q scale_c) + hoff
+  // per (x, tile) of TY = 8 tiles: 1 if a site of the tile or of its ring
+  // in plane x has a solid neighbour (or is solid); planes without run the
+  // wall-free code.  nullptr: every plane of a walled lattice is walled.
+  const uint8_t* tile_walls;
+  // dynamic scheduling (single lattice): a zeroed counter and the run length
+  // in planes; nullptr: static equal ranges
+  int* work_counter;
+  int32_t run_len;
 };
 
 template <typename T>
@@ -77,9 +87,10 @@ struct FStore<__half> {
   __device__ static __forceinline__ float load(const __half* p, int c, int q, const FusedParams& P) {
     return fmaf(P.wscale[c][q], __half2float(__ldg(p)), P.wrho[c][q]);
   }
-  __device__ static __forceinline__ float load2(const __half* p, int c, int q, int b, bool bb,
-                                                const FusedParams& P) {
-    return fmaf(bb ? P.wscale[c][b] : P.wscale[c][q], __half2float(__ldg(p)), bb ? P.wrho[c][b] : P.wrho[c][q]);
+  // opposite populations have equal weights (w_b = w_q), so either decodes
+  // with q's constants
+  __device__ static __forceinline__ float load2(const __half* p, int c, int q, int, bool, const FusedParams& P) {
+    return fmaf(P.wscale[c][q], __half2float(__ldg(p)), P.wrho[c][q]);
   }
   __device__ static __forceinline__ void store(__half* p, float v, int c, int q, const FusedParams& P) {
     *p = __float2half_rn(fmaf(v, P.inv_wscale[c][q], P.hoff[c][q]));
@@ -159,6 +170,7 @@ __device__ __forceinline__ void fused_body(const FusedParams& P, const T* __rest
   const T* const fc[2] = {f, f + size_t(19) * size_t(P.n)};
   T* const fo[2] = {fout, fout + size_t(19) * size_t(P.n)};
   const bool unit = P.unit_tau != 0;
+  const int ntiles = P.tiles_y * P.tiles_z;
   int64_t w = w0;
   while (w < w1) {
     const int tile = int(w / P.nx);
@@ -189,17 +201,41 @@ __device__ __forceinline__ void fused_body(const FusedParams& P, const T* __rest
     // neighbour masks of this thread's interior site at the gathered plane
     // (nbm_next) and at the plane being collided (nbm_cur)
     uint32_t nbm_next = 0, nbm_cur = 0;
+    bool pw_next = WALLS, pw_cur = WALLS;
+    // whether plane xg of this tile needs the wall code (uniform in the CTA)
+    auto walled = [&](int xg) -> bool {
+      return WALLS && (P.tile_walls == nullptr || __ldg(P.tile_walls + size_t(xg) * ntiles + tile) != 0);
+    };
+    // the wall flag and neighbour masks of the next gathered plane are
+    // loaded one plane ahead, so that the population loads, whose addresses
+    // depend on them, do not wait for them
+    bool pw_pre = false;
+    uint32_t nbm_pre_in = 0, nbm_pre_ring = 0;
+    auto prefetch = [&](int xg) {
+      if (!WALLS) return;
+      pw_pre = walled(xg);
+      const uint32_t pb = uint32_t(xg) * plane_sz;
+      nbm_pre_in = (active && nbmask) ? __ldg(nbmask + pb + uint32_t(yz_in.off[1][1])) : 0u;
+      nbm_pre_ring = (has_ring && nbmask) ? __ldg(nbmask + pb + uint32_t(yz_ring.off[1][1])) : 0u;
+    };
 
     // rho/psi of plane xg into psi slot ps (and the tile's populations into
-    // buffer keep, unless keep < 0)
-    auto gather_plane = [&](int ps, int xg, int keep) {
+    // buffer keep, unless keep < 0); prefetches plane xn's flag and masks
+    auto gather_plane = [&](int ps, int xg, int keep, int xn) {
       const uint32_t planes[3] = {uint32_t(wrap(xg - 1, P.nx)) * plane_sz, uint32_t(xg) * plane_sz,
                                   uint32_t(wrap(xg + 1, P.nx)) * plane_sz};
+      const bool pw = WALLS && pw_pre;
+      const uint32_t nbm_in = nbm_pre_in, nbm_ring = nbm_pre_ring;
+      prefetch(xn);
+      pw_next = pw;
       if (active) {
-        const uint32_t nbm = (WALLS && nbmask) ? __ldg(nbmask + planes[1] + uint32_t(yz_in.off[1][1])) : 0u;
+        const uint32_t nbm = pw ? nbm_in : 0u;
         nbm_next = nbm;
         float pop[C][19];
-        fused_gather<T, WALLS, C>(fc, P, planes, yz_in, nbm, pop);
+        if (pw)
+          fused_gather<T, WALLS, C>(fc, P, planes, yz_in, nbm, pop);
+        else
+          fused_gather<T, false, C>(fc, P, planes, yz_in, 0u, pop);
 #pragma unroll
         for (int c = 0; c < C; ++c) {
           const float den = density<19, float>(pop[c]);
@@ -212,9 +248,12 @@ __device__ __forceinline__ void fused_body(const FusedParams& P, const T* __rest
         }
       }
       if (has_ring) {
-        const uint32_t nbm = (WALLS && nbmask) ? __ldg(nbmask + planes[1] + uint32_t(yz_ring.off[1][1])) : 0u;
+        const uint32_t nbm = pw ? nbm_ring : 0u;
         float pop[C][19];
-        fused_gather<T, WALLS, C>(fc, P, planes, yz_ring, nbm, pop);
+        if (pw)
+          fused_gather<T, WALLS, C>(fc, P, planes, yz_ring, nbm, pop);
+        else
+          fused_gather<T, false, C>(fc, P, planes, yz_ring, 0u, pop);
 #pragma unroll
         for (int c = 0; c < C; ++c) {
           const float den = density<19, float>(pop[c]);
@@ -226,22 +265,26 @@ __device__ __forceinline__ void fused_body(const FusedParams& P, const T* __rest
 
     // warm-up: rho/psi of xs-1; rho/psi + populations of xs
     __syncthreads();
-    gather_plane(0, wrap(xs - 1, P.nx), -1);
-    gather_plane(1, xs, 0);
+    prefetch(wrap(xs - 1, P.nx));
+    gather_plane(0, wrap(xs - 1, P.nx), -1, xs);
+    gather_plane(1, xs, 0, wrap(xs + 1, P.nx));
     int cur = 0;
     for (int k = 0; k < run; ++k) {
       const int x = xs + k;
       const int sm = k % 3, s0 = (k + 1) % 3, sp = (k + 2) % 3;  // psi slots of x-1, x, x+1
       nbm_cur = nbm_next;
+      pw_cur = pw_next;
       __syncthreads();  // psi slot sp and pops buffer 1-cur are free
-      gather_plane(sp, wrap(x + 1, P.nx), 1 - cur);
+      gather_plane(sp, wrap(x + 1, P.nx), 1 - cur, wrap(x + 2, P.nx));
       __syncthreads();
-      if (active) {
+      // the collision of plane x, with or without the wall code
+      auto collide = [&](auto wtag) {
+        constexpr bool W = decltype(wtag)::value;
         const uint32_t s = uint32_t(x) * plane_sz + uint32_t(yz_in.off[1][1]);
         const int c1y = ty + 1, c1z = tz + 1;
         // branch-free: solid sites compute like fluid ones and store their
         // own populations (warps straddling a wall run one code path)
-        const bool solid = WALLS && (nbm_cur & 1u);
+        const bool solid = W && (nbm_cur & 1u);
         float den[C];
 #pragma unroll
         for (int c = 0; c < C; ++c) den[c] = sh.rho[s0][c][c1y][c1z];
@@ -262,7 +305,7 @@ __device__ __forceinline__ void fused_body(const FusedParams& P, const T* __rest
             for (int q = 1; q < 19; ++q) {
               const int cx = Conn<19>::cx(q), cy = Conn<19>::cy(q), cz = Conn<19>::cz(q);
               float v = sh.psi[pslot[cx + 1]][c][c1y + cy][c1z + cz];
-              if (WALLS && ((nbm_cur >> q) & 1u)) v = own[c];
+              if (W && ((nbm_cur >> q) & 1u)) v = own[c];
               if (Conn<19>::wclass(q) == 1)
                 stencil_acc(a, cx, cy, cz, v);
               else
@@ -282,7 +325,7 @@ __device__ __forceinline__ void fused_body(const FusedParams& P, const T* __rest
             }
 #pragma unroll
             for (int vd = 0; vd < 3; ++vd) F[f1][vd] = -own[f1] * g[vd];
-            if (WALLS) {
+            if (W) {
               const float wc = P.gwc[f1];
               if (wc != 0.f) {
                 float a[3] = {0.f, 0.f, 0.f}, d[3] = {0.f, 0.f, 0.f};
@@ -369,7 +412,10 @@ __device__ __forceinline__ void fused_body(const FusedParams& P, const T* __rest
             FStore<T>::store(fo[c] + (P.qn[q] + s), solid ? pop[q] : v, c, q, P);
           }
         }
-      }
+      };
+      // (a wall-free plane of a walled lattice has zero neighbour masks: the
+      // wall code computes the same there, so only the gather is specialised)
+      if (active) collide(std::integral_constant<bool, WALLS>{});
       cur = 1 - cur;
     }
     w += run;
@@ -382,9 +428,28 @@ __global__ void __launch_bounds__(TY * kFusedTZ, 8 / TY * 2 > 4 ? 4 : 8 / TY * 2
             double* __restrict__ force_out, FusedParams P) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   FusedShared<TY>& sh = *reinterpret_cast<FusedShared<TY>*>(smem_raw);
-  const int64_t w0 = P.work * blockIdx.x / gridDim.x;
-  const int64_t w1 = P.work * (blockIdx.x + 1) / gridDim.x;
-  fused_body<T, C, WALLS, TY>(P, f, fout, nbmask, force_out, w0, w1, sh);
+  if (!P.work_counter) {
+    const int64_t w0 = P.work * blockIdx.x / gridDim.x;
+    const int64_t w1 = P.work * (blockIdx.x + 1) / gridDim.x;
+    fused_body<T, C, WALLS, TY>(P, f, fout, nbmask, force_out, w0, w1, sh);
+    return;
+  }
+  // dynamic: runs of run_len planes of one tile, taken in tile-major order
+  // from a counter, so that CTAs on cheap (wall-free) tiles take more runs
+  __shared__ int s_item;
+  const int nchunks = (P.nx + P.run_len - 1) / P.run_len;
+  const int units = P.tiles_y * P.tiles_z * nchunks;
+  for (;;) {
+    __syncthreads();  // every thread has read the previous item
+    if (threadIdx.x == 0) s_item = atomicAdd(P.work_counter, 1);
+    __syncthreads();
+    const int item = s_item;
+    if (item >= units) break;
+    const int tile = item / nchunks, ch = item - tile * nchunks;
+    const int64_t w0 = int64_t(tile) * P.nx + int64_t(ch) * P.run_len;
+    const int64_t w1 = min(w0 + P.run_len, int64_t(tile + 1) * P.nx);
+    fused_body<T, C, WALLS, TY>(P, f, fout, nbmask, force_out, w0, w1, sh);
+  }
 }
 
 // One simulation of a batch.  The step reads populations f[(parity + phase)

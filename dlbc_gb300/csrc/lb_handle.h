@@ -27,6 +27,8 @@ struct lbgpu_handle {
   int cur = 0;
   uint8_t* mask = nullptr;
   uint32_t* nbmask = nullptr;       // neighbour masks for the fused step (walls only)
+  uint8_t* tile_walls = nullptr;    // per (x, 8x32 tile) wall flags for the fused step
+  int* work_counter = nullptr;      // the fused step's dynamic scheduling counter
   void* rho = nullptr;
   void* psi = nullptr;
   double* force = nullptr;
@@ -44,6 +46,8 @@ struct lbgpu_handle {
   // FP32/FP16 D3Q19 run the fused single-pass kernel; LBGPU_TWO_KERNEL=1 in
   // the environment at lbgpu_create selects the two-kernel step instead
   bool fused = false;
+  // the FP16 form uses the TMA-staged kernel where the lattice qualifies
+  bool staged = false;
   // per-kernel event timing (lbgpu_profile)
   bool profiling = false;
   std::vector<lbk::StepEvents> ev_pending, ev_pool;

@@ -20,6 +20,8 @@ struct StepBuffers {
   void* fout;           // populations out
   const uint8_t* mask;  // nullptr: no walls
   const uint32_t* nbmask = nullptr;  // neighbour masks (fused step; set iff mask is)
+  const uint8_t* tile_walls = nullptr;  // per (x, 8x32 tile) wall flags (fused step)
+  int* work_counter = nullptr;          // dynamic scheduling counter (fused step)
   void* rho;            // C*N (double for FP64, float otherwise)
   void* psi;            // C*N
   double* force;        // C*N*D when P.record_force
@@ -50,9 +52,12 @@ cudaError_t launch_phase_f16(int phase, int q, int c, const StepBuffers& b, cons
 namespace lbk {
 
 // Fused single-pass D3Q19 step (lb_fused.cuh) for the float-arithmetic
-// forms.  `half_storage` selects half offsets instead of float storage.
+// forms.  `half_storage` selects half offsets instead of float storage;
+// `staged` lets the half form use the TMA-staged kernel (lb_staged.cuh)
+// where the lattice qualifies (staged_eligible).
 cudaError_t launch_fused(bool half_storage, int c, const StepBuffers& b, const StepParams& P, cudaStream_t stream,
-                         int64_t* launches, const StepEvents* ev, int device);
+                         int64_t* launches, const StepEvents* ev, int device, bool staged);
+bool staged_eligible(const StepParams& P, int c, bool half_storage);
 
 }  // namespace lbk
 
