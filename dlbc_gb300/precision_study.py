@@ -9,9 +9,9 @@ fields; the FP64 form is the reference for the errors (it is bit-identical to
 the CPU restatement of the reference, checked at small sizes by the tests).
 
 Reported per form: time and MLUPS, relative L2 error of each component's
-density and velocity against FP64 at checkpoints, and the fraction of sites
+density and velocity against FP64 at checkpoints, the fraction of sites
 whose phase (sign of rho_red - rho_blue) differs from FP64's (the interface
-position error).
+position error), and the relative change of each component's total mass.
 """
 from __future__ import annotations
 
@@ -40,6 +40,7 @@ def spinodal_params(n: int, perturb: float) -> params.LBParams:
 def run_form(p, precision, steps, checkpoints, seed, device=0):
     g = lbgpu.GPULattice(p, precision=precision, device=device)
     g.init_device(seed)
+    mass0, _ = g.reduce()
     out = {}
     done = 0
     t_total = 0.0
@@ -52,7 +53,9 @@ def run_form(p, precision, steps, checkpoints, seed, device=0):
         done = cp
         dens = g.density()
         vel = g.velocity()
-        out[cp] = ([d.astype(np.float64) for d in dens], [v.astype(np.float64) for v in vel])
+        mass, _ = g.reduce()
+        drift = [float((mass[c] - mass0[c]) / mass0[c]) for c in range(len(mass))]
+        out[cp] = ([d.astype(np.float64) for d in dens], [v.astype(np.float64) for v in vel], drift)
     g.close()
     return out, t_total
 
@@ -75,16 +78,18 @@ def main():
     ref, t64 = run_form(p, lbgpu.FP64, args.steps, cps, args.seed)
     report = {"workload": f"{args.n}^3 periodic spinodal decomposition, rho 0.7 +- {args.perturb}, "
                           f"{args.steps} steps, BDist2, g 3.6",
-              "fp64": {"time_s": round(t64, 2), "mlups": round(sites * args.steps / t64 / 1e6, 1)}}
+              "fp64": {"time_s": round(t64, 2), "mlups": round(sites * args.steps / t64 / 1e6, 1),
+                       "mass_drift": {cp: ref[cp][2] for cp in cps}}}
     for name, prec in (("fp32", lbgpu.FP32), ("fp16", lbgpu.FP16)):
         res, t = run_form(p, prec, args.steps, cps, args.seed)
         errs = {}
         for cp in cps:
-            (d, v), (d64, v64) = res[cp], ref[cp]
+            (d, v, drift), (d64, v64, _) = res[cp], ref[cp]
             phase = np.mean(np.sign(d[0] - d[1]) != np.sign(d64[0] - d64[1]))
             errs[cp] = {"rho_l2": [rel_l2(d[c], d64[c]) for c in range(2)],
                         "u_l2": [rel_l2(v[c], v64[c]) for c in range(2)],
-                        "phase_mismatch_fraction": float(phase)}
+                        "phase_mismatch_fraction": float(phase),
+                        "mass_drift": drift}
         report[name] = {"time_s": round(t, 2), "mlups": round(sites * args.steps / t / 1e6, 1), "errors": errs}
         del res
     print(json.dumps(report))
