@@ -97,9 +97,25 @@ def _local_mask(p: LBParams, nl, nc, cc, nlH) -> np.ndarray:
                 m[g[vd] < p.wall_thickness] = 1
             if p.dimension_has_wall[vd][1]:
                 m[g[vd] >= nl[vd] * nc[vd] - p.wall_thickness] = 1
+    elif mi == 1:  # File (mask.d:153-155): the global mask, this process's block
+        gm = _read_global(p.mask_file, tuple(int(x) for x in p.gn[:d]), "mask.maskFile")
+        block = tuple(slice(cc[i] * nl[i], (cc[i] + 1) * nl[i]) for i in range(d))
+        m[tuple(slice(HALO, HALO + nl[i]) for i in range(d))] = gm[block]
     else:
-        raise ValueError("maskInit = File is not supported by the host initialiser")
+        raise ValueError(f"unsupported maskInit {mi}")
     return m
+
+
+def _read_global(path: str, shape, what: str) -> np.ndarray:
+    """A field file as readField reads it (src/dlbc/io/hdf5.d:309): the
+    /OutArray of the global lattice, checked against the lattice size."""
+    from . import h5
+    if not path:
+        raise ValueError(f"{what} is not set")
+    a = h5.read_field(path)
+    if tuple(a.shape[: len(shape)]) != tuple(shape):
+        raise ValueError(f"{what} {path}: shape {a.shape} does not match the lattice {shape}")
+    return a
 
 
 def _local_fluid(p: LBParams, f: int, rng: _Rng, nl, nc, cc, nlH) -> np.ndarray:
@@ -115,9 +131,14 @@ def _local_fluid(p: LBParams, f: int, rng: _Rng, nl, nc, cc, nlH) -> np.ndarray:
         return (grids[i] + float(cc[i] * nl[i])) - float(HALO)
 
     out = np.full(tuple(nlH) + (q,), np.nan)
-    if fi in (_FI["None"], _FI["File"]):
-        if fi == _FI["File"]:
-            raise ValueError("fluidInit = File is not supported by the host initialiser")
+    if fi == _FI["None"]:
+        return out
+    if fi == _FI["File"]:  # init.d:272-275: this process's block of the file
+        ga = _read_global(p.fluid_files[f] if f < len(p.fluid_files) else "", tuple(gsz), "init.fluidFiles")
+        if ga.shape != tuple(gsz) + (q,):
+            raise ValueError(f"init.fluidFiles {p.fluid_files[f]}: shape {ga.shape}, expected {tuple(gsz) + (q,)}")
+        block = tuple(slice(cc[i] * nl[i], (cc[i] + 1) * nl[i]) for i in range(d))
+        out[tuple(slice(HALO, HALO + nl[i]) for i in range(d))] = ga[block]
         return out
     if fi == _FI["Const"]:
         out[...] = dens[0]

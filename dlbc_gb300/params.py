@@ -183,7 +183,9 @@ class LBParams:
     init_axis: int = 0
     interface_thickness: float = 0.0
     lamellae_widths: List[float] = dataclasses.field(default_factory=list)
+    fluid_files: List[str] = dataclasses.field(default_factory=list)
     mask_init: int = 0
+    mask_file: str = ""
     mask_axis: int = 0
     wall_offset: int = 0
     wall_thickness: int = 1
@@ -241,6 +243,8 @@ class LBParams:
         p.init_axis = _enum(d.get("lb.init.initAxis", "X"), AXES, "initAxis")
         p.interface_thickness = float(d.get("lb.init.interfaceThickness", 0.0))
         p.lamellae_widths = [float(x) for x in d.get("lb.init.lamellaeWidths", [])]
+        p.fluid_files = [str(x) for x in _arr(d, "lb.init.fluidFiles", C, fill="")]
+        p.mask_file = str(d.get("lb.mask.maskFile", ""))
         p.mask_init = _enum(d.get("lb.mask.maskInit", "None"), MASK_INITS, "maskInit")
         p.mask_axis = _enum(d.get("lb.mask.initAxis", "X"), AXES, "mask.initAxis")
         p.wall_offset = int(d.get("lb.mask.wallOffset", 0))

@@ -147,6 +147,18 @@ def main(ref: str):
             names.append(key)
     out["keys"] = np.array(names)
     out["cases"] = np.array(INIT_2D)
+    # maskInit = File: the case's input text, its mask file and the hashes of
+    # its t = 0 dumps (the fluid File case reads 0.6 MB population files and
+    # is covered with synthetic files instead)
+    case = "mask-init-file-2d"
+    out["file/" + case + "/input"] = np.array(open(os.path.join(root, case + ".in")).read())
+    out["file/" + case + "/mask"] = h5.read_field(os.path.join(root, "reference-data", f"mask-{case}-t00000000.h5"))
+    for f in sorted(glob.glob(os.path.join(root, "reference-data", f"*-{case}-t00000000.h5"))):
+        base = os.path.basename(f)
+        kind = golden_kind(base)
+        field = base.split("-")[1] if kind not in ("colour", "mask") else ""
+        key = f"file/{case}/{kind}" + (f"-{field}" if field else "")
+        out[key + "/sha256"] = np.array(sha(h5.read_field(f)))
     path = os.path.join(HERE, "init-2d.npz")
     np.savez_compressed(path, **out)
     print(f"{path}: {len(names)} hashes, {os.path.getsize(path)} bytes")
