@@ -152,6 +152,7 @@ def roofline(precision, sites, kernel_ms, peak, peak_kind, traffic=None):
     or k_fused (the single-pass FP32 / FP16 step)."""
     alg = bytes_per_site(precision) * sites
     achieved = alg / (kernel_ms * 1e-3) / 1e9
+    from dlbc_gb300 import lbgpu
     kernel = "k_collide" if precision == lbgpu.FP64 else "k_fused"
     return {"bound": "hbm", "kernel": kernel, "achieved": round(achieved, 1), "peak": peak,
             "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),

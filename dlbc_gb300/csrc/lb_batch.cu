@@ -12,6 +12,7 @@
 // computes the same per-site arithmetic, so tuning steps are ordinary steps.
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <map>
@@ -56,6 +57,8 @@ struct lbgpu_batch {
   int table_cap = 0;
   int table_n = 0;
   int64_t total_work = 0;
+  int64_t total_units = 0;
+  int* d_counters = nullptr;  // dynamic scheduling, one per buffer parity
   bool walls = false;
   bool dirty = true;
   int64_t steps_since_build = 0;
@@ -103,6 +106,7 @@ int build_table(lbgpu_batch* b, int ty) {
   b->table_ids.clear();
   b->table_phase.clear();
   b->total_work = 0;
+  b->total_units = 0;
   b->walls = false;
   for (size_t id = 0; id < b->sims.size(); ++id) {
     lbgpu_handle* h = b->sims[id];
@@ -116,6 +120,10 @@ int build_table(lbgpu_batch* b, int ty) {
     fs.force_out = nullptr;
     fs.work_begin = b->total_work;
     fs.phase = h->cur;
+    fs.P.run_len = h->nx < 64 ? h->nx : 32;
+    fs.nchunks = (h->nx + fs.P.run_len - 1) / fs.P.run_len;
+    fs.unit_begin = b->total_units;
+    b->total_units += int64_t(fs.P.tiles_y) * fs.P.tiles_z * fs.nchunks;
     b->total_work += fs.P.work;
     b->walls = b->walls || h->mask != nullptr;
     tab.push_back(fs);
@@ -135,6 +143,14 @@ int build_table(lbgpu_batch* b, int ty) {
     }
     b->table_cap = cap;
   }
+  if (!b->d_counters) {
+    cudaError_t e = cudaMalloc(&b->d_counters, 2 * sizeof(int));
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      b->d_counters = nullptr;  // static scheduling
+    }
+  }
+  if (b->d_counters) cudaMemsetAsync(b->d_counters, 0, 2 * sizeof(int), b->stream);
   if (b->table_n) {
     cudaError_t e = cudaMemcpyAsync(b->d_table, tab.data(), sizeof(lbk::FusedSim) * tab.size(),
                                     cudaMemcpyHostToDevice, b->stream);
@@ -156,9 +172,16 @@ void sync_members(lbgpu_batch* b) {
 }
 
 cudaError_t launch_one(lbgpu_batch* b, int parity) {
+  // LBGPU_BATCH_STATIC=1: equal static shares instead of dynamic runs
+  static const bool kStatic = [] {
+    const char* s = getenv("LBGPU_BATCH_STATIC");
+    return s && s[0] == '1';
+  }();
   b->launches++;
   return lbk::launch_fused_batch(b->precision == LBGPU_FP16, b->shape.ty, b->walls, b->d_table, b->table_n,
-                                 b->total_work, parity, b->shape.ctas_per_sm, b->stream, b->device);
+                                 b->total_work, parity, b->shape.ctas_per_sm, b->stream, b->device,
+                                 b->total_units,
+                                 (!kStatic && b->total_units < (int64_t(1) << 31)) ? b->d_counters : nullptr);
 }
 
 // advance n steps with the current table and shape
@@ -316,6 +339,7 @@ void lbgpu_batch_destroy(lbgpu_batch* b) {
     if (h) lbgpu_destroy(h);
   drop_graph(b);
   if (b->d_table) cudaFree(b->d_table);
+  if (b->d_counters) cudaFree(b->d_counters);
   cudaFree(b->staging);
   if (b->own_stream) cudaStreamDestroy(b->own_stream);
   delete b;

@@ -95,15 +95,24 @@ cudaError_t go_single(const StepBuffers& b, const FusedParams& F, cudaStream_t s
   cudaError_t e = kernel_setup(kern, smem, TY * kFusedTZ, device, info, &per_sm);
   if (e != cudaSuccess) return e;
   int64_t grid = int64_t(per_sm) * sm_count(device);
-  if (grid > F.work) grid = F.work;
+  FusedParams G = F;
+  if (G.work_counter) {
+    // runs of 32 planes, halved while there would be fewer than two runs
+    // per CTA (each run gathers two extra planes to warm up)
+    const int64_t tiles = int64_t(G.tiles_y) * G.tiles_z;
+    int rl = 32;
+    while (rl > 4 && tiles * ((G.nx + rl - 1) / rl) < 2 * grid) rl /= 2;
+    G.run_len = rl < G.nx ? rl : G.nx;
+  }
+  if (grid > G.work) grid = G.work;
   kern<<<unsigned(grid), TY * kFusedTZ, smem, st>>>(static_cast<const T*>(b.f), static_cast<T*>(b.fout), b.nbmask,
-                                                    b.force, F);
+                                                    b.force, G);
   return cudaGetLastError();
 }
 
 template <typename T, bool W, int TY>
 cudaError_t go_batch(const FusedSim* sims, int nsims, int64_t total, int parity, int ctas_per_sm, cudaStream_t st,
-                     int device) {
+                     int device, int64_t total_units, int* counters) {
   static KernelInfo info;
   auto kern = k_fused_batch<T, 2, W, TY>;
   const int smem = int(sizeof(FusedShared<TY>));
@@ -114,7 +123,7 @@ cudaError_t go_batch(const FusedSim* sims, int nsims, int64_t total, int parity,
   int64_t grid = int64_t(per_sm) * sm_count(device);
   if (grid > total) grid = total;
   if (grid < 1) return cudaSuccess;
-  kern<<<unsigned(grid), TY * kFusedTZ, smem, st>>>(sims, nsims, total, parity);
+  kern<<<unsigned(grid), TY * kFusedTZ, smem, st>>>(sims, nsims, total, parity, total_units, counters);
   return cudaGetLastError();
 }
 
@@ -151,9 +160,9 @@ cudaError_t launch_fused(bool half_storage, int c, const StepBuffers& b, const S
   FusedParams F = make_fused_params(P, 8);
   F.tile_walls = b.tile_walls;
   if (b.work_counter && !(staged && staged_eligible(P, c, half_storage))) {
-    // runs of at most 32 planes (two of them gathered twice: warm-up)
+    // dynamic runs (length chosen at launch)
     F.work_counter = b.work_counter;
-    F.run_len = P.nx < 64 ? P.nx : 32;
+    F.run_len = 32;
     cudaMemsetAsync(b.work_counter, 0, sizeof(int), st);
   }
   const bool w = b.mask != nullptr;
@@ -185,8 +194,10 @@ cudaError_t launch_fused(bool half_storage, int c, const StepBuffers& b, const S
 }
 
 cudaError_t launch_fused_batch(bool half_storage, int ty, bool walls, const FusedSim* sims, int nsims,
-                               int64_t total_work, int parity, int ctas_per_sm, cudaStream_t st, int device) {
-#define LB_BATCH(T, W, TYV) go_batch<T, W, TYV>(sims, nsims, total_work, parity, ctas_per_sm, st, device)
+                               int64_t total_work, int parity, int ctas_per_sm, cudaStream_t st, int device,
+                               int64_t total_units, int* counters) {
+#define LB_BATCH(T, W, TYV) \
+  go_batch<T, W, TYV>(sims, nsims, total_work, parity, ctas_per_sm, st, device, total_units, counters)
   if (half_storage) {
     if (ty == 4) return walls ? LB_BATCH(__half, true, 4) : LB_BATCH(__half, false, 4);
     return walls ? LB_BATCH(__half, true, 8) : LB_BATCH(__half, false, 8);

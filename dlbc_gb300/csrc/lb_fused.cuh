@@ -460,51 +460,79 @@ struct FusedSim {
   const uint32_t* nbmask;  // neighbour masks; nullptr: no solid site
   double* force_out;       // nullptr unless recording
   int64_t work_begin;      // first plane-tile of this simulation in the batch
+  int64_t unit_begin;      // first run of this simulation (dynamic scheduling)
   int32_t phase;
-  int32_t pad;
+  int32_t nchunks;         // runs per tile: ceil(nx / P.run_len)
 };
 
-// Many independent lattices of any sizes in one persistent launch: the
-// concatenated plane-tile work of all simulations is split into equal
-// contiguous ranges, one per CTA.
+// Many independent lattices of any sizes in one persistent launch.  With
+// `counters`, CTAs take runs of at most run_len planes of one tile (all
+// simulations' runs concatenated) from counters[parity] and zero the other
+// counter for the next launch; without, the concatenated plane-tile work is
+// split into equal contiguous ranges, one per CTA.
 template <typename T, int C, bool WALLS, int TY>
 __global__ void __launch_bounds__(TY * kFusedTZ, 8 / TY * 2 > 4 ? 4 : 8 / TY * 2)
-    k_fused_batch(const FusedSim* __restrict__ sims, int nsims, int64_t total_work, int parity) {
+    k_fused_batch(const FusedSim* __restrict__ sims, int nsims, int64_t total_work, int parity,
+                  int64_t total_units, int* __restrict__ counters) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   FusedShared<TY>& sh = *reinterpret_cast<FusedShared<TY>*>(smem_raw);
   __shared__ FusedParams Ps;
   __shared__ int s_idx;
-  const int64_t w0 = total_work * blockIdx.x / gridDim.x;
-  const int64_t w1 = total_work * (blockIdx.x + 1) / gridDim.x;
-  int64_t w = w0;
-  while (w < w1) {
-    __syncthreads();
+  __shared__ long long s_w[2];
+  if (counters && blockIdx.x == 0 && threadIdx.x == 0) counters[1 - parity] = 0;
+  // static: this CTA's equal share [w, wend) of the plane-tiles; dynamic:
+  // runs taken from the counter
+  long long w = total_work * blockIdx.x / gridDim.x;
+  const long long wend = total_work * (blockIdx.x + 1) / gridDim.x;
+  for (;;) {
+    __syncthreads();  // every thread has used the previous range and Ps
     if (threadIdx.x == 0) {
-      int lo = 0, hi = nsims - 1;  // last simulation with work_begin <= w
-      while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (sims[mid].work_begin <= w)
-          lo = mid;
-        else
-          hi = mid - 1;
+      long long r0 = 0, r1 = 0;
+      int idx = 0;
+      const long long key = counters ? (long long)atomicAdd(counters + parity, 1) : w;
+      if (counters ? key < total_units : key < wend) {
+        int lo = 0, hi = nsims - 1;  // last simulation starting at or before key
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if ((counters ? sims[mid].unit_begin : sims[mid].work_begin) <= key)
+            lo = mid;
+          else
+            hi = mid - 1;
+        }
+        idx = lo;
+        if (counters) {
+          const long long local = key - sims[lo].unit_begin;
+          const int nch = sims[lo].nchunks;
+          const long long tile = local / nch, ch = local - tile * nch;
+          const int nx = sims[lo].P.nx, rl = sims[lo].P.run_len;
+          r0 = sims[lo].work_begin + tile * nx + ch * rl;
+          const long long tile_end = sims[lo].work_begin + (tile + 1) * nx;
+          r1 = r0 + rl < tile_end ? r0 + rl : tile_end;
+        } else {
+          const long long sim_end = sims[lo].work_begin + sims[lo].P.work;
+          r0 = key;
+          r1 = wend < sim_end ? wend : sim_end;
+        }
       }
-      s_idx = lo;
+      s_w[0] = r0;
+      s_w[1] = r1;
+      s_idx = idx;
     }
     __syncthreads();
+    if (s_w[0] >= s_w[1]) break;
     const int i = s_idx;
     // stage this simulation's parameters (FusedParams is a multiple of 4 bytes)
     const int* src = reinterpret_cast<const int*>(&sims[i].P);
     int* dst = reinterpret_cast<int*>(&Ps);
     for (int k = threadIdx.x; k < int(sizeof(FusedParams) / 4); k += blockDim.x) dst[k] = src[k];
-    const int64_t wb = sims[i].work_begin;
-    const int64_t we = wb + sims[i].P.work;
-    const int64_t end = min(w1, we);
+    const long long wb = sims[i].work_begin;
     const int par = (parity + sims[i].phase) & 1;
     const T* fin = static_cast<const T*>(sims[i].f[par]);
     T* fout = const_cast<T*>(static_cast<const T*>(sims[i].f[1 - par]));
+    const long long r0 = s_w[0], r1 = s_w[1];
     __syncthreads();
-    fused_body<T, C, WALLS, TY>(Ps, fin, fout, sims[i].nbmask, sims[i].force_out, w - wb, end - wb, sh);
-    w = end;
+    fused_body<T, C, WALLS, TY>(Ps, fin, fout, sims[i].nbmask, sims[i].force_out, r0 - wb, r1 - wb, sh);
+    w = r1;
   }
 }
 

@@ -72,7 +72,10 @@ size_t fused_smem_bytes(int ty);
 
 // One timestep of every simulation in `sims` (device array, two-component,
 // D3Q19) in one persistent launch.  ctas_per_sm <= 0: as many as fit.
+// counters (two ints, zero before the first launch): dynamic scheduling of
+// total_units runs; nullptr: static equal ranges of total_work plane-tiles.
 cudaError_t launch_fused_batch(bool half_storage, int ty, bool walls, const FusedSim* sims, int nsims,
-                               int64_t total_work, int parity, int ctas_per_sm, cudaStream_t stream, int device);
+                               int64_t total_work, int parity, int ctas_per_sm, cudaStream_t stream, int device,
+                               int64_t total_units, int* counters);
 
 }  // namespace lbk
