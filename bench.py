@@ -216,12 +216,18 @@ def batched_params(n_sims=256, seed=3):
     return out
 
 
-def run_batched(device, torch, n_sims=256, steps=2000, baseline_steps=20):
+def run_batched(device, torch, n_sims=256, steps=2000, baseline_steps=20, dist=None):
     """The batched workload in one batch (FP16 offset storage, FP32 arithmetic), timed with
     CUDA events on the batch's stream; the sequential baseline runs each size
-    class alone in the plain FP64 form for a few steps and extrapolates."""
-    from dlbc_gb300 import lbgpu
-    ps = batched_params(n_sims)
+    class alone in the plain FP64 form for a few steps and extrapolates.  With
+    several ranks the lattices are split over them by size (no exchange) and
+    the time is the slowest rank's."""
+    from dlbc_gb300 import lbgpu, replicas
+    all_ps = batched_params(n_sims)
+    world = dist.get_world_size() if dist is not None else 1
+    rank = dist.get_rank() if dist is not None else 0
+    mine = replicas.shard([q.gn[0] * q.gn[1] * q.gn[2] for q in all_ps], world)[rank]
+    ps = [all_ps[i] for i in mine]
     b = lbgpu.Batch(precision=lbgpu.FP16, device=device)
     for p in ps:
         b.add_device(p)
@@ -237,11 +243,12 @@ def run_batched(device, torch, n_sims=256, steps=2000, baseline_steps=20):
     b.step(steps)
     stop.record(stream)
     stop.synchronize()
-    ms = start.elapsed_time(stop)
+    ms = replicas.max_over_ranks(start.elapsed_time(stop), dist, device=f"cuda:{device}")
     launches = b.launch_count - n0
-    sites = sum(p.gn[0] * p.gn[1] * p.gn[2] for p in ps)
+    sites = sum(p.gn[0] * p.gn[1] * p.gn[2] for p in all_ps)
     dev_bytes = b.device_bytes
     b.close()
+    ps = all_ps
     # sequential plain-form baseline per size class
     per_step = {}
     for L in sorted({p.gn[0] for p in ps}):
@@ -260,6 +267,7 @@ def run_batched(device, torch, n_sims=256, steps=2000, baseline_steps=20):
         "workload": f"{n_sims} periodic D3Q19 two-sphere lattices, L in {{32,48,64,80,96}}, {steps} steps, "
                     f"tau~U[0.8,1.2], g~U[3.2,4.0]",
         "form": "fp16 offset storage, fp32 arithmetic", "sims": n_sims, "steps": steps,
+        "ranks": world, "sharding": "whole lattices, balanced by sites (largest first), no exchange",
         "total_sites": int(sites), "time_s": round(ms / 1e3, 3), "sims_per_s": round(n_sims / (ms / 1e3), 3),
         "aggregate_mlups": round(sites * steps / (ms / 1e3) / 1e6, 1), "launch_shape": list(shape),
         "kernel_launches": launches, "device_bytes": int(dev_bytes),
@@ -270,15 +278,33 @@ def run_batched(device, torch, n_sims=256, steps=2000, baseline_steps=20):
     }
 
 
-def run_served(device, n_requests=32, step_scale=0.1, rate=50.0, budget_gb=120.0):
+def run_served(device, n_requests=32, step_scale=0.1, rate=50.0, budget_gb=120.0, dist=None):
     """The served workload (request steps scaled by step_scale to keep the run short):
-    Poisson arrivals, admission by an HBM budget, continuous batching."""
+    Poisson arrivals, admission by an HBM budget, continuous batching.  With
+    several ranks, request i goes to rank i mod N (each GPU serves its own
+    stream, no exchange); latencies are gathered on rank 0."""
     import numpy as np
-    from dlbc_gb300 import lbgpu, serve
+    from dlbc_gb300 import lbgpu, replicas, serve
     reqs = serve.request_stream(n_requests, rate=rate, seed=2024, step_scale=step_scale)
+    world = dist.get_world_size() if dist is not None else 1
+    rank = dist.get_rank() if dist is not None else 0
     srv = serve.Server(precision=lbgpu.FP16, budget_bytes=budget_gb * 1e9, device=device)
-    out = srv.run(reqs)
+    out = srv.run([r for r in reqs if r.rid % world == rank])
+    parts = replicas.gather_to_root(out, dist)
+    if rank != 0:
+        return None
+    if world > 1:
+        results = [r for part in parts for r in part["results"]]
+        lat = np.array([r["latency"] for r in results])
+        wall = max(part["makespan_s"] for part in parts)
+        work = sum(r["sites"] * r["steps"] for r in results)
+        out = {"requests": len(results), "p50_latency_s": float(np.percentile(lat, 50)),
+               "p99_latency_s": float(np.percentile(lat, 99)), "makespan_s": wall,
+               "aggregate_mlups": work / wall / 1e6, "site_steps": sum(p["site_steps"] for p in parts),
+               "peak_members": max(p["peak_members"] for p in parts),
+               "peak_device_bytes": max(p["peak_device_bytes"] for p in parts), "results": results}
     out.pop("results")
+    out["ranks"] = world
     mean_work = float(np.mean([r.sites * r.steps for r in reqs]))
     out["sustainable_rate_per_s"] = round(out["aggregate_mlups"] * 1e6 / mean_work, 3)
     out["sustainable_rate_per_s_full_length"] = round(out["aggregate_mlups"] * 1e6 / (mean_work / step_scale), 4)
@@ -358,7 +384,7 @@ def main():
     torch.cuda.set_device(local)
     device = local
 
-    from dlbc_gb300 import build, init, lbgpu
+    from dlbc_gb300 import build, init, lbgpu, replicas
     build.build()
     p = workload_params(LATTICE)
     fluids, mask = init.init_fields(p)
@@ -378,10 +404,7 @@ def main():
     with ClockSampler(device) as clk:
         ms_step, k2_ms, k1_ms, launches = time_form(p, fluids, mask, head, args.steps, args.warmup, device, torch)
     barrier()
-    t_local = torch.tensor([ms_step], dtype=torch.float64, device=f"cuda:{device}")
-    if dist is not None:
-        dist.all_reduce(t_local, op=dist.ReduceOp.MAX)
-    ms_max = float(t_local.item())
+    ms_max = replicas.max_over_ranks(ms_step, dist, device=f"cuda:{device}")
     value = world * sites / (ms_max * 1e-3) / 1e6
 
     # ---- end to end through the C ABI with pinned host buffers:
@@ -405,10 +428,7 @@ def main():
             g.download(hb)
         barrier()
         e2e_s = time.perf_counter() - t0
-        e2e_t = torch.tensor([e2e_s], dtype=torch.float64, device=f"cuda:{device}")
-        if dist is not None:
-            dist.all_reduce(e2e_t, op=dist.ReduceOp.MAX)
-        e2e_value = world * sites * n_e2e / float(e2e_t.item()) / 1e6
+        e2e_value = world * sites * n_e2e / replicas.max_over_ranks(e2e_s, dist, device=f"cuda:{device}") / 1e6
         e2e = {"value": round(e2e_value, 2), "unit": UNIT,
                "h2d_bytes_per_step": sum(int(x.numel()) * 8 for x in hb) + int(hm.numel()) * 4,
                "d2h_bytes_per_step": sum(int(x.numel()) * 8 for x in hb), "steps": n_e2e,
@@ -430,8 +450,8 @@ def main():
                            "step_roofline_frac": round(bytes_per_site(prec) * sites / (f_ms * 1e-3) / 1e9 / peak,
                                                        4)}
 
-    batched = None if args.no_batched else run_batched(device, torch)
-    served = None if args.no_served else run_served(device)
+    batched = None if args.no_batched else run_batched(device, torch, dist=dist)
+    served = None if args.no_served else run_served(device, dist=dist)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

@@ -140,6 +140,29 @@ def test_download_roundtrip_and_halo():
         assert np.array_equal(back[c], fl[c])
 
 
+@pytest.mark.parametrize("precision", [lbgpu.FP64, lbgpu.FP32, lbgpu.FP16])
+def test_pinned_host_arrays(precision):
+    """Page-locked host arrays (pinned torch tensors, as the end-to-end
+    benchmark passes) give the same results as pageable numpy arrays, halo
+    images included."""
+    import torch
+    p = droplet_channel((12, 10, 16), radius=3.0, acc=1e-4)
+    fl, m = init.init_fields(p)
+    a = lbgpu.GPULattice(p, precision=precision)
+    a.upload(fl, m)
+    a.step(3)
+    ra = a.download()
+    b = lbgpu.GPULattice(p, precision=precision)
+    pf = [torch.from_numpy(x.copy()).pin_memory() for x in fl]
+    pm = torch.from_numpy(m.copy()).pin_memory()
+    b.upload(pf, pm)
+    b.step(3)
+    out = [torch.empty(x.shape, dtype=torch.float64).pin_memory() for x in fl]
+    b.download(out)
+    for c in range(2):
+        assert np.array_equal(out[c].numpy(), ra[c], equal_nan=True)
+
+
 def test_mass_conservation_and_reduction():
     p = spinodal((32, 24, 16))
     o, g = run_both(p, 100)
