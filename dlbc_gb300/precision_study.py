@@ -37,8 +37,8 @@ def spinodal_params(n: int, perturb: float) -> params.LBParams:
     return params.LBParams.from_dict(params.parse_lines(lines), "d3q19")
 
 
-def run_form(p, precision, steps, checkpoints, seed, device=0):
-    g = lbgpu.GPULattice(p, precision=precision, device=device)
+def run_form(p, precision, steps, checkpoints, seed, device=0, rho0=(0.0, 0.0)):
+    g = lbgpu.GPULattice(p, precision=precision, device=device, rho0=rho0)
     g.init_device(seed)
     mass0, _ = g.reduce()
     out = {}
@@ -71,6 +71,9 @@ def main():
     ap.add_argument("--perturb", type=float, default=0.02)
     ap.add_argument("--seed", type=int, default=11)
     ap.add_argument("--checkpoints", default="500,1000,2000,5000")
+    ap.add_argument("--fp16-origin", type=float, action="append", default=[],
+                    help="also run the FP16 form with offsets from this density instead of the mean "
+                         "(a tiny value such as 1e-12 stores plain scaled f_q / w_q)")
     args = ap.parse_args()
     cps = sorted({int(c) for c in args.checkpoints.split(",") if int(c) <= args.steps} | {args.steps})
     p = spinodal_params(args.n, args.perturb)
@@ -80,8 +83,10 @@ def main():
                           f"{args.steps} steps, BDist2, g 3.6",
               "fp64": {"time_s": round(t64, 2), "mlups": round(sites * args.steps / t64 / 1e6, 1),
                        "mass_drift": {cp: ref[cp][2] for cp in cps}}}
-    for name, prec in (("fp32", lbgpu.FP32), ("fp16", lbgpu.FP16)):
-        res, t = run_form(p, prec, args.steps, cps, args.seed)
+    forms = [("fp32", lbgpu.FP32, (0.0, 0.0)), ("fp16", lbgpu.FP16, (0.0, 0.0))]
+    forms += [(f"fp16 origin {v:g}", lbgpu.FP16, (v, v)) for v in args.fp16_origin]
+    for name, prec, rho0 in forms:
+        res, t = run_form(p, prec, args.steps, cps, args.seed, rho0=rho0)
         errs = {}
         for cp in cps:
             (d, v, drift), (d64, v64, _) = res[cp], ref[cp]
