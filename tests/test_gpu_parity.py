@@ -276,6 +276,60 @@ def test_staged_half_kernel_matches_unstaged(case):
         assert np.array_equal(fa[c], fb[c], equal_nan=True)
 
 
+def _run_env(p, steps, precision, env, record_force=True):
+    import os
+    old = {k: os.environ.get(k) for k in env}
+    os.environ.update(env)
+    try:
+        fl, m = init.init_fields(p)
+        g = lbgpu.GPULattice(p, precision=precision)
+        g.upload(fl, m)
+        if record_force:
+            g.set_record_force(True)
+        g.step(steps)
+        return g.population(), g.force()
+    finally:
+        for k, v in old.items():
+            if v is None:
+                del os.environ[k]
+            else:
+                os.environ[k] = v
+
+
+@pytest.mark.parametrize("precision", [lbgpu.FP32, lbgpu.FP16])
+@pytest.mark.parametrize("case", ["spinodal", "walls"])
+def test_cluster_kernel_matches_single_cta_kernel(precision, case):
+    """The 2 x 2 cluster variant of the fused step reads half of each tile's
+    ring from its neighbours' shared memory instead of gathering it: the same
+    values, so bit-identical populations and forces (periodic wrap of the
+    cluster's outer ring, walls and the wall force included)."""
+    import subprocess
+    import sys
+    if case == "spinodal":
+        p = spinodal((20, 32, 64), perturb=0.03)
+    else:
+        p = droplet_channel((18, 48, 128), radius=6.0, acc=1e-3, gwc=(0.25, -0.15))
+    # LBGPU_CLUSTER is read once per process: run the cluster form in a child
+    code = (
+        "import sys, numpy as np; sys.path[:0] = ['tests', '.']\n"
+        "from test_gpu_parity import _run_env, spinodal, droplet_channel, lbgpu\n"
+        f"p = spinodal((20, 32, 64), perturb=0.03) if {case!r} == 'spinodal' else "
+        "droplet_channel((18, 48, 128), radius=6.0, acc=1e-3, gwc=(0.25, -0.15))\n"
+        f"pop, fo = _run_env(p, 21, {precision}, {{}})\n"
+        "np.savez(sys.argv[1], *pop, *fo)\n")
+    import tempfile
+    with tempfile.TemporaryDirectory() as d:
+        out = f"{d}/cluster.npz"
+        env = dict(__import__("os").environ, LBGPU_CLUSTER="1")
+        subprocess.run([sys.executable, "-c", code, out], check=True, env=env)
+        z = np.load(out)
+        single = [z[f"arr_{i}"] for i in range(4)]
+    pop, fo = _run_env(p, 21, precision, {})  # this process: single-CTA tiles
+    for c in range(2):
+        assert np.array_equal(pop[c], single[c])
+        assert np.array_equal(fo[c], single[2 + c], equal_nan=True)
+
+
 def test_launch_count_and_errors():
     p = spinodal((8, 8, 8))
     fl, m = init.init_fields(p)
