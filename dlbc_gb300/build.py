@@ -1,11 +1,15 @@
 """Build the CUDA library ``dlbc_gb300/_build/liblbgpu.so`` for sm_103a.
 
-Three translation units, compiled in parallel with one ``-gencode``:
+Translation units compiled in parallel with one ``-gencode``:
 
-* ``lb_step_f64.cu`` and ``lb_api.cu`` with ``-fmad=false`` (the FP64 form
-  and the double-precision moments must round every product and sum as the
-  reference does);
-* ``lb_step_lp.cu`` (FP32 / FP16-storage forms) with contraction allowed.
+* ``lb_step_f64.cu``, ``lb_api.cu`` and ``lb_init.cu`` with ``-fmad=false``
+  (the FP64 form and the double-precision moments must round every product
+  and sum as the reference does);
+* the fused FP32 / FP16-storage step (``lb_fused*.cu``, split by storage
+  type and batching) also with ``-fmad=false``: its fused multiply-adds are
+  explicit, so all its kernel variants give the same bits;
+* the two-kernel FP32 / FP16 step and the rest (``lb_step_lp.cu``,
+  ``lb_batch.cu``, ``lb_noalloc.cu``) with contraction allowed.
 """
 from __future__ import annotations
 
@@ -28,7 +32,12 @@ UNITS = {
     "lb_api.cu": ["-fmad=false"],
     "lb_init.cu": ["-fmad=false"],
     "lb_step_lp.cu": [],
-    "lb_fused.cu": [],
+    # the fused kernels: explicit fmaf only, so that every variant of the
+    # step computes the same bits
+    "lb_fused.cu": ["-fmad=false"],
+    "lb_fused_f32.cu": ["-fmad=false"],
+    "lb_fused_f16.cu": ["-fmad=false"],
+    "lb_fused_batch.cu": ["-fmad=false"],
     "lb_batch.cu": [],
     "lb_noalloc.cu": [],
 }

@@ -434,12 +434,15 @@ int lb_handle_create(const lbgpu_config* cfg, bool lite, double* staging, size_t
   }
   h->f[0] = ptrs[0];
   h->f[1] = ptrs[1];
+  h->fbytes = fbytes;
   h->rho = ptrs[2];
   h->psi = ptrs[3];
   if (h->fused && !lite) {
     e = cudaMalloc(&h->work_counter, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(h->work_counter, 0, sizeof(int));
     if (e != cudaSuccess) {
       cudaGetLastError();
+      if (h->work_counter) cudaFree(h->work_counter);
       h->work_counter = nullptr;  // static scheduling
     } else {
       h->device_bytes += sizeof(int);
@@ -501,7 +504,16 @@ __global__ void k_tile_walls(const uint32_t* __restrict__ nbm, uint8_t* __restri
   out[i] = any != 0;
 }
 
+int lb_sync_solids(lbgpu_handle* h, int cur, cudaStream_t st) {
+  if (!h->mask || !h->fused || h->solids_synced) return LBGPU_OK;
+  cudaError_t e = cudaMemcpyAsync(h->f[1 - cur], h->f[cur], h->fbytes, cudaMemcpyDeviceToDevice, st);
+  if (e != cudaSuccess) return h->cuda_fail(e, "solid-site copy");
+  h->solids_synced = true;
+  return LBGPU_OK;
+}
+
 int lb_update_nbmask(lbgpu_handle* h) {
+  h->solids_synced = false;  // new populations or a new mask
   const bool want = h->mask && (h->fused || h->lite) && h->Q == 19;
   const int tiles_y = (h->ny + 7) / 8, tiles_z = (h->nz + 31) / 32;
   const int64_t nflags = int64_t(h->nx) * tiles_y * tiles_z;
@@ -804,10 +816,11 @@ int lbgpu_step(lbgpu_handle* h, int32_t nsteps) {
     cudaError_t e;
     if (h->cfg.precision == LBGPU_FP64)
       e = lbk::launch_step_f64(h->Q, h->C, b, P, h->stream, &h->launches, evp);
-    else if (h->fused)
+    else if (h->fused) {
+      if (int rc = lb_sync_solids(h, h->cur, h->stream)) return rc;
       e = lbk::launch_fused(h->cfg.precision == LBGPU_FP16, h->C, b, P, h->stream, &h->launches, evp,
                             h->cfg.device, h->staged);
-    else if (h->cfg.precision == LBGPU_FP32)
+    } else if (h->cfg.precision == LBGPU_FP32)
       e = lbk::launch_step_f32(h->Q, h->C, b, P, h->stream, &h->launches, evp);
     else
       e = lbk::launch_step_f16(h->Q, h->C, b, P, h->stream, &h->launches, evp);

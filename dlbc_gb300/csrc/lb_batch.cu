@@ -187,6 +187,14 @@ cudaError_t launch_one(lbgpu_batch* b, int parity) {
 // advance n steps with the current table and shape
 int run_steps(lbgpu_batch* b, int n) {
   if (b->table_n == 0 || n <= 0) return LBGPU_OK;
+  // members with walls whose buffers do not both hold the solid sites yet
+  for (size_t i = 0; i < b->table_ids.size(); ++i) {
+    lbgpu_handle* h = b->sims[b->table_ids[i]];
+    if (h && h->mask && !h->solids_synced) {
+      const int cur = int((b->table_phase[i] + b->steps_since_build) & 1);
+      if (int rc = lb_sync_solids(h, cur, b->stream)) return b->fail(rc, h->err);
+    }
+  }
   cudaError_t e;
   int done = 0;
   // a direct launch first: it makes the parity even for the graph and sets

@@ -1,5 +1,6 @@
-// Launchers of the fused single-pass step (lb_fused.cuh): one lattice, or a
-// batch of lattices in one persistent launch.
+// The fused single-pass step (lb_fused.cuh): parameters, the single-lattice
+// dispatch (kernels in lb_fused_f32.cu / lb_fused_f16.cu) and the opt-in
+// variants (cp.async staging, thread-block clusters).
 #include <cuda_runtime.h>
 
 #include <stdlib.h>
@@ -7,6 +8,7 @@
 #include <mutex>
 
 #include "lb_fused.cuh"
+#include "lb_fused_launch.cuh"
 #include "lb_launch.h"
 #include "lb_staged.cuh"
 
@@ -56,78 +58,6 @@ FusedParams make_fused_params(const StepParams& P, int ty) {
 size_t fused_smem_bytes(int ty) { return ty == 4 ? sizeof(FusedShared<4>) : sizeof(FusedShared<8>); }
 
 namespace {
-
-// per (kernel, device): shared-memory opt-in done and resident CTAs per SM
-struct KernelInfo {
-  std::mutex mu;
-  int per_sm[64] = {0};
-};
-
-template <typename K>
-cudaError_t kernel_setup(K kern, int smem, int threads, int device, KernelInfo& info, int* per_sm) {
-  std::lock_guard<std::mutex> lock(info.mu);
-  if (!info.per_sm[device & 63]) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e != cudaSuccess) return e;
-    int n = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, threads, smem);
-    if (e != cudaSuccess) return e;
-    info.per_sm[device & 63] = n > 0 ? n : 1;
-  }
-  *per_sm = info.per_sm[device & 63];
-  return cudaSuccess;
-}
-
-int sm_count(int device) {
-  static int cache[64] = {0};
-  if (!cache[device & 63]) {
-    int sms = 0;
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    cache[device & 63] = sms > 0 ? sms : 1;
-  }
-  return cache[device & 63];
-}
-
-template <typename T, int C, bool W, int TY>
-cudaError_t go_single(const StepBuffers& b, const FusedParams& F, cudaStream_t st, int device) {
-  static KernelInfo info;
-  auto kern = k_fused<T, C, W, TY>;
-  const int smem = int(sizeof(FusedShared<TY>));
-  int per_sm = 0;
-  cudaError_t e = kernel_setup(kern, smem, TY * kFusedTZ, device, info, &per_sm);
-  if (e != cudaSuccess) return e;
-  int64_t grid = int64_t(per_sm) * sm_count(device);
-  FusedParams G = F;
-  if (G.work_counter) {
-    // runs of 32 planes, halved while there would be fewer than two runs
-    // per CTA (each run gathers two extra planes to warm up)
-    const int64_t tiles = int64_t(G.tiles_y) * G.tiles_z;
-    int rl = 32;
-    while (rl > 4 && tiles * ((G.nx + rl - 1) / rl) < 2 * grid) rl /= 2;
-    G.run_len = rl < G.nx ? rl : G.nx;
-  }
-  if (grid > G.work) grid = G.work;
-  kern<<<unsigned(grid), TY * kFusedTZ, smem, st>>>(static_cast<const T*>(b.f), static_cast<T*>(b.fout), b.nbmask,
-                                                    b.force, G);
-  return cudaGetLastError();
-}
-
-template <typename T, bool W, int TY>
-cudaError_t go_batch(const FusedSim* sims, int nsims, int64_t total, int parity, int ctas_per_sm, cudaStream_t st,
-                     int device, int64_t total_units, int* counters) {
-  static KernelInfo info;
-  auto kern = k_fused_batch<T, 2, W, TY>;
-  const int smem = int(sizeof(FusedShared<TY>));
-  int per_sm = 0;
-  cudaError_t e = kernel_setup(kern, smem, TY * kFusedTZ, device, info, &per_sm);
-  if (e != cudaSuccess) return e;
-  if (ctas_per_sm > 0 && ctas_per_sm < per_sm) per_sm = ctas_per_sm;
-  int64_t grid = int64_t(per_sm) * sm_count(device);
-  if (grid > total) grid = total;
-  if (grid < 1) return cudaSuccess;
-  kern<<<unsigned(grid), TY * kFusedTZ, smem, st>>>(sims, nsims, total, parity, total_units, counters);
-  return cudaGetLastError();
-}
 
 template <int C, bool W>
 cudaError_t go_staged(const StepBuffers& b, const FusedParams& F, cudaStream_t st, int device) {
@@ -215,6 +145,7 @@ cudaError_t launch_fused(bool half_storage, int c, const StepBuffers& b, const S
   }();
   const bool cluster = kCluster && F.work_counter && c == 2 && P.ny % 16 == 0 && P.nz % 64 == 0 &&
                        !(staged && staged_eligible(P, c, half_storage));
+  const bool mom = c == 2 && P.unit_tau && P.eq_form == 2;
   if (cluster) {
     if (half_storage)
       e = w ? go_cluster<__half, 2, true>(b, F, st, device) : go_cluster<__half, 2, false>(b, F, st, device);
@@ -226,33 +157,13 @@ cudaError_t launch_fused(bool half_storage, int c, const StepBuffers& b, const S
     else
       e = w ? go_staged<1, true>(b, F, st, device) : go_staged<1, false>(b, F, st, device);
   } else if (half_storage) {
-    if (c == 2)
-      e = w ? go_single<__half, 2, true, 8>(b, F, st, device) : go_single<__half, 2, false, 8>(b, F, st, device);
-    else
-      e = w ? go_single<__half, 1, true, 8>(b, F, st, device) : go_single<__half, 1, false, 8>(b, F, st, device);
+    e = launch_fused_single_f16(c, w, mom, b, F, st, device);
   } else {
-    if (c == 2)
-      e = w ? go_single<float, 2, true, 8>(b, F, st, device) : go_single<float, 2, false, 8>(b, F, st, device);
-    else
-      e = w ? go_single<float, 1, true, 8>(b, F, st, device) : go_single<float, 1, false, 8>(b, F, st, device);
+    e = launch_fused_single_f32(c, w, mom, b, F, st, device);
   }
   if (ev) cudaEventRecord(ev->ev[2], st);
   *launches += 1;
   return e;
-}
-
-cudaError_t launch_fused_batch(bool half_storage, int ty, bool walls, const FusedSim* sims, int nsims,
-                               int64_t total_work, int parity, int ctas_per_sm, cudaStream_t st, int device,
-                               int64_t total_units, int* counters) {
-#define LB_BATCH(T, W, TYV) \
-  go_batch<T, W, TYV>(sims, nsims, total_work, parity, ctas_per_sm, st, device, total_units, counters)
-  if (half_storage) {
-    if (ty == 4) return walls ? LB_BATCH(__half, true, 4) : LB_BATCH(__half, false, 4);
-    return walls ? LB_BATCH(__half, true, 8) : LB_BATCH(__half, false, 8);
-  }
-  if (ty == 4) return walls ? LB_BATCH(float, true, 4) : LB_BATCH(float, false, 4);
-  return walls ? LB_BATCH(float, true, 8) : LB_BATCH(float, false, 8);
-#undef LB_BATCH
 }
 
 }  // namespace lbk

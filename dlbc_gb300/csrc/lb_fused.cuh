@@ -104,6 +104,11 @@ struct FusedShared {
   float rho[3][2][TY + 2][kFusedRZ];
 };
 
+// shared-memory address of a generic pointer into shared memory
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
 __device__ __forceinline__ int wrap(int v, int n) { return v < 0 ? v + n : (v >= n ? v - n : v); }
 
 // acc += v * c for a lattice velocity c with components in {-1, 0, 1}
@@ -114,6 +119,60 @@ __device__ __forceinline__ void stencil_acc(float (&acc)[3], int cx, int cy, int
   if (cy < 0) acc[1] -= v;
   if (cz > 0) acc[2] += v;
   if (cz < 0) acc[2] -= v;
+}
+
+// Float arithmetic of the fused kernels.  Their translation units are
+// compiled without FMA contraction and every fused multiply-add is written
+// out with fmaf, so the same source expression gives the same bits in every
+// kernel variant (single lattice, batch, populations-free, staged, cluster).
+
+// S = w_axis * sum_axis + w_diag * sum_diag (w = 1/18, 1/36)
+__device__ __forceinline__ float stencil_weigh(float axis, float diag) {
+  return fmaf(1.0f / 18.0f, axis, (1.0f / 36.0f) * diag);
+}
+
+// dv = tau (F / rho + a) + w, or with tau = 1: F / rho + a + w
+__device__ __forceinline__ float shifted_velocity(float Fc, float rden, float acc, float wv, float tau, bool unit) {
+  const float u = fmaf(Fc, rden, acc);
+  return unit ? u + wv : fmaf(tau, u, wv);
+}
+
+// BGK relaxation pop (1 - omega) + omega eq
+__device__ __forceinline__ float relax(float pop, float omo, float omega, float eq) {
+  return fmaf(pop, omo, omega * eq);
+}
+
+// The BDist2 D3Q19 equilibrium (eqdist.d:102-184) in float, the density
+// folded into the pair constants: with u' = 3 dv and cst = 1 - 3/2 dv.dv,
+// a pair +-c with weight w (1/36, twice that on the axes) gets
+// rho w (cst + (c.u')^2 / 2) +- rho w (cst c.u' + (c.u')^3 / 6), the rest
+// population rho/3 cst.  The same mathematical values as the reference's
+// expression, in fewer operations (about 75 instead of 120).
+__device__ __forceinline__ void eq_bdist2_f(const float (&dv)[3], float rho, float (&dist)[19]) {
+  const float ux = 3.0f * dv[0], uy = 3.0f * dv[1], uz = 3.0f * dv[2];
+  const float uu = fmaf(dv[2], uz, fmaf(dv[1], uy, dv[0] * ux));
+  const float cst = fmaf(-0.5f, uu, 1.0f);
+  const float r1 = (rho * (1.0f / 36.0f)) * cst;   // rho aN1 cst
+  const float rh = rho * (1.0f / 72.0f);           // rho aN1 / 2
+  const float r6 = rho * (1.0f / 216.0f);          // rho aN1 / 6
+  const float a1 = 2.0f * r1, ah = 2.0f * rh, a6 = 2.0f * r6;
+  auto pair = [&](float cu, float k1, float kh, float k6, int ip, int im) {
+    const float cu2 = cu * cu;
+    const float even = fmaf(kh, cu2, k1);
+    const float odd = fmaf(k6, cu2, k1) * cu;
+    dist[ip] = even + odd;
+    dist[im] = even - odd;
+  };
+  pair(ux, a1, ah, a6, 1, 2);
+  pair(uy, a1, ah, a6, 3, 4);
+  pair(uz, a1, ah, a6, 5, 6);
+  pair(ux + uy, r1, rh, r6, 7, 14);
+  pair(ux - uy, r1, rh, r6, 13, 8);
+  pair(ux + uz, r1, rh, r6, 11, 18);
+  pair(ux - uz, r1, rh, r6, 12, 17);
+  pair(uy + uz, r1, rh, r6, 9, 16);
+  pair(uy - uz, r1, rh, r6, 15, 10);
+  dist[0] = (rho * (1.0f / 3.0f)) * cst;
 }
 
 // (y, z) offsets of a site and its 8 in-plane neighbours: off[cy+1][cz+1]
@@ -171,7 +230,11 @@ __device__ __forceinline__ float dsmem_ld(const float* local, uint32_t cta) {
   return v;
 }
 
-template <typename T, int C, bool WALLS, int TY, bool CL = false>
+// MOM: every tau is 1 and the equilibrium is BDist2, so the collision needs
+// only the density and momentum of each component, not the populations: the
+// gather keeps the three momentum components per component in the population
+// buffer instead of the 19 populations.
+template <typename T, int C, bool WALLS, int TY, bool CL = false, bool MOM = false>
 __device__ __forceinline__ void fused_body(const FusedParams& P, const T* __restrict__ f, T* __restrict__ fout,
                                            const uint32_t* __restrict__ nbmask, double* __restrict__ force_out,
                                            int64_t w0, int64_t w1, FusedShared<TY>& sh,
@@ -182,7 +245,7 @@ __device__ __forceinline__ void fused_body(const FusedParams& P, const T* __rest
   const uint32_t plane_sz = uint32_t(P.ny) * uint32_t(P.nz);
   const T* const fc[2] = {f, f + size_t(19) * size_t(P.n)};
   T* const fo[2] = {fout, fout + size_t(19) * size_t(P.n)};
-  const bool unit = P.unit_tau != 0;
+  const bool unit = MOM || P.unit_tau != 0;
   const int ntiles = P.tiles_y * P.tiles_z;
   int64_t w = w0;
   while (w < w1) {
@@ -304,8 +367,13 @@ __device__ __forceinline__ void fused_body(const FusedParams& P, const T* __rest
           sh.rho[ps][c][ty + 1][tz + 1] = den;
           sh.psi[ps][c][ty + 1][tz + 1] = P.psi_form ? 1.0f - __expf(-den) : den;
           if (keep >= 0) {
+            if (MOM) {
 #pragma unroll
-            for (int q = 0; q < 19; ++q) sh.pops[keep][c][q][t] = pop[c][q];
+              for (int vd = 0; vd < 3; ++vd) sh.pops[keep][c][vd][t] = moment<19, float>(pop[c], vd);
+            } else {
+#pragma unroll
+              for (int q = 0; q < 19; ++q) sh.pops[keep][c][q][t] = pop[c][q];
+            }
           }
         }
       }
@@ -353,8 +421,9 @@ __device__ __forceinline__ void fused_body(const FusedParams& P, const T* __rest
         constexpr bool W = decltype(wtag)::value;
         const uint32_t s = uint32_t(x) * plane_sz + uint32_t(yz_in.off[1][1]);
         const int c1y = ty + 1, c1z = tz + 1;
-        // branch-free: solid sites compute like fluid ones and store their
-        // own populations (warps straddling a wall run one code path)
+        // branch-free: solid sites compute like fluid ones but store nothing
+        // (both population buffers hold their constant populations; warps
+        // straddling a wall run one code path)
         const bool solid = W && (nbm_cur & 1u);
         float den[C];
 #pragma unroll
@@ -383,7 +452,7 @@ __device__ __forceinline__ void fused_body(const FusedParams& P, const T* __rest
                 stencil_acc(d, cx, cy, cz, v);
             }
 #pragma unroll
-            for (int vd = 0; vd < 3; ++vd) S[c][vd] = (1.0f / 18.0f) * a[vd] + (1.0f / 36.0f) * d[vd];
+            for (int vd = 0; vd < 3; ++vd) S[c][vd] = stencil_weigh(a[vd], d[vd]);
           }
 #pragma unroll
           for (int f1 = 0; f1 < C; ++f1) {
@@ -410,8 +479,7 @@ __device__ __forceinline__ void fused_body(const FusedParams& P, const T* __rest
                     stencil_acc(d, cx, cy, cz, v);
                 }
 #pragma unroll
-                for (int vd = 0; vd < 3; ++vd)
-                  F[f1][vd] -= own[f1] * wc * ((1.0f / 18.0f) * a[vd] + (1.0f / 36.0f) * d[vd]);
+                for (int vd = 0; vd < 3; ++vd) F[f1][vd] -= own[f1] * wc * stencil_weigh(a[vd], d[vd]);
               }
             }
           }
@@ -435,10 +503,15 @@ __device__ __forceinline__ void fused_body(const FusedParams& P, const T* __rest
         // of the last component stay in registers for its collision
         float pop[19];
         float wv[3] = {0.f, 0.f, 0.f};
-        if (P.eq_form == 2) {
+        if (MOM || P.eq_form == 2) {
           float a[3] = {0.f, 0.f, 0.f};
 #pragma unroll
           for (int c = 0; c < C; ++c) {
+            if (MOM) {
+#pragma unroll
+              for (int vd = 0; vd < 3; ++vd) a[vd] += sh.pops[cur][c][vd][t];
+              continue;
+            }
 #pragma unroll
             for (int q = 0; q < 19; ++q) pop[q] = sh.pops[cur][c][q][t];
             if (unit) {
@@ -453,34 +526,31 @@ __device__ __forceinline__ void fused_body(const FusedParams& P, const T* __rest
 #pragma unroll
           for (int vd = 0; vd < 3; ++vd) wv[vd] = a[vd] * rtot;
         }
-        // --- collision; solid sites store their populations unchanged.  With
-        // tau == 1 the new populations are the equilibrium (pop*0 + 1*eq)
+        // --- collision; solid sites store nothing.  With tau == 1 the new
+        // populations are the equilibrium (pop*0 + 1*eq)
 #pragma unroll
         for (int cc = 0; cc < C; ++cc) {
           const int c = C - 1 - cc;  // last component first: its populations are loaded
-          if (!(P.eq_form == 2 && cc == 0)) {
+          if (!MOM && !(P.eq_form == 2 && cc == 0)) {
 #pragma unroll
             for (int q = 0; q < 19; ++q) pop[q] = sh.pops[cur][c][q][t];
           }
           const float rden = __frcp_rn(den[c]);
           float dv[3];
-          if (unit) {
 #pragma unroll
-            for (int vd = 0; vd < 3; ++vd) dv[vd] = fmaf(F[c][vd], rden, P.acc[vd]) + wv[vd];
-          } else {
-#pragma unroll
-            for (int vd = 0; vd < 3; ++vd) dv[vd] = P.tau[c] * fmaf(F[c][vd], rden, P.acc[vd]) + wv[vd];
-          }
+          for (int vd = 0; vd < 3; ++vd) dv[vd] = shifted_velocity(F[c][vd], rden, P.acc[vd], wv[vd], P.tau[c], unit);
           float eq[19];
-          if (P.eq_form == 2)
-            eq_bdist2<19, float>(dv, den[c], eq);
+          if (MOM || P.eq_form == 2)
+            eq_bdist2_f(dv, den[c], eq);
           else
             eq_poly<19, float>(pop, dv, den[c], P.eq_form == 1, eq);
           const float omega = P.omega[c], omo = P.one_minus_omega[c];
+          if (!solid) {
 #pragma unroll
-          for (int q = 0; q < 19; ++q) {
-            const float v = unit ? eq[q] : pop[q] * omo + omega * eq[q];
-            FStore<T>::store(fo[c] + (P.qn[q] + s), solid ? pop[q] : v, c, q, P);
+            for (int q = 0; q < 19; ++q) {
+              const float v = (MOM || unit) ? eq[q] : relax(pop[q], omo, omega, eq[q]);
+              FStore<T>::store(fo[c] + (P.qn[q] + s), v, c, q, P);
+            }
           }
         }
       };
@@ -493,7 +563,7 @@ __device__ __forceinline__ void fused_body(const FusedParams& P, const T* __rest
   }
 }
 
-template <typename T, int C, bool WALLS, int TY>
+template <typename T, int C, bool WALLS, int TY, bool MOM = false>
 __global__ void __launch_bounds__(TY * kFusedTZ, 8 / TY * 2 > 4 ? 4 : 8 / TY * 2)
     k_fused(const T* __restrict__ f, T* __restrict__ fout, const uint32_t* __restrict__ nbmask,
             double* __restrict__ force_out, FusedParams P) {
@@ -502,7 +572,7 @@ __global__ void __launch_bounds__(TY * kFusedTZ, 8 / TY * 2 > 4 ? 4 : 8 / TY * 2
   if (!P.work_counter) {
     const int64_t w0 = P.work * blockIdx.x / gridDim.x;
     const int64_t w1 = P.work * (blockIdx.x + 1) / gridDim.x;
-    fused_body<T, C, WALLS, TY>(P, f, fout, nbmask, force_out, w0, w1, sh);
+    fused_body<T, C, WALLS, TY, false, MOM>(P, f, fout, nbmask, force_out, w0, w1, sh);
     return;
   }
   // dynamic: runs of run_len planes of one tile, taken in tile-major order
@@ -519,7 +589,7 @@ __global__ void __launch_bounds__(TY * kFusedTZ, 8 / TY * 2 > 4 ? 4 : 8 / TY * 2
     const int tile = item / nchunks, ch = item - tile * nchunks;
     const int64_t w0 = int64_t(tile) * P.nx + int64_t(ch) * P.run_len;
     const int64_t w1 = min(w0 + P.run_len, int64_t(tile + 1) * P.nx);
-    fused_body<T, C, WALLS, TY>(P, f, fout, nbmask, force_out, w0, w1, sh);
+    fused_body<T, C, WALLS, TY, false, MOM>(P, f, fout, nbmask, force_out, w0, w1, sh);
   }
 }
 

@@ -1,0 +1,46 @@
+// The batched fused step: many lattices in one persistent launch.
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include "lb_fused.cuh"
+#include "lb_fused_launch.cuh"
+#include "lb_launch.h"
+
+namespace lbk {
+
+namespace {
+
+template <typename T, bool W, int TY>
+cudaError_t go_batch(const FusedSim* sims, int nsims, int64_t total, int parity, int ctas_per_sm, cudaStream_t st,
+                     int device, int64_t total_units, int* counters) {
+  static KernelInfo info;
+  auto kern = k_fused_batch<T, 2, W, TY>;
+  const int smem = int(sizeof(FusedShared<TY>));
+  int per_sm = 0;
+  cudaError_t e = kernel_setup(kern, smem, TY * kFusedTZ, device, info, &per_sm);
+  if (e != cudaSuccess) return e;
+  if (ctas_per_sm > 0 && ctas_per_sm < per_sm) per_sm = ctas_per_sm;
+  int64_t grid = int64_t(per_sm) * sm_count(device);
+  if (grid > total) grid = total;
+  if (grid < 1) return cudaSuccess;
+  kern<<<unsigned(grid), TY * kFusedTZ, smem, st>>>(sims, nsims, total, parity, total_units, counters);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_fused_batch(bool half_storage, int ty, bool walls, const FusedSim* sims, int nsims,
+                               int64_t total_work, int parity, int ctas_per_sm, cudaStream_t st, int device,
+                               int64_t total_units, int* counters) {
+#define LB_BATCH(T, W, TYV) \
+  go_batch<T, W, TYV>(sims, nsims, total_work, parity, ctas_per_sm, st, device, total_units, counters)
+  if (half_storage) {
+    if (ty == 4) return walls ? LB_BATCH(__half, true, 4) : LB_BATCH(__half, false, 4);
+    return walls ? LB_BATCH(__half, true, 8) : LB_BATCH(__half, false, 8);
+  }
+  if (ty == 4) return walls ? LB_BATCH(float, true, 4) : LB_BATCH(float, false, 4);
+  return walls ? LB_BATCH(float, true, 8) : LB_BATCH(float, false, 8);
+#undef LB_BATCH
+}
+
+}  // namespace lbk

@@ -1,0 +1,47 @@
+// The single-lattice fused step with float populations.
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include "lb_fused.cuh"
+#include "lb_fused_launch.cuh"
+#include "lb_launch.h"
+
+namespace lbk {
+
+namespace {
+
+template <typename T, int C, bool W, int TY, bool MOM = false>
+cudaError_t go_single(const StepBuffers& b, const FusedParams& F, cudaStream_t st, int device) {
+  static KernelInfo info;
+  auto kern = k_fused<T, C, W, TY, MOM>;
+  const int smem = int(sizeof(FusedShared<TY>));
+  int per_sm = 0;
+  cudaError_t e = kernel_setup(kern, smem, TY * kFusedTZ, device, info, &per_sm);
+  if (e != cudaSuccess) return e;
+  int64_t grid = int64_t(per_sm) * sm_count(device);
+  FusedParams G = F;
+  if (G.work_counter) {
+    // runs of 32 planes, halved while there would be fewer than two runs
+    // per CTA (each run gathers two extra planes to warm up)
+    const int64_t tiles = int64_t(G.tiles_y) * G.tiles_z;
+    int rl = 32;
+    while (rl > 4 && tiles * ((G.nx + rl - 1) / rl) < 2 * grid) rl /= 2;
+    G.run_len = rl < G.nx ? rl : G.nx;
+  }
+  if (grid > G.work) grid = G.work;
+  kern<<<unsigned(grid), TY * kFusedTZ, smem, st>>>(static_cast<const T*>(b.f), static_cast<T*>(b.fout), b.nbmask,
+                                                    b.force, G);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_fused_single_f32(int c, bool w, bool mom, const StepBuffers& b, const FusedParams& F, cudaStream_t st,
+                   int device) {
+  if (mom)
+    return w ? go_single<float, 2, true, 8, true>(b, F, st, device) : go_single<float, 2, false, 8, true>(b, F, st, device);
+  if (c == 2) return w ? go_single<float, 2, true, 8>(b, F, st, device) : go_single<float, 2, false, 8>(b, F, st, device);
+  return w ? go_single<float, 1, true, 8>(b, F, st, device) : go_single<float, 1, false, 8>(b, F, st, device);
+}
+
+}  // namespace lbk

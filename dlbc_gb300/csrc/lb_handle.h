@@ -24,6 +24,7 @@ struct lbgpu_handle {
   cudaStream_t stream = nullptr;       // where work is queued
   cudaStream_t own_stream = nullptr;   // created with the handle
   void* f[2] = {nullptr, nullptr};
+  size_t fbytes = 0;                // bytes of one population buffer
   int cur = 0;
   uint8_t* mask = nullptr;
   uint32_t* nbmask = nullptr;       // neighbour masks for the fused step (walls only)
@@ -46,8 +47,14 @@ struct lbgpu_handle {
   // FP32/FP16 D3Q19 run the fused single-pass kernel; LBGPU_TWO_KERNEL=1 in
   // the environment at lbgpu_create selects the two-kernel step instead
   bool fused = false;
-  // the FP16 form uses the TMA-staged kernel where the lattice qualifies
+  // LBGPU_STAGED=1: the FP16 form uses the cp.async-staged kernel where the
+  // lattice qualifies
   bool staged = false;
+  // The fused step does not write solid sites, so both population buffers
+  // must hold their (constant) populations: false after an upload, a device
+  // initialisation or a mask change, until lb_sync_solids copies the
+  // current buffer over the other one.
+  bool solids_synced = false;
   // per-kernel event timing (lbgpu_profile)
   bool profiling = false;
   std::vector<lbk::StepEvents> ev_pending, ev_pool;
@@ -78,3 +85,6 @@ int64_t lb_member_bytes(const lbgpu_config* cfg);
 int lb_ensure_moments(lbgpu_handle* h);
 // (re)build or drop the neighbour masks after the mask changed
 int lb_update_nbmask(lbgpu_handle* h);
+// copy buffer cur over the other one when the fused step needs the solid
+// sites in both (see solids_synced)
+int lb_sync_solids(lbgpu_handle* h, int cur, cudaStream_t st);

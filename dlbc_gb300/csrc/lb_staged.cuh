@@ -46,10 +46,6 @@ struct StagedShared {
   float rho[3][2][TY + 2][kFusedRZ];
 };
 
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
 __device__ __forceinline__ void cp_async16(uint32_t dst, const void* src) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
 }
@@ -282,7 +278,7 @@ __global__ void __launch_bounds__(TY * kFusedTZ, 1)
                 stencil_acc(dd, cx, cy, cz, v);
             }
 #pragma unroll
-            for (int vd = 0; vd < 3; ++vd) S[c][vd] = (1.0f / 18.0f) * a[vd] + (1.0f / 36.0f) * dd[vd];
+            for (int vd = 0; vd < 3; ++vd) S[c][vd] = stencil_weigh(a[vd], dd[vd]);
           }
 #pragma unroll
           for (int f1 = 0; f1 < C; ++f1) {
@@ -309,8 +305,7 @@ __global__ void __launch_bounds__(TY * kFusedTZ, 1)
                     stencil_acc(dd, cx, cy, cz, v);
                 }
 #pragma unroll
-                for (int vd = 0; vd < 3; ++vd)
-                  F[f1][vd] -= own[f1] * wc * ((1.0f / 18.0f) * a[vd] + (1.0f / 36.0f) * dd[vd]);
+                for (int vd = 0; vd < 3; ++vd) F[f1][vd] -= own[f1] * wc * stencil_weigh(a[vd], dd[vd]);
               }
             }
           }
@@ -355,23 +350,21 @@ __global__ void __launch_bounds__(TY * kFusedTZ, 1)
             staged_gather_c<WALLS, TY>(sh, bc, fc[c], P, c, ty + 2, tz + kStagedZH, s, nbm_cur, pop);
           const float rden = __frcp_rn(den[c]);
           float dv[3];
-          if (unit) {
 #pragma unroll
-            for (int vd = 0; vd < 3; ++vd) dv[vd] = fmaf(F[c][vd], rden, P.acc[vd]) + wv[vd];
-          } else {
-#pragma unroll
-            for (int vd = 0; vd < 3; ++vd) dv[vd] = P.tau[c] * fmaf(F[c][vd], rden, P.acc[vd]) + wv[vd];
-          }
+          for (int vd = 0; vd < 3; ++vd) dv[vd] = shifted_velocity(F[c][vd], rden, P.acc[vd], wv[vd], P.tau[c], unit);
           float eq[19];
           if (P.eq_form == 2)
-            eq_bdist2<19, float>(dv, den[c], eq);
+            eq_bdist2_f(dv, den[c], eq);
           else
             eq_poly<19, float>(pop, dv, den[c], P.eq_form == 1, eq);
           const float omega = P.omega[c], omo = P.one_minus_omega[c];
+          // solid sites store nothing: both buffers hold their populations
+          if (!solid) {
 #pragma unroll
-          for (int q = 0; q < 19; ++q) {
-            const float v = unit ? eq[q] : pop[q] * omo + omega * eq[q];
-            FStore<__half>::store(fo[c] + (P.qn[q] + s), solid ? pop[q] : v, c, q, P);
+            for (int q = 0; q < 19; ++q) {
+              const float v = unit ? eq[q] : relax(pop[q], omo, omega, eq[q]);
+              FStore<__half>::store(fo[c] + (P.qn[q] + s), v, c, q, P);
+            }
           }
         }
       }
