@@ -157,6 +157,24 @@ __global__ void __launch_bounds__(128) k_density_psi(const T* __restrict__ f, co
   }
 }
 
+// Division by one divisor b for several numerators: in double the integer
+// IEEE division (lbmath::div_rn, the same bits as a / b for far fewer FP64
+// operations), in float the plain division.
+template <typename R>
+struct Divisor;
+template <>
+struct Divisor<double> {
+  lbmath::DivRecip r;
+  __device__ __forceinline__ explicit Divisor(double b) : r(lbmath::div_recip(b)) {}
+  __device__ __forceinline__ double div(double a) const { return lbmath::div_rn(a, r); }
+};
+template <>
+struct Divisor<float> {
+  float b;
+  __device__ __forceinline__ explicit Divisor(float b_) : b(b_) {}
+  __device__ __forceinline__ float div(float a) const { return a / b; }
+};
+
 // ---------------------------------------------------------------------------
 // kernel 2: force + collision, writes the new populations
 // ---------------------------------------------------------------------------
@@ -287,18 +305,20 @@ __global__ void __launch_bounds__(128) k_collide(const T* __restrict__ f, T* __r
     }
     R tot = den[0];
     if (C > 1) tot = tot + den[1];
+    const Divisor<R> by_tot(tot);
 #pragma unroll
-    for (int vd = 0; vd < D; ++vd) wv[vd] = wv[vd] / tot;
+    for (int vd = 0; vd < D; ++vd) wv[vd] = by_tot.div(wv[vd]);
   }
 
   // --- collision (collision.d:198-218)
 #pragma unroll
   for (int c = 0; c < C; ++c) {
     const R tau = R(P.tau[c]);
+    const Divisor<R> by_den(den[c]);
     R dv[3];
 #pragma unroll
     for (int vd = 0; vd < D; ++vd) {
-      const R a = R(P.acc[vd]) + F[c][vd] / den[c];
+      const R a = R(P.acc[vd]) + by_den.div(F[c][vd]);
       dv[vd] = unit ? a : tau * a;
       if (P.eq_form == 2) dv[vd] = dv[vd] + wv[vd];
     }

@@ -179,4 +179,130 @@ LB_HD double lb_exp(double x) {
   return (y * pow2i(M + 600)) * pow2i(-600);
 }
 
+// ---------------------------------------------------------------------------
+// IEEE double division a / b (round to nearest even) in integer arithmetic.
+//
+// GB300 executes FP64 at a small fraction of its integer rate, and a
+// hardware-sequence division costs about 14 FP64 operations.  The FP64
+// timestep divides 9 times per site (F/rho per component, the weighted
+// velocity by the total density), so it uses this instead for operands in
+// the common range; IEEE division is exactly specified, so the result is
+// the same bits as a / b (tested against the hardware division).
+//
+// For b = mb 2^(eb-1075) with mb in (2^52, 2^53), DivRecip holds
+// v ~ 2^116 / mb within a few units: a correctly rounded float reciprocal
+// of mb's top 24 bits (relative error < 2^-22) refined by two Newton steps
+// v += v (2^116 - mb v) / 2^116 in 64/128-bit integer arithmetic.  For
+// a = ma 2^(ea-1075) (ma scaled so that ma/mb is in [1, 2)),
+// q = floor(ma 2^53 / mb) is floor(ma v / 2^63) or one more, fixed with the
+// exact remainder ma 2^53 - q mb; q's 54 bits are the mantissa, the
+// rounding bit and (with the remainder) the sticky bit.  Operands or
+// results outside the normal range, and b a power of two, take a / b.
+// ---------------------------------------------------------------------------
+LB_HD uint64_t umulhi64(uint64_t a, uint64_t b) {
+#if defined(__CUDA_ARCH__)
+  return __umul64hi(a, b);
+#else
+  return (uint64_t)(((unsigned __int128)a * b) >> 64);
+#endif
+}
+
+LB_HD float frcp_rn(float x) {
+#if defined(__CUDA_ARCH__)
+  return __frcp_rn(x);
+#else
+  return 1.0f / x;  // correctly rounded, as __frcp_rn
+#endif
+}
+
+struct DivRecip {
+  double b;      // the divisor
+  uint64_t mb;   // its 53-bit significand
+  uint64_t v;    // ~2^116 / mb
+  int eb;        // its biased exponent
+  uint64_t sb;   // its sign bit (bit 63)
+  bool ok;       // normal, finite, not a power of two
+};
+
+// one Newton step for v ~ 2^116 / m; e = 2^116 - m v is taken >> sh
+// (|e| < 2^(62 + sh)) and the correction v e / 2^116 as
+// umulhi(v, |e| >> sh) >> (52 - sh)
+LB_HD uint64_t recip_step(uint64_t m, uint64_t v, int sh) {
+  const uint64_t pl = m * v, ph = umulhi64(m, v);  // m v < 2^117
+  // e = 2^116 - (ph:pl) as a signed 128-bit value (hi:lo)
+  const uint64_t lo = 0 - pl;
+  const uint64_t hi = (uint64_t(1) << 52) - ph - (pl != 0 ? 1 : 0);
+  const bool neg = (int64_t)hi < 0;
+  // |e| (128-bit) >> sh, fits in 63 bits
+  uint64_t ahi = hi, alo = lo;
+  if (neg) {
+    alo = 0 - lo;
+    ahi = ~hi + (lo == 0 ? 1 : 0);
+  }
+  const uint64_t es = (ahi << (64 - sh)) | (alo >> sh);
+  const uint64_t corr = umulhi64(v, es) >> (52 - sh);
+  return neg ? v - corr : v + corr;
+}
+
+LB_HD DivRecip div_recip(double b) {
+  DivRecip r;
+  r.b = b;
+  const uint64_t ub = double_to_bits(b);
+  r.eb = int((ub >> 52) & 0x7ff);
+  r.sb = ub & (uint64_t(1) << 63);
+  const uint64_t fb = ub & ((uint64_t(1) << 52) - 1);
+  r.mb = fb | (uint64_t(1) << 52);
+  r.ok = r.eb != 0 && r.eb != 0x7ff && fb != 0;
+  r.v = 0;
+  if (!r.ok) return r;
+  // v0 from the float reciprocal of mb's top 24 bits (mf exact, in (2^23, 2^24))
+  const float mf = (float)(uint32_t)(r.mb >> 29);
+  const float rf = frcp_rn(mf);  // in [2^-24, 2^-23]
+  uint32_t rb;
+  memcpy(&rb, &rf, sizeof rb);
+  const uint64_t sig = (uint64_t)((rb & 0x7fffffu) | 0x800000u);
+  const int e = int((rb >> 23) & 0xff);  // 103 for rf < 2^-23, 104 for rf = 2^-23
+  uint64_t v = e == 103 ? sig << 40 : ~uint64_t(0);  // rf * 2^87
+  v = recip_step(r.mb, v, 32);  // |e| < 2^94 before, relative error ~2^-45 after
+  v = recip_step(r.mb, v, 10);  // |e| < 2^72 before, within a few units after
+  r.v = v;
+  return r;
+}
+
+LB_HD double div_rn(double a, const DivRecip& r) {
+  const uint64_t ua = double_to_bits(a);
+  const int ea = int((ua >> 52) & 0x7ff);
+  const uint64_t sign = (ua & (uint64_t(1) << 63)) ^ r.sb;
+  if (r.ok && (ua << 1) == 0) return bits_to_double(sign);  // +-0 / b
+  if (!r.ok || ea == 0 || ea == 0x7ff) return a / r.b;
+  uint64_t ma = (ua & ((uint64_t(1) << 52) - 1)) | (uint64_t(1) << 52);
+  int e = ea - r.eb + 1023;
+  if (ma < r.mb) {
+    ma <<= 1;
+    e -= 1;
+  }
+  if (e < 1 || e > 2045) return a / r.b;  // subnormal or overflowing quotient
+  // q = floor(ma 2^53 / mb) in [2^53, 2^54), remainder rem in [0, mb)
+  const uint64_t pl = ma * r.v, ph = umulhi64(ma, r.v);
+  uint64_t q = (ph << 1) | (pl >> 63);
+  uint64_t rem = (ma << 53) - q * r.mb;  // exact: the true value is < 2 mb < 2^54
+  if ((int64_t)rem < 0) {
+    q -= 1;
+    rem += r.mb;
+  }
+  if (rem >= r.mb) {
+    q += 1;
+    rem -= r.mb;
+  }
+  uint64_t m53 = q >> 1;
+  if ((q & 1) && (rem != 0 || (m53 & 1))) m53 += 1;
+  if (m53 == (uint64_t(1) << 53)) {
+    m53 >>= 1;
+    e += 1;
+  }
+  return bits_to_double(sign | (uint64_t(e) << 52) | (m53 & ((uint64_t(1) << 52) - 1)));
+}
+
+LB_HD double div_rn(double a, double b) { return div_rn(a, div_recip(b)); }
+
 }  // namespace lbmath

@@ -797,4 +797,8 @@ void or_exp(int mode, int n, const double* x, double* out) {
   for (int i = 0; i < n; ++i) out[i] = mode == 1 ? lbmath::lb_exp(x[i]) : (double)expl((long double)x[i]);
 }
 
+void or_div(int n, const double* a, const double* b, double* out) {
+  for (int i = 0; i < n; ++i) out[i] = lbmath::div_rn(a[i], b[i]);
+}
+
 }  // extern "C"

@@ -100,6 +100,10 @@ double or_uniform_sequence(uint32_t seed, double a, double b, int n, double* out
 /* exp of n arguments with exp_mode `mode` (see or_config) */
 void or_exp(int mode, int n, const double* x, double* out);
 
+/* a[i] / b[i] by the kernels' integer IEEE division (lbmath::div_rn), so
+ * that tests can hold it against the hardware division */
+void or_div(int n, const double* a, const double* b, double* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -79,6 +79,8 @@ def lib() -> C.CDLL:
         L.or_uniform_sequence.restype = C.c_double
         L.or_exp.argtypes = [C.c_int, C.c_int, dp, dp]
         L.or_exp.restype = None
+        L.or_div.argtypes = [C.c_int, dp, dp, dp]
+        L.or_div.restype = None
         _lib = L
     return _lib
 
@@ -89,6 +91,15 @@ def exp(x, mode: int = 1):
     x = np.ascontiguousarray(x, np.float64)
     out = np.empty_like(x)
     lib().or_exp(mode, x.size, x, out)
+    return out
+
+
+def div(a, b):
+    """a / b elementwise by the kernels' integer IEEE division."""
+    a = np.ascontiguousarray(a, np.float64)
+    b = np.ascontiguousarray(b, np.float64)
+    out = np.empty_like(a)
+    lib().or_div(a.size, a, b, out)
     return out
 
 
