@@ -178,8 +178,10 @@ struct Divisor<float> {
 // ---------------------------------------------------------------------------
 // kernel 2: force + collision, writes the new populations
 // ---------------------------------------------------------------------------
+// (at most 168 registers, three 128-thread CTAs per SM: the FP64 form is
+// latency bound at two)
 template <typename T, typename R, int Q, int C, bool WALLS, bool STREAM = true>
-__global__ void __launch_bounds__(128) k_collide(const T* __restrict__ f, T* __restrict__ fout,
+__global__ void __launch_bounds__(128, 3) k_collide(const T* __restrict__ f, T* __restrict__ fout,
                                                  const uint8_t* __restrict__ mask, const R* __restrict__ rho,
                                                  const R* __restrict__ psi, double* __restrict__ force_out,
                                                  StepParams P) {
