@@ -26,6 +26,14 @@
 // result is the correctly rounded exp(x) except for arguments within that
 // distance of a rounding boundary (a few in a million).  The reduction
 // constants keep R's error below that bound for |x| < 2^10.
+//
+// lb_exp itself evaluates the common range 2^-83 <= |x| <= 707 in integer
+// fixed-point arithmetic (no FP64 operations, ~2^-90 relative, then rounded
+// to 64 and to 53 significant bits exactly as the 80-bit evaluation is;
+// see its comment) and uses the FP64 routine above (lb_exp_fp64) elsewhere.
+// Where the two differ (~1.4e-7 of arguments) the integer one is the exact
+// double rounding.  The division helpers at the end (div_rn) serve the same
+// purpose: IEEE division in integer arithmetic.
 #pragma once
 
 #include <stdint.h>
@@ -67,6 +75,16 @@ LB_HD double pow2i(int e) { return bits_to_double((uint64_t)(e + 1023) << 52); }
 #else
 #define LB_EXP_TABLE_QUAL static const
 #endif
+
+// the integer exp's table is read with divergent indices: global memory
+#if defined(__CUDA_ARCH__)
+#define LB_EXP256_QUAL __device__
+#else
+#define LB_EXP256_QUAL static const
+#endif
+}  // namespace lbmath
+#include "lb_exp_table.h"
+namespace lbmath {
 
 // {S_lead, S_trail} for J = 0..31
 LB_EXP_TABLE_QUAL double kExpTable[32][2] = {
@@ -116,7 +134,15 @@ LB_HD double fma_(double a, double b, double c) {
 // exp(x) in IEEE double, identical on host (compiled with
 // -ffp-contract=off) and device (compiled with -fmad=false; the explicit
 // fma_ calls are the only fused operations).
-LB_HD double lb_exp(double x) {
+LB_HD uint64_t umulhi64(uint64_t a, uint64_t b) {
+#if defined(__CUDA_ARCH__)
+  return __umul64hi(a, b);
+#else
+  return (uint64_t)(((unsigned __int128)a * b) >> 64);
+#endif
+}
+
+LB_HD double lb_exp_fp64(double x) {
   const double kInvL = 0x1.71547652b82fep+5;   // 32/ln2
   const double kL1 = 0x1.62e42ff000000p-6;     // ln2/32, leading 32 bits
   const double kL2 = -0x1.718432a1b0e26p-40;   // ln2/32 - kL1
@@ -180,6 +206,113 @@ LB_HD double lb_exp(double x) {
 }
 
 // ---------------------------------------------------------------------------
+// The same exp in integer fixed-point arithmetic, for 2^-83 <= |x| <= 707
+// (every other argument takes lb_exp_fp64).  GB300 executes FP64 at a small
+// fraction of its integer rate and lb_exp_fp64 costs ~60 FP64 operations;
+// this costs none.  It computes exp(x) to ~2^-90 relative and then rounds it
+// exactly as the reference's 80-bit evaluation does: to a 64-bit
+// significand, then to 53 bits (both round to nearest even).
+//   N = round(|x| 256/ln2) (from |x|'s significand times 256/ln2 in 2^-55
+//       units; a rare off-by-one only enlarges |R| negligibly), J = N mod
+//       256, M = floor(N / 256) (signs applied)
+//   R = x - N ln2/256 in units of 2^-136: |x| 2^136 and N ln2/256 2^136
+//       agree above bit 127, so their difference mod 2^128 is R exactly
+//       (up to ln2/256's rounding, < 2^-118)
+//   exp(R) = 1 + R + R^2/2 + R^3 P(R), P(R) = sum_i R^i/(i+3)! (i < 6), in
+//       units of 2^-126: R^2 from R's top 64 bits plus the cross term, P by
+//       Horner in 2^-63 units (|R| <= ln2/512, truncation below 2^-104)
+//   exp(x) = 2^M * (2^(J/256) in 2^-127 units, kExp256) * exp(R)
+// ---------------------------------------------------------------------------
+typedef unsigned __int128 lb_u128;
+typedef __int128 lb_i128;
+
+LB_HD int64_t mulhi64(int64_t a, int64_t b) {
+#if defined(__CUDA_ARCH__)
+  return __mul64hi(a, b);
+#else
+  return (int64_t)(((__int128)a * b) >> 64);
+#endif
+}
+
+LB_HD uint64_t exp_table(int j, int w) {
+#if defined(__CUDA_ARCH__)
+  return __ldg(&kExp256[j][w]);
+#else
+  return kExp256[j][w];
+#endif
+}
+
+LB_HD double lb_exp(double x) {
+  const uint64_t ux = double_to_bits(x);
+  const int ex = int((ux >> 52) & 0x7ff);
+  const uint64_t ax = ux & 0x7fffffffffffffffull;
+  // 2^-83 <= |x| <= 707 (0x408618 = 707's top bits)
+  if (ex < 940 || ax > 0x4086180000000000ull) return lb_exp_fp64(x);
+  const bool neg = (ux >> 63) != 0;
+  const uint64_t mx = (ux & 0xfffffffffffffull) | (uint64_t(1) << 52);
+  // N = round(|x| 256/ln2) = round(mx kExpK 2^(ex - 1130))
+  const int sn = 1130 - 64 - 1 - ex;  // in [33, 125]
+  const uint64_t n2 = sn >= 64 ? 0 : (umulhi64(mx, kExpK) >> sn);
+  const int64_t nabs = (int64_t)((n2 + 1) >> 1);
+  // R = |x| - nabs ln2/256 in 2^-136 units (mod 2^128), then the sign of x
+  const lb_u128 X = (lb_u128)mx << (ex - 939);
+  const lb_u128 L = ((lb_u128)kExpL136Hi << 64) | kExpL136Lo;
+  lb_u128 Ru = X - (lb_u128)(uint64_t)nabs * L;
+  if (neg) Ru = (lb_u128)0 - Ru;
+  const lb_i128 R = (lb_i128)Ru;
+  const int64_t N = neg ? -nabs : nabs;
+  const bool rneg = R < 0;
+  const lb_u128 A = rneg ? (lb_u128)0 - Ru : Ru;  // |R|
+  const uint64_t a1 = (uint64_t)(A >> 64), a0 = (uint64_t)A;
+  const int64_t r1 = (int64_t)(R >> 64);  // R 2^72
+  // E = exp(R) in 2^-126 units
+  lb_i128 E = (lb_i128)1 << 126;
+  E += R >> 10;
+  const lb_u128 a1sq = (lb_u128)a1 * a1;  // R^2 2^144
+  E += (lb_i128)(a1sq >> 19) + (lb_i128)(umulhi64(a1, a0) >> 18);
+  int64_t p = kExpP5;
+  p = kExpP4 + (mulhi64(r1, p) >> 8);
+  p = kExpP3 + (mulhi64(r1, p) >> 8);
+  p = kExpP2 + (mulhi64(r1, p) >> 8);
+  p = kExpP1 + (mulhi64(r1, p) >> 8);
+  p = kExpP0 + (mulhi64(r1, p) >> 8);
+  const uint64_t s2 = (uint64_t)(a1sq >> 62);       // R^2 2^82
+  const uint64_t s3 = umulhi64(s2, a1);             // |R|^3 2^90
+  const uint64_t t = umulhi64(s3, (uint64_t)p);     // |R|^3 P 2^89
+  const lb_i128 T = (lb_i128)((lb_u128)t << 37);
+  E += rneg ? -T : T;
+  // V = E * 2^(J/256) in 2^-125 units (in [0.998, 1.998] 2^125)
+  const int J = int(N & 255);
+  const int64_t M = N >> 8;  // floor
+  const uint64_t th = exp_table(J, 0), tl = exp_table(J, 1);
+  const lb_u128 Eu = (lb_u128)E;
+  const uint64_t eh = (uint64_t)(Eu >> 64), el = (uint64_t)Eu;
+  const lb_u128 V = (lb_u128)eh * th + (lb_u128)umulhi64(eh, tl) + (lb_u128)umulhi64(el, th);
+  // round to a 64-bit significand, then to 53 bits (nearest even both)
+  int Lb = (V >> 125) != 0 ? 125 : 124;  // leading bit
+  uint64_t m64 = (uint64_t)(V >> (Lb - 63));
+  const bool rb = ((V >> (Lb - 64)) & 1) != 0;
+  const bool st = (V & (((lb_u128)1 << (Lb - 64)) - 1)) != 0;
+  if (rb && (st || (m64 & 1))) {
+    m64 += 1;
+    if (m64 == 0) {
+      m64 = uint64_t(1) << 63;
+      Lb += 1;
+    }
+  }
+  uint64_t m53 = m64 >> 11;
+  if (((m64 >> 10) & 1) && ((m64 & 0x3ff) != 0 || (m53 & 1))) {
+    m53 += 1;
+    if (m53 == (uint64_t(1) << 53)) {
+      m53 >>= 1;
+      Lb += 1;
+    }
+  }
+  const int64_t e = int64_t(Lb) + M + 898;
+  return bits_to_double((uint64_t(e) << 52) | (m53 & 0xfffffffffffffull));
+}
+
+// ---------------------------------------------------------------------------
 // IEEE double division a / b (round to nearest even) in integer arithmetic.
 //
 // GB300 executes FP64 at a small fraction of its integer rate, and a
@@ -199,14 +332,6 @@ LB_HD double lb_exp(double x) {
 // rounding bit and (with the remainder) the sticky bit.  Operands or
 // results outside the normal range, and b a power of two, take a / b.
 // ---------------------------------------------------------------------------
-LB_HD uint64_t umulhi64(uint64_t a, uint64_t b) {
-#if defined(__CUDA_ARCH__)
-  return __umul64hi(a, b);
-#else
-  return (uint64_t)(((unsigned __int128)a * b) >> 64);
-#endif
-}
-
 LB_HD float frcp_rn(float x) {
 #if defined(__CUDA_ARCH__)
   return __frcp_rn(x);

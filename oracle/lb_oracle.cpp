@@ -794,7 +794,8 @@ double or_uniform_sequence(uint32_t seed, double a, double b, int n, double* out
 }
 
 void or_exp(int mode, int n, const double* x, double* out) {
-  for (int i = 0; i < n; ++i) out[i] = mode == 1 ? lbmath::lb_exp(x[i]) : (double)expl((long double)x[i]);
+  for (int i = 0; i < n; ++i)
+    out[i] = mode == 1 ? lbmath::lb_exp(x[i]) : mode == 2 ? lbmath::lb_exp_fp64(x[i]) : (double)expl((long double)x[i]);
 }
 
 void or_div(int n, const double* a, const double* b, double* out) {

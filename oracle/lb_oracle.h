@@ -97,7 +97,8 @@ double or_total_mass(const or_lattice* L, int c);               /* fluid sites, 
 /* Mt19937 uniform(a, b) as Phobos std.random (src/dlbc/random.d:55-89) */
 double or_uniform_sequence(uint32_t seed, double a, double b, int n, double* out);
 
-/* exp of n arguments with exp_mode `mode` (see or_config) */
+/* exp of n arguments with exp_mode `mode` (see or_config); mode 2: the
+ * kernels' FP64 fallback routine (lbmath::lb_exp_fp64) */
 void or_exp(int mode, int n, const double* x, double* out);
 
 /* a[i] / b[i] by the kernels' integer IEEE division (lbmath::div_rn), so

@@ -86,8 +86,9 @@ def lib() -> C.CDLL:
 
 
 def exp(x, mode: int = 1):
-    """exp of a float64 array: mode 1 the kernels' lbmath::lb_exp, mode 0
-    long double expl rounded to double."""
+    """exp of a float64 array: mode 1 the kernels' lbmath::lb_exp, mode 2
+    its FP64 routine for arguments outside the integer range
+    (lbmath::lb_exp_fp64), mode 0 long double expl rounded to double."""
     x = np.ascontiguousarray(x, np.float64)
     out = np.empty_like(x)
     lib().or_exp(mode, x.size, x, out)
