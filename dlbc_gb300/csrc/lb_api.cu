@@ -52,9 +52,7 @@ template <>
 __device__ __forceinline__ float to_storage<float>(double v, int, int, const StepParams&, int) {
   return float(v);
 }
-__device__ __forceinline__ float wq(int Q, int q) {
-  return Q == 19 ? lbk::weight<19, float>(q) : lbk::weight<9, float>(q);
-}
+__device__ __forceinline__ float wq(int Q, int q) { return float(lbk::weight_of(Q, q)); }
 template <>
 __device__ __forceinline__ __half to_storage<__half>(double v, int q, int c, const StepParams& P, int Q) {
   return __float2half_rn((float(v) * (1.0f / wq(Q, q)) - P.rho0[c]) * P.inv_scale[c]);
@@ -76,7 +74,7 @@ __device__ __forceinline__ double from_storage<__half>(__half v, int q, int c, c
 }
 
 struct Geo {
-  int nx, ny, nz, nxh, nyh, nzh, hz, Q;
+  int nx, ny, nz, nxh, nyh, nzh, hy, hz, Q;  // hy, hz: halo in y, z (0 where the lattice has no such axis)
   int64_t n;
 };
 
@@ -93,7 +91,7 @@ __global__ void k_upload(const double* __restrict__ stage, T* __restrict__ f, in
   const int xh = xh0 + pl;
   const int x = xh - kHalo;
   if (x < 0 || x >= g.nx) return;
-  const double* src = stage + ((int64_t(pl) * g.nyh + (y + kHalo)) * g.nzh + (z + g.hz)) * g.Q;
+  const double* src = stage + ((int64_t(pl) * g.nyh + (y + g.hy)) * g.nzh + (z + g.hz)) * g.Q;
   const int64_t site = (int64_t(x) * g.ny + y) * g.nz + z;
   T* fc = f + int64_t(c) * g.Q * g.n;
   for (int q = 0; q < g.Q; ++q) fc[int64_t(q) * g.n + site] = to_storage<T>(src[q], q, c, P, g.Q);
@@ -110,7 +108,7 @@ __global__ void k_download(double* __restrict__ stage, const T* __restrict__ f, 
   const int64_t r = i - int64_t(pl) * per_plane;
   const int yh = int(r / g.nzh), zh = int(r - int64_t(yh) * g.nzh);
   const int x = ((xh0 + pl - kHalo) % g.nx + g.nx) % g.nx;
-  const int y = ((yh - kHalo) % g.ny + g.ny) % g.ny;
+  const int y = ((yh - g.hy) % g.ny + g.ny) % g.ny;
   const int z = ((zh - g.hz) % g.nz + g.nz) % g.nz;
   const int64_t site = (int64_t(x) * g.ny + y) * g.nz + z;
   double* dst = stage + i * g.Q;
@@ -128,7 +126,7 @@ __global__ void k_upload_mask(const int32_t* __restrict__ stage_mask, uint8_t* _
   const int y = int(r / g.nz), z = int(r - int64_t(y) * g.nz);
   const int x = xh0 + pl - kHalo;
   if (x < 0 || x >= g.nx) return;
-  const int v = stage_mask[(int64_t(pl) * g.nyh + (y + kHalo)) * g.nzh + (z + g.hz)];
+  const int v = stage_mask[(int64_t(pl) * g.nyh + (y + g.hy)) * g.nzh + (z + g.hz)];
   mask[(int64_t(x) * g.ny + y) * g.nz + z] = v != 0;
   if (v != 0) atomicAdd(nsolid, 1);
 }
@@ -215,6 +213,7 @@ Geo geo_of(const lbgpu_handle* h) {
   g.nxh = h->nxh;
   g.nyh = h->nyh;
   g.nzh = h->nzh;
+  g.hy = h->hy;
   g.hz = h->hz;
   g.Q = h->Q;
   g.n = h->n;
@@ -245,12 +244,15 @@ template <typename T>
 cudaError_t launch_moments(lbgpu_handle* h, double* den, double* vel, double* col) {
   const Geo g = geo_of(h);
   const unsigned blocks = unsigned(ceil_div(g.n, 128));
+  const T* f = static_cast<const T*>(h->f[h->cur]);
   if (h->Q == 19)
-    k_moments<T, 19><<<blocks, 128, 0, h->stream>>>(static_cast<const T*>(h->f[h->cur]), h->mask, h->C, g, h->P,
-                                                     den, vel, col);
+    k_moments<T, 19><<<blocks, 128, 0, h->stream>>>(f, h->mask, h->C, g, h->P, den, vel, col);
+  else if (h->Q == 9)
+    k_moments<T, 9><<<blocks, 128, 0, h->stream>>>(f, h->mask, h->C, g, h->P, den, vel, col);
+  else if (h->Q == 5)
+    k_moments<T, 5><<<blocks, 128, 0, h->stream>>>(f, h->mask, h->C, g, h->P, den, vel, col);
   else
-    k_moments<T, 9><<<blocks, 128, 0, h->stream>>>(static_cast<const T*>(h->f[h->cur]), h->mask, h->C, g, h->P,
-                                                    den, vel, col);
+    k_moments<T, 3><<<blocks, 128, 0, h->stream>>>(f, h->mask, h->C, g, h->P, den, vel, col);
   h->launches++;
   return cudaGetLastError();
 }
@@ -258,12 +260,15 @@ cudaError_t launch_moments(lbgpu_handle* h, double* den, double* vel, double* co
 template <typename T>
 cudaError_t launch_reduce(lbgpu_handle* h, double* partial, int nblocks, int64_t per_block, double* out) {
   const Geo g = geo_of(h);
+  const T* f = static_cast<const T*>(h->f[h->cur]);
   if (h->Q == 19)
-    k_reduce_partial<T, 19><<<nblocks, kRedThreads, 0, h->stream>>>(static_cast<const T*>(h->f[h->cur]), h->mask,
-                                                                     h->C, g, h->P, per_block, partial);
+    k_reduce_partial<T, 19><<<nblocks, kRedThreads, 0, h->stream>>>(f, h->mask, h->C, g, h->P, per_block, partial);
+  else if (h->Q == 9)
+    k_reduce_partial<T, 9><<<nblocks, kRedThreads, 0, h->stream>>>(f, h->mask, h->C, g, h->P, per_block, partial);
+  else if (h->Q == 5)
+    k_reduce_partial<T, 5><<<nblocks, kRedThreads, 0, h->stream>>>(f, h->mask, h->C, g, h->P, per_block, partial);
   else
-    k_reduce_partial<T, 9><<<nblocks, kRedThreads, 0, h->stream>>>(static_cast<const T*>(h->f[h->cur]), h->mask,
-                                                                    h->C, g, h->P, per_block, partial);
+    k_reduce_partial<T, 3><<<nblocks, kRedThreads, 0, h->stream>>>(f, h->mask, h->C, g, h->P, per_block, partial);
   k_reduce_final<<<1, 32, 0, h->stream>>>(partial, nblocks, out);
   h->launches += 2;
   return cudaGetLastError();
@@ -274,8 +279,8 @@ int validate(const lbgpu_config* c, std::string* why) {
     *why = "null config";
     return LBGPU_E_INVALID;
   }
-  if (!((c->d == 3 && c->q == 19) || (c->d == 2 && c->q == 9))) {
-    *why = "only D3Q19 and D2Q9 are supported";
+  if (!((c->d == 3 && c->q == 19) || (c->d == 2 && c->q == 9) || (c->d == 1 && (c->q == 3 || c->q == 5)))) {
+    *why = "only D3Q19, D2Q9, D1Q3 and D1Q5 are supported";
     return LBGPU_E_INVALID;
   }
   if (c->components < 1 || c->components > LBGPU_MAX_COMPONENTS) {
@@ -347,11 +352,12 @@ int lb_handle_create(const lbgpu_config* cfg, bool lite, double* staging, size_t
   h->Q = cfg->q;
   h->C = cfg->components;
   h->nx = cfg->gn[0];
-  h->ny = cfg->gn[1];
+  h->ny = cfg->d >= 2 ? cfg->gn[1] : 1;
   h->nz = cfg->d == 3 ? cfg->gn[2] : 1;
+  h->hy = cfg->d >= 2 ? kHalo : 0;
   h->hz = cfg->d == 3 ? kHalo : 0;
   h->nxh = h->nx + 2 * kHalo;
-  h->nyh = h->ny + 2 * kHalo;
+  h->nyh = h->ny + 2 * h->hy;
   h->nzh = h->nz + 2 * h->hz;
   h->n = int64_t(h->nx) * h->ny * h->nz;
   h->lite = lite;
@@ -628,7 +634,7 @@ int lbgpu_upload(lbgpu_handle* h, const double* const* fluids, const int32_t* ma
       double sum = 0.0;
       int64_t cnt = 0;
       for (int x = kHalo; x < h->nx + kHalo; ++x)
-        for (int y = kHalo; y < h->ny + kHalo; ++y)
+        for (int y = h->hy; y < h->ny + h->hy; ++y)
           for (int z = h->hz; z < h->nz + h->hz; ++z) {
             const double* p = a + ((int64_t(x) * h->nyh + y) * h->nzh + z) * h->Q;
             double s = 0.0;
@@ -638,11 +644,11 @@ int lbgpu_upload(lbgpu_handle* h, const double* const* fluids, const int32_t* ma
           }
       if (rho0 <= 0.0) rho0 = sum / double(cnt);
       for (int x = kHalo; x < h->nx + kHalo; ++x)
-        for (int y = kHalo; y < h->ny + kHalo; ++y)
+        for (int y = h->hy; y < h->ny + h->hy; ++y)
           for (int z = h->hz; z < h->nz + h->hz; ++z) {
             const double* p = a + ((int64_t(x) * h->nyh + y) * h->nzh + z) * h->Q;
             for (int q = 0; q < h->Q; ++q) {
-              const double w = h->Q == 19 ? lbk::weight<19, double>(q) : lbk::weight<9, double>(q);
+              const double w = lbk::weight_of(h->Q, q);
               maxdev = std::max(maxdev, fabs(p[q] / w - rho0));
             }
           }

@@ -20,7 +20,9 @@ namespace lbk {
 
 // ---------------------------------------------------------------------------
 // Connectivities (src/dlbc/lb/connectivity.d:250-418).  Kernels index the
-// lattice as [x][y][z] with z contiguous; D2Q9 runs with a z extent of 1.
+// lattice as [x][y][z] with z contiguous; D2Q9 runs with a z extent of 1,
+// D1Q3 and D1Q5 with y and z extents of 1.  css is the speed of sound
+// squared (generateSpeedOfSound, connectivity.d:213-245).
 // ---------------------------------------------------------------------------
 template <int Q>
 struct Conn;
@@ -47,6 +49,7 @@ struct Conn<19> {
   }
   // weight class: 0 rest, 1 axis (1/18), 2 diagonal (1/36)
   __host__ __device__ static constexpr int wclass(int q) { return q == 0 ? 0 : (q < 7 ? 1 : 2); }
+  __host__ __device__ static constexpr double css() { return 1.0 / 3.0; }
 };
 
 template <>
@@ -63,13 +66,50 @@ struct Conn<9> {
     return q == 0 ? 0 : q == 1 ? 2 : q == 2 ? 1 : q == 3 ? 4 : q == 4 ? 3 : q == 5 ? 8 : q == 6 ? 7 : q == 7 ? 6 : 5;
   }
   __host__ __device__ static constexpr int wclass(int q) { return q == 0 ? 0 : (q < 5 ? 1 : 2); }
+  __host__ __device__ static constexpr double css() { return 1.0 / 3.0; }
+};
+
+// D1Q3 (generateD1Q3, connectivity.d:339-345): 0, +1, -1
+template <>
+struct Conn<3> {
+  static constexpr int D = 1;
+  __host__ __device__ static constexpr int cx(int q) { return q == 1 ? 1 : q == 2 ? -1 : 0; }
+  __host__ __device__ static constexpr int cy(int) { return 0; }
+  __host__ __device__ static constexpr int cz(int) { return 0; }
+  __host__ __device__ static constexpr int bounce(int q) { return q == 1 ? 2 : q == 2 ? 1 : 0; }
+  __host__ __device__ static constexpr int wclass(int q) { return q == 0 ? 0 : 1; }
+  __host__ __device__ static constexpr double css() { return 1.0 / 3.0; }
+};
+
+// D1Q5 (generateD1Q5, connectivity.d:347-353): 0, +1, -1, +2, -2
+template <>
+struct Conn<5> {
+  static constexpr int D = 1;
+  __host__ __device__ static constexpr int cx(int q) {
+    return q == 1 ? 1 : q == 2 ? -1 : q == 3 ? 2 : q == 4 ? -2 : 0;
+  }
+  __host__ __device__ static constexpr int cy(int) { return 0; }
+  __host__ __device__ static constexpr int cz(int) { return 0; }
+  __host__ __device__ static constexpr int bounce(int q) {
+    return q == 1 ? 2 : q == 2 ? 1 : q == 3 ? 4 : q == 4 ? 3 : 0;
+  }
+  __host__ __device__ static constexpr int wclass(int q) { return q == 0 ? 0 : (q < 3 ? 1 : 2); }
+  __host__ __device__ static constexpr double css() { return 1.0; }
 };
 
 template <int Q, typename R>
 __host__ __device__ __forceinline__ R weight(int q) {
-  // generateWeights (connectivity.d:253-256, :266-269)
+  // generateWeights (connectivity.d:250-295)
   if (Q == 19) return Conn<19>::wclass(q) == 0 ? R(1.0 / 3.0) : Conn<19>::wclass(q) == 1 ? R(1.0 / 18.0) : R(1.0 / 36.0);
-  return Conn<9>::wclass(q) == 0 ? R(4.0 / 9.0) : Conn<9>::wclass(q) == 1 ? R(1.0 / 9.0) : R(1.0 / 36.0);
+  if (Q == 9) return Conn<9>::wclass(q) == 0 ? R(4.0 / 9.0) : Conn<9>::wclass(q) == 1 ? R(1.0 / 9.0) : R(1.0 / 36.0);
+  if (Q == 3) return q == 0 ? R(4.0 / 6.0) : R(1.0 / 6.0);
+  return q == 0 ? R(6.0 / 12.0) : q < 3 ? R(2.0 / 12.0) : R(1.0 / 12.0);
+}
+
+// weight of population q of connectivity Q (host and device, runtime Q)
+__host__ __device__ __forceinline__ double weight_of(int Q, int q) {
+  return Q == 19 ? weight<19, double>(q) : Q == 9 ? weight<9, double>(q) : Q == 3 ? weight<3, double>(q)
+                                                                                    : weight<5, double>(q);
 }
 
 template <int Q>
@@ -87,8 +127,12 @@ __device__ __forceinline__ R density(const R* a) {
     const R lo = ((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + (a[7] + a[8])));
     const R hi = ((a[9] + a[10]) + (a[11] + (a[12] + a[13]))) + ((a[14] + a[15]) + (a[16] + (a[17] + a[18])));
     return R(0) + (lo + hi);
-  } else {
+  } else if (Q == 9) {
     return R(0) + (((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + (a[7] + a[8]))));
+  } else if (Q == 5) {
+    return R(0) + ((a[0] + a[1]) + (a[2] + (a[3] + a[4])));
+  } else {
+    return R(0) + (a[0] + (a[1] + a[2]));
   }
 }
 
@@ -100,8 +144,10 @@ __device__ __forceinline__ R moment(const R* a, int vd) {
 #pragma unroll
   for (int q = 1; q < Q; ++q) {
     const int c = cvel<Q>(q, vd);
-    if (c > 0) s = s + a[q];
-    if (c < 0) s = s - a[q];
+    if (c == 1) s = s + a[q];
+    if (c == -1) s = s - a[q];
+    if (c == 2) s = s + a[q] * R(2);   // D1Q5: a * c exactly
+    if (c == -2) s = s - a[q] * R(2);
   }
   return s;
 }
@@ -187,7 +233,7 @@ __device__ __forceinline__ void eq_bdist2(const R* dv, R rho0, R* dist) {
 template <int Q, typename R>
 __device__ __forceinline__ void eq_poly(const R* pop, const R* dv, R rho0, bool third, R* dist) {
   constexpr int D = Conn<Q>::D;
-  const R css = R(1.0 / 3.0);
+  const R css = R(Conn<Q>::css());
   const R css2 = R(2.0) * css;
   const R css2p2 = css2 * css;
   const R css6p3 = R(3.0) * css2p2 * css;
@@ -197,7 +243,8 @@ __device__ __forceinline__ void eq_poly(const R* pop, const R* dv, R rho0, bool 
   R v[3];
 #pragma unroll
   for (int vd = 0; vd < D; ++vd) v[vd] = dv[vd] + moment<Q, R>(pop, vd) * recip;
-  R vdotv = v[0] * v[0] + v[1] * v[1];
+  R vdotv = v[0] * v[0];
+  if (D >= 2) vdotv = vdotv + v[1] * v[1];
   if (D == 3) vdotv = vdotv + v[2] * v[2];
   const R k2 = vdotv / css2;
   dist[0] = rho0 * weight<Q, R>(0) * ((R(1.0) + R(0) / css + R(0) * R(0) / css2p2) - k2);
@@ -213,11 +260,13 @@ __device__ __forceinline__ void eq_poly(const R* pop, const R* dv, R rho0, bool 
     for (int vd = 0; vd < D; ++vd) {
       const int c = cvel<Q>(q, vd);
       if (c == 0) continue;
+      // |c| = 1: +-v exactly; D1Q5's |c| = 2: v * c
+      const R vc = (c == 1) ? v[vd] : (c == -1) ? -v[vd] : v[vd] * R(c);
       if (first) {
-        vdc = (c > 0) ? v[vd] : -v[vd];
+        vdc = vc;
         first = false;
       } else {
-        vdc = (c > 0) ? vdc + v[vd] : vdc - v[vd];
+        vdc = vdc + vc;
       }
     }
     // v . c_b = -(v . c_q) exactly

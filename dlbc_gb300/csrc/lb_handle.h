@@ -19,7 +19,8 @@ struct lbgpu_handle {
   int d = 3, Q = 19, C = 2;
   int nx = 1, ny = 1, nz = 1;       // kernel extents (nz = 1 for D2Q9)
   int nxh = 1, nyh = 1, nzh = 1;    // haloed host extents
-  int hz = kHalo;                   // halo in z (0 for D2Q9)
+  int hy = kHalo;                   // halo in y (0 for D1Q3/D1Q5)
+  int hz = kHalo;                   // halo in z (0 for D2Q9, D1Q3, D1Q5)
   int64_t n = 0;
   cudaStream_t stream = nullptr;       // where work is queued
   cudaStream_t own_stream = nullptr;   // created with the handle

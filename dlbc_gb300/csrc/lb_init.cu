@@ -223,7 +223,7 @@ __global__ void k_init_stats(InitDev I, int64_t n, int pass, const double* __res
         acc[c] += r;
       } else {
         for (int q = 0; q < I.Q; ++q) {
-          const double w = I.Q == 19 ? lbk::weight<19, double>(q) : lbk::weight<9, double>(q);
+          const double w = lbk::weight_of(I.Q, q);
           acc[c] = fmax(acc[c], fabs(pop[q] / w - rho0[c]));
         }
       }
@@ -257,7 +257,7 @@ __device__ __forceinline__ float encode<float>(double v, int, int, int, const St
 }
 template <>
 __device__ __forceinline__ __half encode<__half>(double v, int Q, int q, int c, const StepParams& P) {
-  const float w = Q == 19 ? lbk::weight<19, float>(q) : lbk::weight<9, float>(q);
+  const float w = float(lbk::weight_of(Q, q));
   return __float2half_rn((float(v) * (1.0f / w) - P.rho0[c]) * P.inv_scale[c]);
 }
 
@@ -356,7 +356,10 @@ int build_init(const lbgpu_handle* h, const lbgpu_init* ini, InitDev* I, std::st
   }
   // eqDistUnity (eqdist.d:310-315): the weights, except BDist2 on D2Q9
   for (int q = 0; q < h->Q; ++q)
-    I->eqpop[q] = h->Q == 19 ? lbk::weight<19, double>(q) : lbk::weight<9, double>(q);
+    I->eqpop[q] = lbk::weight_of(h->Q, q);
+  // eqDistUnity of BDist2: D1Q3/D1Q5 return the population itself (1, 0, ...)
+  if ((h->Q == 3 || h->Q == 5) && h->cfg.eq_form == LBGPU_EQ_BDIST2)
+    for (int q = 0; q < h->Q; ++q) I->eqpop[q] = q == 0 ? 1.0 : 0.0;
   if (h->Q == 9 && h->cfg.eq_form == LBGPU_EQ_BDIST2) {
     const double aN1 = 1.0 / 24.0;
     I->eqpop[0] = 0.5;

@@ -78,7 +78,8 @@ struct Store<__half, R, Q> {
 // site coordinates and wrapped neighbour coordinates
 struct Site {
   int x, y, z;
-  int xs[3], ys[3], zs[3];  // coordinate - 1, coordinate, coordinate + 1 (periodic)
+  int xs[5];                // x - 2 .. x + 2 (periodic; +-2 only for D1Q5)
+  int ys[3], zs[3];         // coordinate - 1, coordinate, coordinate + 1 (periodic)
 };
 
 __device__ __forceinline__ Site make_site(int64_t s, const StepParams& P) {
@@ -87,9 +88,11 @@ __device__ __forceinline__ Site make_site(int64_t s, const StepParams& P) {
   S.z = int(s - t * P.nz);
   S.x = int(t / P.ny);
   S.y = int(t - int64_t(S.x) * P.ny);
-  S.xs[0] = S.x == 0 ? P.nx - 1 : S.x - 1;
-  S.xs[1] = S.x;
-  S.xs[2] = S.x == P.nx - 1 ? 0 : S.x + 1;
+  S.xs[1] = S.x == 0 ? P.nx - 1 : S.x - 1;
+  S.xs[2] = S.x;
+  S.xs[3] = S.x == P.nx - 1 ? 0 : S.x + 1;
+  S.xs[0] = S.xs[1] == 0 ? P.nx - 1 : S.xs[1] - 1;
+  S.xs[4] = S.xs[3] == P.nx - 1 ? 0 : S.xs[3] + 1;
   S.ys[0] = S.y == 0 ? P.ny - 1 : S.y - 1;
   S.ys[1] = S.y;
   S.ys[2] = S.y == P.ny - 1 ? 0 : S.y + 1;
@@ -102,10 +105,21 @@ __device__ __forceinline__ Site make_site(int64_t s, const StepParams& P) {
 // index of site + sign*c_q
 template <int Q>
 __device__ __forceinline__ int64_t nb_index(const Site& S, int q, int sign, const StepParams& P) {
-  const int ix = S.xs[1 + sign * Conn<Q>::cx(q)];
+  const int ix = S.xs[2 + sign * Conn<Q>::cx(q)];
   const int iy = S.ys[1 + sign * Conn<Q>::cy(q)];
   const int iz = S.zs[1 + sign * Conn<Q>::cz(q)];
   return (int64_t(ix) * P.ny + iy) * P.nz + iz;
+}
+
+// F -= prefactor * c for a velocity component c in {-2, ..., 2}, exactly as
+// the reference's `force[vd] -= prefactor * cv[vq][vd]` (force.d:283, :304)
+template <typename R>
+__device__ __forceinline__ R force_sub(R F, R prefactor, int c) {
+  if (c == 1) return F - prefactor;
+  if (c == -1) return F + prefactor;
+  if (c == 2) return F - prefactor * R(2);
+  if (c == -2) return F + prefactor * R(2);
+  return F;
 }
 
 // Pull-streamed populations of one component at a fluid site.
@@ -239,11 +253,7 @@ __global__ void __launch_bounds__(128, 3) k_collide(const T* __restrict__ f, T* 
           const R psiden2 = (WALLS && __ldg(mask + nb)) ? ps[f2] : __ldg(p2 + nb);
           const R prefactor = (Conn<Q>::wclass(q) == 1 ? wpsi1 : wpsi2) * psiden2 * cc;
 #pragma unroll
-          for (int vd = 0; vd < D; ++vd) {
-            const int cv = cvel<Q>(q, vd);
-            if (cv > 0) F[f1][vd] = F[f1][vd] - prefactor;
-            if (cv < 0) F[f1][vd] = F[f1][vd] + prefactor;
-          }
+          for (int vd = 0; vd < D; ++vd) F[f1][vd] = force_sub(F[f1][vd], prefactor, cvel<Q>(q, vd));
         }
       }
       if (WALLS) {
@@ -256,11 +266,7 @@ __global__ void __launch_bounds__(128, 3) k_collide(const T* __restrict__ f, T* 
             if (__ldg(mask + nb)) {
               const R prefactor = (Conn<Q>::wclass(q) == 1 ? wpsi1 : wpsi2) * __ldg(r1 + nb) * wc;
 #pragma unroll
-              for (int vd = 0; vd < D; ++vd) {
-                const int cv = cvel<Q>(q, vd);
-                if (cv > 0) F[f1][vd] = F[f1][vd] - prefactor;
-                if (cv < 0) F[f1][vd] = F[f1][vd] + prefactor;
-              }
+              for (int vd = 0; vd < D; ++vd) F[f1][vd] = force_sub(F[f1][vd], prefactor, cvel<Q>(q, vd));
             }
           }
         }
@@ -325,10 +331,18 @@ __global__ void __launch_bounds__(128, 3) k_collide(const T* __restrict__ f, T* 
       if (P.eq_form == 2) dv[vd] = dv[vd] + wv[vd];
     }
     R eq[Q];
-    if (P.eq_form == 2)
-      eq_bdist2<Q, R>(dv, den[c], eq);
-    else
+    if (P.eq_form == 2) {
+      if constexpr (Conn<Q>::D == 1) {
+        // BDist2 is not implemented for 1D and returns the population
+        // itself (eqdist.d:268-272)
+#pragma unroll
+        for (int q = 0; q < Q; ++q) eq[q] = pop[c][q];
+      } else {
+        eq_bdist2<Q, R>(dv, den[c], eq);
+      }
+    } else {
       eq_poly<Q, R>(pop[c], dv, den[c], P.eq_form == 1, eq);
+    }
     const R omega = R(P.omega[c]);
     const R omo = R(P.one_minus_omega[c]);
     T* oc = fout + int64_t(c) * Q * P.n;

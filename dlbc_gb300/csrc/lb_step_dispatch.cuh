@@ -35,6 +35,10 @@ cudaError_t dispatch_step(int q, int c, const StepBuffers& b, const StepParams& 
   LB_CASE(19, 1)
   LB_CASE(9, 2)
   LB_CASE(9, 1)
+  LB_CASE(3, 2)
+  LB_CASE(3, 1)
+  LB_CASE(5, 2)
+  LB_CASE(5, 1)
 #undef LB_CASE
   return cudaErrorInvalidValue;
 }
@@ -73,6 +77,10 @@ cudaError_t dispatch_phase(int phase, int q, int c, const StepBuffers& b, const 
   LB_CASE(19, 1)
   LB_CASE(9, 2)
   LB_CASE(9, 1)
+  LB_CASE(3, 2)
+  LB_CASE(3, 1)
+  LB_CASE(5, 2)
+  LB_CASE(5, 1)
 #undef LB_CASE
   return cudaErrorInvalidValue;
 }

@@ -188,7 +188,8 @@ def read_input(files: Sequence[str], cli: Sequence[str] = ()) -> Tuple[Dict[str,
 def _connectivity(d: Dict[str, Any], dq: Optional[str]) -> str:
     if dq:
         return dq
-    return "d2q9" if len(d.get("lattice.gn", [])) == 2 else "d3q19"
+    # one extent: D1Q3, the reference's tested 1D build (D1Q5 on request)
+    return {1: "d1q3", 2: "d2q9"}.get(len(d.get("lattice.gn", [])), "d3q19")
 
 
 # ---------------------------------------------------------------------------
@@ -468,7 +469,7 @@ def main(argv: Optional[Sequence[str]] = None) -> int:
     ap.add_argument("-r", "--restore", default="", help="restore from checkpoint <name>-<id>-t<time>")
     ap.add_argument("--show-input", action="store_true", help="print the parameter input and exit")
     ap.add_argument("--precision", choices=sorted(lbgpu.PRECISIONS), default="fp64")
-    ap.add_argument("--connectivity", choices=["d3q19", "d2q9"], default=None)
+    ap.add_argument("--connectivity", choices=["d3q19", "d2q9", "d1q3", "d1q5"], default=None)
     ap.add_argument("--device", type=int, default=0)
     ap.add_argument("--device-init", action="store_true",
                     help="compute initial fields on the device (random initialisers then use a "

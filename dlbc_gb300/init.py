@@ -32,13 +32,21 @@ def weights(q: int) -> np.ndarray:
         return np.array([1.0 / 3.0] + [1.0 / 18.0] * 6 + [1.0 / 36.0] * 12)
     if q == 9:
         return np.array([4.0 / 9.0] + [1.0 / 9.0] * 4 + [1.0 / 36.0] * 4)
+    if q == 3:
+        return np.array([4.0 / 6.0, 1.0 / 6.0, 1.0 / 6.0])
+    if q == 5:
+        return np.array([6.0 / 12.0, 2.0 / 12.0, 2.0 / 12.0, 1.0 / 12.0, 1.0 / 12.0])
     raise ValueError(q)
 
 
 def eq_dist_unity(q: int, eq_form: int) -> np.ndarray:
     """eqDistUnity (src/dlbc/lb/eqdist.d:310-315): the equilibrium of unit
     density at rest.  It equals the lattice weights except for BDist2 on
-    D2Q9, whose constants (eqdist.d:186-230) give 1/2, 1/12 and 1/24."""
+    D2Q9, whose constants (eqdist.d:186-230) give 1/2, 1/12 and 1/24, and
+    BDist2 on D1Q3/D1Q5, which returns the population itself
+    (eqdist.d:268-272): (1, 0, ..., 0)."""
+    if eq_form == 2 and q in (3, 5):
+        return np.array([1.0] + [0.0] * (q - 1))
     if eq_form == 2 and q == 9:
         aN1 = 1.0 / 24.0
         return np.array([0.5] + [2.0 * aN1] * 4 + [aN1] * 4)

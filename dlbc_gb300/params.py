@@ -209,6 +209,10 @@ class LBParams:
             dim, q = 3, 19
         elif dq == "d2q9":
             dim, q = 2, 9
+        elif dq == "d1q3":
+            dim, q = 1, 3
+        elif dq == "d1q5":
+            dim, q = 1, 5
         else:
             raise ParameterError(f"unsupported connectivity {dq}")
         p = cls(d=dim, q=q, raw=dict(d))

@@ -59,7 +59,8 @@ extern "C" {
 #define LBGPU_FP16 2        /* half storage of f - w_q*rho0 (scaled) + float arithmetic */
 
 typedef struct lbgpu_config {
-  int32_t d, q;               /* 3/19 (D3Q19) or 2/9 (D2Q9): gconn (src/dlbc/lb/connectivity.d) */
+  int32_t d, q;               /* 3/19 (D3Q19), 2/9 (D2Q9), 1/3 (D1Q3) or 1/5 (D1Q5): gconn
+                               * (src/dlbc/lb/connectivity.d) */
   int32_t gn[3];              /* lattice.gn (gn[2] ignored when d == 2); each >= 2 */
   int32_t components;         /* lb.components, 1 or 2 */
   int32_t shan_chen;          /* lb.force.enableShanChen */
@@ -196,7 +197,8 @@ int lbgpu_kernel_time(lbgpu_handle* h, int32_t which, double* total_ms, int64_t*
  * owns the GPU, or a caller that cannot take cudaMalloc's implicit device
  * synchronisation while its other streams run).  The caller passes device
  * pointers: f_in and f_out hold the populations in the kernels' SoA layout,
- * element [c][q][site] with site = (x*gn[1] + y)*gn[2] + z (D2Q9: x*gn[1] + y),
+ * element [c][q][site] with site = (x*gn[1] + y)*gn[2] + z (D2Q9: x*gn[1] + y;
+ * D1Q3/D1Q5: x),
  * as doubles (LBGPU_FP64) or floats (LBGPU_FP32); mask is uint8 [site]
  * (nonzero = solid) or NULL.  The work is queued on `stream` (a cudaStream_t,
  * NULL for the legacy default stream) and `cfg->device` is used.

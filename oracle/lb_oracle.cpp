@@ -29,6 +29,7 @@ struct Conn {
   int c[19][3];
   double w[19];
   int bounce[19];
+  double css;  // speed of sound squared (generateSpeedOfSound, connectivity.d:213-245)
 };
 
 Conn make_conn(int d, int q) {
@@ -56,9 +57,24 @@ Conn make_conn(int d, int q) {
     k.w[0] = 4.0 / 9.0;
     for (int i = 1; i < 5; ++i) k.w[i] = 1.0 / 9.0;
     for (int i = 5; i < 9; ++i) k.w[i] = 1.0 / 36.0;
+  } else if (d == 1 && q == 3) {
+    // generateD1Q3 (connectivity.d:339-345): 0, +1, -1; weights 4/6, 1/6
+    static const int v[3][3] = {{0, 0, 0}, {1, 0, 0}, {-1, 0, 0}};
+    memcpy(k.c, v, sizeof v);
+    k.w[0] = 4.0 / 6.0;
+    k.w[1] = k.w[2] = 1.0 / 6.0;
+  } else if (d == 1 && q == 5) {
+    // generateD1Q5 (connectivity.d:347-353): 0, +1, -1, +2, -2; weights
+    // 6/12, 2/12, 1/12
+    static const int v[5][3] = {{0, 0, 0}, {1, 0, 0}, {-1, 0, 0}, {2, 0, 0}, {-2, 0, 0}};
+    memcpy(k.c, v, sizeof v);
+    k.w[0] = 6.0 / 12.0;
+    k.w[1] = k.w[2] = 2.0 / 12.0;
+    k.w[3] = k.w[4] = 1.0 / 12.0;
   } else {
     k.q = 0;
   }
+  k.css = (d == 1 && q == 5) ? 1.0 : 1.0 / 3.0;
   // generateBounce (connectivity.d:198-212): first j with c_i + c_j == 0
   for (int i = 0; i < k.q; ++i)
     for (int j = 0; j < k.q; ++j)
@@ -133,11 +149,13 @@ template <typename F>
 void for_physical(const or_lattice& L, F&& fn) {
   const long x0 = L.h, x1 = L.n[0] + L.h;
 #pragma omp parallel for schedule(static) if (L.cfg.threads > 1) num_threads(L.cfg.threads > 1 ? L.cfg.threads : 1)
-  for (long x = x0; x < x1; ++x)
-    for (long y = L.h; y < L.n[1] + L.h; ++y) {
+  for (long x = x0; x < x1; ++x) {
+    const long yh = (L.d >= 2) ? L.h : 0;
+    for (long y = yh; y < L.n[1] + yh; ++y) {
       const long zh = (L.d == 3) ? L.h : 0;
       for (long z = zh; z < L.n[2] + zh; ++z) fn(x, y, z, L.idx(x, y, z));
     }
+  }
 }
 
 template <typename F>
@@ -185,14 +203,21 @@ bool is_on_edge(const or_lattice& L, long x, long y, long z) {
   return false;
 }
 
-// advectFieldsKernel (src/dlbc/lb/advection.d:61-89)
+// advectFieldsKernel (src/dlbc/lb/advection.d:61-89).  D1Q5's |c| = 2
+// velocities would pull halo site 1 from outside the haloed array (the
+// reference reads out of bounds there; its D1Q5 test is disabled): for D1Q5
+// only physical sites are advected and the halo is refreshed with their
+// periodic images afterwards, which is what the other connectivities' halo
+// sites hold after advection anyway.
 void advect(or_lattice& L) {
   const int q = L.q;
+  const bool long_vel = L.d == 1 && q == 5;
   for (int f = 0; f < L.C; ++f) {
     const double* src = L.fluids[f].data();
     double* dst = L.advection.data();
     for_all(L, [&](long x, long y, long z, long i) {
       if (is_on_edge(L, x, y, z)) return;
+      if (long_vel && (x < L.h || x >= L.n[0] + L.h)) return;
       double* pop = dst + i * q;
       if (!L.solid(i)) {  // isAdvectable
         for (int vq = 0; vq < q; ++vq) {
@@ -207,6 +232,7 @@ void advect(or_lattice& L) {
       }
     });
     std::swap(L.fluids[f], L.advection);
+    if (long_vel) exchange_field(L, L.fluids[f].data(), q);
   }
 }
 
@@ -319,7 +345,7 @@ void eq_dist(const or_lattice& L, const double* pop, const double* dv, double rh
   const int q = L.q, d = L.d;
   const int form = L.cfg.eq_form;
   if (form == 0 || form == 1) {
-    const double css = 1.0 / 3.0;
+    const double css = L.k.css;
     double pv[3];
     raw_velocity(L, pop, rho0, pv);
     double v[3] = {0, 0, 0};
@@ -396,6 +422,10 @@ void eq_dist(const or_lattice& L, const double* pop, const double* dv, double rh
 #undef OR_PAIR
     dist[0] = aN0 * cst;
     for (int vq = 0; vq < q; ++vq) dist[vq] *= rho0;
+  } else {
+    // D1Q3 / D1Q5: BDist2 is not implemented and returns the population
+    // itself (eqdist.d:268-272)
+    for (int vq = 0; vq < q; ++vq) dist[vq] = pop[vq];
   }
 }
 
@@ -444,7 +474,8 @@ extern "C" {
 
 or_lattice* or_create(const or_config* cfg) {
   if (!cfg) return nullptr;
-  if (!((cfg->d == 3 && cfg->q == 19) || (cfg->d == 2 && cfg->q == 9))) return nullptr;
+  if (!((cfg->d == 3 && cfg->q == 19) || (cfg->d == 2 && cfg->q == 9) || (cfg->d == 1 && (cfg->q == 3 || cfg->q == 5))))
+    return nullptr;
   if (cfg->components < 1 || cfg->components > OR_MAXC) return nullptr;
   or_lattice* L = new or_lattice;
   L->cfg = *cfg;
@@ -689,7 +720,7 @@ int or_init_lattice(or_lattice* Lp, const or_init* ini) {
       for (long y = 0; y < nl[1]; ++y)
         for (long z = 0; z < nl[2]; ++z) {
           const long lx = x + h, ly = (d >= 2) ? y + h : y, lz = (d == 3) ? z + h : z;
-          const long gx = x + cc[0] * nl[0] + h, gy = y + cc[1] * nl[1] + h;
+          const long gx = x + cc[0] * nl[0] + h, gy = (d >= 2) ? y + cc[1] * nl[1] + h : y;
           const long gz = (d == 3) ? z + cc[2] * nl[2] + h : z;
           const long gi = L.idx(gx, gy, gz), li = lidx(lx, ly, lz);
           L.mask[gi] = lmask[li];
@@ -727,9 +758,9 @@ void or_run(or_lattice* L, int nsteps) {
 
 static void phys_copy(const or_lattice* L, const double* src, int len, double* out) {
   long o = 0;
-  const long zh = (L->d == 3) ? L->h : 0;
+  const long zh = (L->d == 3) ? L->h : 0, yh = (L->d >= 2) ? L->h : 0;
   for (long x = L->h; x < L->n[0] + L->h; ++x)
-    for (long y = L->h; y < L->n[1] + L->h; ++y)
+    for (long y = yh; y < L->n[1] + yh; ++y)
       for (long z = zh; z < L->n[2] + zh; ++z) {
         memcpy(out + o * len, src + L->idx(x, y, z) * len, sizeof(double) * len);
         ++o;
@@ -768,18 +799,18 @@ void or_force(const or_lattice* L, int c, double* out) { phys_copy(L, L->force[c
 
 void or_mask_phys(const or_lattice* L, int32_t* out) {
   long o = 0;
-  const long zh = (L->d == 3) ? L->h : 0;
+  const long zh = (L->d == 3) ? L->h : 0, yh = (L->d >= 2) ? L->h : 0;
   for (long x = L->h; x < L->n[0] + L->h; ++x)
-    for (long y = L->h; y < L->n[1] + L->h; ++y)
+    for (long y = yh; y < L->n[1] + yh; ++y)
       for (long z = zh; z < L->n[2] + zh; ++z) out[o++] = L->mask[L->idx(x, y, z)];
 }
 
 double or_total_mass(const or_lattice* L, int c) {
   // localTotalMass (density.d:136-147): fluid physical sites, sequential
   double mass = 0.0;
-  const long zh = (L->d == 3) ? L->h : 0;
+  const long zh = (L->d == 3) ? L->h : 0, yh = (L->d >= 2) ? L->h : 0;
   for (long x = L->h; x < L->n[0] + L->h; ++x)
-    for (long y = L->h; y < L->n[1] + L->h; ++y)
+    for (long y = yh; y < L->n[1] + yh; ++y)
       for (long z = zh; z < L->n[2] + zh; ++z) {
         const long i = L->idx(x, y, z);
         if (!L->solid(i)) mass += L->density_of(&L->fluids[c][i * L->q]);

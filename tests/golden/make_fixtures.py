@@ -3,7 +3,7 @@
 
 Run from the repository root with the reference checkout available:
 
-    python tests/golden/make_fixtures.py /root/reference
+    python tests/golden/make_fixtures.py /root/reference [case ...]
 
 For every case it stores, in ``tests/golden/<case>.npz``:
 
@@ -40,6 +40,8 @@ CASES = [
      "reference-data/*-t%08d.h5", {0: 0.0, 1000: 0.0}),
     ("laplace-quasi-1d-d2q9", "lb/laplace-quasi-1d", "laplace-quasi-1d-d2q9.in", "d2q9",
      "reference-data/d2q9/*-t%08d.h5", {0: 0.0, 1000: 1e-15}),
+    ("laplace-quasi-1d-d1q3", "lb/laplace-quasi-1d", "laplace-quasi-1d-d1q3.in", "d1q3",
+     "reference-data/d1q3/*-t%08d.h5", {0: 0.0, 1000: 1e-15}),
     # restored from the t = 0 checkpoint, 5 steps; the test compares without a tolerance
     ("checkpoint-3d", "technical/checkpoint-3d", "checkpoint-3d.in.source", "d3q19",
      "reference-data/*-t%08d.h5", {0: 0.0, 5: 0.0}),
@@ -97,9 +99,11 @@ def store(out: dict, key: str, a: np.ndarray, full: bool):
         out[key + "/data"] = a[[nx // 4, nx // 2]]
 
 
-def main(ref: str):
+def main(ref: str, only=()):
     tests = os.path.join(ref, "tests", "runnable", "tests")
     for name, tdir, inp, dq, pattern, tsteps in CASES:
+        if only and name not in only:
+            continue
         root = os.path.join(tests, tdir)
         out = {"input": np.array(open(os.path.join(root, inp)).read()), "dq": np.array(dq)}
         keys = []
@@ -112,7 +116,7 @@ def main(ref: str):
                 field = base.split("-")[1] if kind not in ("colour", "mask") else ""
                 a = h5.read_field(f)
                 key = f"t{t}/{kind}" + (f"-{field}" if field else "")
-                store(out, key, a, full=(dq == "d2q9"))
+                store(out, key, a, full=(dq != "d3q19"))
                 out[key + "/tol"] = np.array(tol)
                 keys.append(key)
         out["keys"] = np.array(keys)
@@ -129,6 +133,8 @@ def main(ref: str):
         np.savez_compressed(path, **out)
         print(f"{path}: {len(keys)} arrays, {os.path.getsize(path)} bytes")
 
+    if only and "init-2d" not in only:
+        return
     root = os.path.join(tests, "lb", "init-2d")
     out = {}
     names = []
@@ -165,4 +171,5 @@ def main(ref: str):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    # optional further arguments: only these cases (the rest are left as they are)
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference", tuple(sys.argv[2:]))

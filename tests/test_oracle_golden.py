@@ -20,10 +20,12 @@ from oracle import oracle as orc
 # a dmd build; the reference's harness compares poiseuille-2d exactly and the
 # quasi-1d colour to 1e-15, the oracle (IEEE double, no FMA) is within 10 ulp
 # of them after 1000 steps.
-KNOWN_DEVIATIONS = {("poiseuille-2d", 1000): 2.5e-15, ("laplace-quasi-1d-d2q9", 1000): 2.5e-15}
+KNOWN_DEVIATIONS = {("poiseuille-2d", 1000): 2.5e-15, ("laplace-quasi-1d-d2q9", 1000): 2.5e-15,
+                    # x87 expl: 1.0e-15; the kernels' exact double-rounded exp: 1.6e-15
+                    ("laplace-quasi-1d-d1q3", 1000): 2.5e-15}
 
 CASES = ["merging-droplets-3d", "bdist2-sc-3d", "laplace-droplet-3d", "merging-droplets-2d",
-         "bdist2-sc-2d", "poiseuille-2d", "laplace-quasi-1d-d2q9", "checkpoint-3d"]
+         "bdist2-sc-2d", "poiseuille-2d", "laplace-quasi-1d-d2q9", "laplace-quasi-1d-d1q3", "checkpoint-3d"]
 
 # D3Q19 BDist2 Shan-Chen cases whose every golden file (t = 0 to the last
 # dump) the oracle reproduces bit for bit with either exp, including the
