@@ -45,6 +45,11 @@ namespace lbk {
 // Tiles are TY x 32 sites (TY = 4 or 8, a template parameter; 32 = one warp
 // along the contiguous z axis), one thread per site.
 constexpr int kFusedTZ = 32;
+// CTAs per SM of the populations-free single-lattice kernel (28 KB of shared
+// memory each): three at up to 85 registers with walls, four at 64 without
+// (measured best on GB300; the wall code spills at 64)
+template <bool WALLS>
+constexpr int mom_ctas() { return WALLS ? 3 : 4; }
 constexpr int kFusedRZ = kFusedTZ + 2;   // tile + one-site ring
 
 // float copies of the step parameters (no double arithmetic in the kernel)
@@ -99,9 +104,11 @@ struct FStore<__half> {
   }
 };
 
-template <int TY>
+// NP = 19: the tile's populations; NP = 3: its momentum per component (the
+// populations-free collision), which leaves room for more CTAs per SM
+template <int TY, int NP = 19>
 struct FusedShared {
-  float pops[2][2][19][TY * kFusedTZ];  // [buffer][c][q][site in tile]
+  float pops[2][2][NP][TY * kFusedTZ];  // [buffer][c][q][site in tile]
   float psi[3][2][TY + 2][kFusedRZ];    // [plane slot][c][y+1][z+1]
   float rho[3][2][TY + 2][kFusedRZ];
 };
@@ -239,7 +246,7 @@ __device__ __forceinline__ float dsmem_ld(const float* local, uint32_t cta) {
 template <typename T, int C, bool WALLS, int TY, bool CL = false, bool MOM = false>
 __device__ __forceinline__ void fused_body(const FusedParams& P, const T* __restrict__ f, T* __restrict__ fout,
                                            const uint32_t* __restrict__ nbmask, double* __restrict__ force_out,
-                                           int64_t w0, int64_t w1, FusedShared<TY>& sh,
+                                           int64_t w0, int64_t w1, FusedShared<TY, MOM ? 3 : 19>& sh,
                                            int crank = 0) {
   constexpr int kFusedTY = TY;
   const int t = threadIdx.x;
@@ -565,12 +572,14 @@ __device__ __forceinline__ void fused_body(const FusedParams& P, const T* __rest
   }
 }
 
+// (the populations-free variant needs 28 KB of shared memory instead of 94,
+// which leaves L1 room for the ring re-reads and allows 3-4 CTAs per SM)
 template <typename T, int C, bool WALLS, int TY, bool MOM = false>
-__global__ void __launch_bounds__(TY * kFusedTZ, 8 / TY * 2 > 4 ? 4 : 8 / TY * 2)
+__global__ void __launch_bounds__(TY * kFusedTZ, MOM ? (8 / TY) * mom_ctas<WALLS>() : (8 / TY * 2 > 4 ? 4 : 8 / TY * 2))
     k_fused(const T* __restrict__ f, T* __restrict__ fout, const uint32_t* __restrict__ nbmask,
             double* __restrict__ force_out, FusedParams P) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  FusedShared<TY>& sh = *reinterpret_cast<FusedShared<TY>*>(smem_raw);
+  FusedShared<TY, MOM ? 3 : 19>& sh = *reinterpret_cast<FusedShared<TY, MOM ? 3 : 19>*>(smem_raw);
   if (!P.work_counter) {
     const int64_t w0 = P.work * blockIdx.x / gridDim.x;
     const int64_t w1 = P.work * (blockIdx.x + 1) / gridDim.x;
@@ -721,7 +730,13 @@ __global__ void __launch_bounds__(TY * kFusedTZ, 8 / TY * 2 > 4 ? 4 : 8 / TY * 2
     T* fout = const_cast<T*>(static_cast<const T*>(sims[i].f[1 - par]));
     const long long r0 = s_w[0], r1 = s_w[1];
     __syncthreads();
-    fused_body<T, C, WALLS, TY>(Ps, fin, fout, sims[i].nbmask, sims[i].force_out, r0 - wb, r1 - wb, sh);
+    // tau = 1 BDist2 members take the populations-free collision (the same
+    // bits as the general body, with fewer instructions)
+    if (C == 2 && Ps.unit_tau && Ps.eq_form == 2)
+      fused_body<T, C, WALLS, TY, false, true>(Ps, fin, fout, sims[i].nbmask, sims[i].force_out, r0 - wb, r1 - wb,
+                                               *reinterpret_cast<FusedShared<TY, 3>*>(smem_raw));
+    else
+      fused_body<T, C, WALLS, TY>(Ps, fin, fout, sims[i].nbmask, sims[i].force_out, r0 - wb, r1 - wb, sh);
     w = r1;
   }
 }
