@@ -306,3 +306,40 @@ def test_post_advection_hook_sees_streamed_populations(tmp_path, monkeypatch):
         for q in range(19):
             want = np.roll(before[..., q], shift=tuple(cv[q]), axis=(0, 1, 2))
             assert np.array_equal(after[..., q], want), (c, q)
+
+
+# ---------------------------------------------------------------------------
+# a one-dimensional reference input through the driver
+# ---------------------------------------------------------------------------
+
+def _run_quasi_1d(tmp_path, monkeypatch, lattice_cls):
+    """The reference's laplace-quasi-1d D1Q3 input run by the driver for its
+    1000 steps: the density and colour dumps at t = 0 and t = 1000 under the
+    reference's names, within the reference's accuracy of its goldens (the
+    t = 1000 allowance as in the oracle's golden tests)."""
+    z, p = load_case("laplace-quasi-1d-d1q3")
+    inp = tmp_path / "laplace-quasi-1d-d1q3.in"
+    inp.write_text(str(z["input"]))
+    monkeypatch.chdir(tmp_path)
+    sim = driver.Simulation([str(inp)], sim_id="20261204T000000", lattice_cls=lattice_cls)
+    sim.setup()
+    sim.run()
+    sim.close()
+    checked = 0
+    for t in (0, 1000):
+        for key, kind in golden_arrays(z, t):
+            stem = "colour-red-blue" if kind == "colour" else kind
+            f = tmp_path / "output" / "d1q3" / f"{stem}-laplace-d1q3-gcc3.6-20261204T000000-t{t:08d}.h5"
+            tol = 0.0 if t == 0 else 2.5e-15
+            assert compare(z, key, h5.read_field(str(f)), tol), key
+            checked += 1
+    assert checked == 6
+
+
+def test_quasi_1d_d1q3_case_cpu(tmp_path, monkeypatch):
+    _run_quasi_1d(tmp_path, monkeypatch, OracleLattice)
+
+
+@pytest.mark.gpu
+def test_quasi_1d_d1q3_case_gpu(tmp_path, monkeypatch):
+    _run_quasi_1d(tmp_path, monkeypatch, lbgpu.GPULattice)
