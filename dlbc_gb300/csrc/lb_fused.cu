@@ -55,7 +55,6 @@ FusedParams make_fused_params(const StepParams& P, int ty) {
   return F;
 }
 
-size_t fused_smem_bytes(int ty) { return ty == 4 ? sizeof(FusedShared<4>) : sizeof(FusedShared<8>); }
 
 namespace {
 

@@ -53,7 +53,7 @@ namespace lbk {
 
 // Fused single-pass D3Q19 step (lb_fused.cuh) for the float-arithmetic
 // forms.  `half_storage` selects half offsets instead of float storage;
-// `staged` lets the half form use the TMA-staged kernel (lb_staged.cuh)
+// `staged` lets the half form use the cp.async-staged kernel (lb_staged.cuh)
 // where the lattice qualifies (staged_eligible).
 cudaError_t launch_fused(bool half_storage, int c, const StepBuffers& b, const StepParams& P, cudaStream_t stream,
                          int64_t* launches, const StepEvents* ev, int device, bool staged);
@@ -68,7 +68,6 @@ struct FusedSim;
 
 // float parameters of the fused kernel for tiles of height ty (4 or 8)
 FusedParams make_fused_params(const StepParams& P, int ty);
-size_t fused_smem_bytes(int ty);
 
 // One timestep of every simulation in `sims` (device array, two-component,
 // D3Q19) in one persistent launch.  ctas_per_sm <= 0: as many as fit.

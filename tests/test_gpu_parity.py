@@ -282,7 +282,7 @@ def _run_half(p, steps, staged, record_force=False):
 
 @pytest.mark.parametrize("case", ["spinodal", "walls", "wall-force", "small-y", "nz8", "nz40", "one-component"])
 def test_staged_half_kernel_matches_unstaged(case):
-    """The TMA-staged FP16 kernel does the unstaged fused kernel's per-site
+    """The cp.async-staged FP16 kernel does the unstaged fused kernel's per-site
     arithmetic on the same values: bit-identical populations and forces,
     including periodic wrap of the staged rows (nz = 8, 40), partial tiles
     and bounce-back next to walls."""
