@@ -221,23 +221,37 @@ Geo geo_of(const lbgpu_handle* h) {
 }
 
 template <typename T>
-cudaError_t launch_upload(lbgpu_handle* h, int c, int xh0, int np) {
+cudaError_t launch_upload(lbgpu_handle* h, const double* stage, int c, int xh0, int np) {
   const Geo g = geo_of(h);
   const int64_t work = int64_t(g.ny) * g.nz * np;
-  k_upload<T><<<unsigned(ceil_div(work, 256)), 256, 0, h->stream>>>(h->staging, static_cast<T*>(h->f[h->cur]), c,
-                                                                     xh0, np, g, h->P);
+  k_upload<T><<<unsigned(ceil_div(work, 256)), 256, 0, h->stream>>>(stage, static_cast<T*>(h->f[h->cur]), c, xh0,
+                                                                     np, g, h->P);
   h->launches++;
   return cudaGetLastError();
 }
 
 template <typename T>
-cudaError_t launch_download(lbgpu_handle* h, int c, int xh0, int np) {
+cudaError_t launch_download(lbgpu_handle* h, double* stage, int c, int xh0, int np) {
   const Geo g = geo_of(h);
   const int64_t work = int64_t(g.nyh) * g.nzh * np;
   k_download<T><<<unsigned(ceil_div(work, 256)), 256, 0, h->stream>>>(
-      h->staging, static_cast<const T*>(h->f[h->cur]), c, xh0, np, g, h->P);
+      stage, static_cast<const T*>(h->f[h->cur]), c, xh0, np, g, h->P);
   h->launches++;
   return cudaGetLastError();
+}
+
+// the copy stream and its events (created on first use)
+cudaError_t xfer_setup(lbgpu_handle* h) {
+  if (h->copy_stream) return cudaSuccess;
+  cudaError_t e = cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking);
+  for (int i = 0; i < 4 && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&h->xfer_ev[i], cudaEventDisableTiming);
+  return e;
+}
+
+// half `buf` of the staging buffer (256-byte aligned halves)
+double* stage_half(const lbgpu_handle* h, int buf) {
+  const size_t half = (h->staging_bytes / 2) & ~size_t(255);
+  return reinterpret_cast<double*>(reinterpret_cast<char*>(h->staging) + size_t(buf) * half);
 }
 
 template <typename T>
@@ -611,6 +625,12 @@ void lbgpu_destroy(lbgpu_handle* h) {
     for (auto ev : e.ev) cudaEventDestroy(ev);
   for (auto& e : h->ev_pool)
     for (auto ev : e.ev) cudaEventDestroy(ev);
+  if (h->copy_stream) {
+    cudaStreamSynchronize(h->copy_stream);
+    for (auto ev : h->xfer_ev)
+      if (ev) cudaEventDestroy(ev);
+    cudaStreamDestroy(h->copy_stream);
+  }
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
   delete h;
 }
@@ -622,7 +642,6 @@ int lbgpu_upload(lbgpu_handle* h, const double* const* fluids, const int32_t* ma
   cudaSetDevice(h->cfg.device);
   cudaError_t e;
   const size_t plane_vals = size_t(h->nyh) * h->nzh * h->Q;
-  const int planes_per_chunk = int(std::max<size_t>(1, h->staging_bytes / (plane_vals * sizeof(double))));
 
   // FP16 offset storage: rest density and scale per component
   if (h->cfg.precision == LBGPU_FP16) {
@@ -665,21 +684,37 @@ int lbgpu_upload(lbgpu_handle* h, const double* const* fluids, const int32_t* ma
     }
   }
 
+  // chunks of whole haloed x-planes through alternating staging halves: the
+  // copy of one chunk (copy stream) overlaps the transpose of the previous
+  // one (h->stream)
+  e = xfer_setup(h);
+  if (e != cudaSuccess) return h->cuda_fail(e, "transfer stream");
+  const int ppc = int(std::max<size_t>(1, ((h->staging_bytes / 2) & ~size_t(255)) / (plane_vals * sizeof(double))));
+  cudaEventRecord(h->xfer_ev[2], h->stream);  // earlier work on the staging buffer
+  cudaEventRecord(h->xfer_ev[3], h->stream);
+  int k = 0;
   for (int c = 0; c < h->C; ++c) {
-    for (int xh0 = 0; xh0 < h->nxh; xh0 += planes_per_chunk) {
-      const int np = std::min(planes_per_chunk, h->nxh - xh0);
+    for (int xh0 = 0; xh0 < h->nxh; xh0 += ppc) {
+      const int np = std::min(ppc, h->nxh - xh0);
       // only planes that hold physical sites matter
       if (xh0 + np <= kHalo || xh0 >= h->nx + kHalo) continue;
-      e = cudaMemcpyAsync(h->staging, fluids[c] + size_t(xh0) * plane_vals, size_t(np) * plane_vals * sizeof(double),
-                          cudaMemcpyHostToDevice, h->stream);
+      const int buf = k & 1;
+      double* stage = stage_half(h, buf);
+      cudaStreamWaitEvent(h->copy_stream, h->xfer_ev[2 + buf], 0);  // the half's previous transpose is done
+      e = cudaMemcpyAsync(stage, fluids[c] + size_t(xh0) * plane_vals, size_t(np) * plane_vals * sizeof(double),
+                          cudaMemcpyHostToDevice, h->copy_stream);
       if (e != cudaSuccess) return h->cuda_fail(e, "upload copy");
+      cudaEventRecord(h->xfer_ev[buf], h->copy_stream);
+      cudaStreamWaitEvent(h->stream, h->xfer_ev[buf], 0);
       if (h->cfg.precision == LBGPU_FP64)
-        e = launch_upload<double>(h, c, xh0, np);
+        e = launch_upload<double>(h, stage, c, xh0, np);
       else if (h->cfg.precision == LBGPU_FP32)
-        e = launch_upload<float>(h, c, xh0, np);
+        e = launch_upload<float>(h, stage, c, xh0, np);
       else
-        e = launch_upload<__half>(h, c, xh0, np);
+        e = launch_upload<__half>(h, stage, c, xh0, np);
       if (e != cudaSuccess) return h->cuda_fail(e, "upload kernel");
+      cudaEventRecord(h->xfer_ev[2 + buf], h->stream);
+      ++k;
     }
   }
 
@@ -842,25 +877,37 @@ int lbgpu_download(lbgpu_handle* h, double* const* fluids) {
   if (!h->uploaded) return h->fail(LBGPU_E_NOTREADY, "lbgpu_download before lbgpu_upload");
   cudaSetDevice(h->cfg.device);
   const size_t plane_vals = size_t(h->nyh) * h->nzh * h->Q;
-  const int planes_per_chunk = int(std::max<size_t>(1, h->staging_bytes / (plane_vals * sizeof(double))));
-  cudaError_t e;
+  cudaError_t e = xfer_setup(h);
+  if (e != cudaSuccess) return h->cuda_fail(e, "transfer stream");
+  // as the upload, in the other direction: the transpose of one chunk
+  // (h->stream) overlaps the copy of the previous one (copy stream)
+  const int ppc = int(std::max<size_t>(1, ((h->staging_bytes / 2) & ~size_t(255)) / (plane_vals * sizeof(double))));
+  int k = 0;
   for (int c = 0; c < h->C; ++c) {
     if (!fluids[c]) continue;
-    for (int xh0 = 0; xh0 < h->nxh; xh0 += planes_per_chunk) {
-      const int np = std::min(planes_per_chunk, h->nxh - xh0);
+    for (int xh0 = 0; xh0 < h->nxh; xh0 += ppc) {
+      const int np = std::min(ppc, h->nxh - xh0);
+      const int buf = k & 1;
+      double* stage = stage_half(h, buf);
+      if (k >= 2) cudaStreamWaitEvent(h->stream, h->xfer_ev[2 + buf], 0);  // the half's previous copy is done
       if (h->cfg.precision == LBGPU_FP64)
-        e = launch_download<double>(h, c, xh0, np);
+        e = launch_download<double>(h, stage, c, xh0, np);
       else if (h->cfg.precision == LBGPU_FP32)
-        e = launch_download<float>(h, c, xh0, np);
+        e = launch_download<float>(h, stage, c, xh0, np);
       else
-        e = launch_download<__half>(h, c, xh0, np);
+        e = launch_download<__half>(h, stage, c, xh0, np);
       if (e != cudaSuccess) return h->cuda_fail(e, "download kernel");
-      e = cudaMemcpyAsync(fluids[c] + size_t(xh0) * plane_vals, h->staging, size_t(np) * plane_vals * sizeof(double),
-                          cudaMemcpyDeviceToHost, h->stream);
+      cudaEventRecord(h->xfer_ev[buf], h->stream);
+      cudaStreamWaitEvent(h->copy_stream, h->xfer_ev[buf], 0);
+      e = cudaMemcpyAsync(fluids[c] + size_t(xh0) * plane_vals, stage, size_t(np) * plane_vals * sizeof(double),
+                          cudaMemcpyDeviceToHost, h->copy_stream);
       if (e != cudaSuccess) return h->cuda_fail(e, "download copy");
+      cudaEventRecord(h->xfer_ev[2 + buf], h->copy_stream);
+      ++k;
     }
   }
-  e = cudaStreamSynchronize(h->stream);
+  e = cudaStreamSynchronize(h->copy_stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
   if (e != cudaSuccess) return h->cuda_fail(e, "download");
   return LBGPU_OK;
 }

@@ -38,6 +38,11 @@ struct lbgpu_handle {
   int force_valid = 0;
   double* staging = nullptr;
   size_t staging_bytes = 0;
+  // host transfers: copies on copy_stream into alternating halves of the
+  // staging buffer, overlapping the transposes of the other half on stream
+  // (events: [0..1] half filled, [2..3] half free again)
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t xfer_ev[4] = {nullptr, nullptr, nullptr, nullptr};
   bool owns_staging = true;         // false: borrowed from a batch
   bool lite = false;                // batch member: no rho/psi scratch (fused step only)
   double* moments = nullptr;        // device scratch for lbgpu_moments / lbgpu_reduce
