@@ -166,6 +166,51 @@ __device__ __forceinline__ float psi_of<float>(float rho, int psi_form) {
   return psi_form ? 1.0f - expf(-rho) : rho;
 }
 
+// Division by one divisor b for several numerators: in double the integer
+// IEEE division (lbmath::div_rn, the same bits as a / b for far fewer FP64
+// operations), in float the plain division.
+template <typename R>
+struct Divisor;
+template <>
+struct Divisor<double> {
+  lbmath::DivRecip r;
+  __device__ __forceinline__ explicit Divisor(double b) : r(lbmath::div_recip(b)) {}
+  __device__ __forceinline__ double div(double a) const { return lbmath::div_rn(a, r); }
+};
+template <>
+struct Divisor<float> {
+  float b;
+  __device__ __forceinline__ explicit Divisor(float b_) : b(b_) {}
+  __device__ __forceinline__ float div(float a) const { return a / b; }
+};
+
+// 2x and x/2 for the arithmetic type: exact scalings by a power of two, in
+// double as an exponent step on the bits (integer operations; GB300 runs
+// FP64 at a small fraction of its integer rate) where the operand and the
+// result are normal numbers, else the multiplication
+template <typename R>
+__device__ __forceinline__ R twice(R x) {
+  return R(2) * x;
+}
+template <>
+__device__ __forceinline__ double twice<double>(double x) {
+  const uint64_t u = lbmath::double_to_bits(x);
+  const uint64_t e = (u >> 52) & 0x7ff;
+  if (e != 0 && e < 0x7fe) return lbmath::bits_to_double(u + (uint64_t(1) << 52));
+  return 2.0 * x;
+}
+template <typename R>
+__device__ __forceinline__ R halve(R x) {
+  return R(0.5) * x;
+}
+template <>
+__device__ __forceinline__ double halve<double>(double x) {
+  const uint64_t u = lbmath::double_to_bits(x);
+  const uint64_t e = (u >> 52) & 0x7ff;
+  if (e > 1 && e != 0x7ff) return lbmath::bits_to_double(u - (uint64_t(1) << 52));
+  return 0.5 * x;
+}
+
 // ---------------------------------------------------------------------------
 // Equilibria (src/dlbc/lb/eqdist.d:61-278).  `pop` is only read by the
 // SecondOrder/ThirdOrder forms (their velocity is the population's own
@@ -181,7 +226,7 @@ __device__ __forceinline__ void eq_bdist2(const R* dv, R rho0, R* dist) {
     const R holdit = R(1.0) / R(1.0 / 3.0);
     const R tux = dv[0], tuy = dv[1], tuz = dv[2];
     const R tuxt = tux * holdit, tuyt = tuy * holdit, tuzt = tuz * holdit;
-    const R uke = R(0.5) * (tux * tuxt + tuy * tuyt + tuz * tuzt);
+    const R uke = halve<R>(tux * tuxt + tuy * tuyt + tuz * tuzt);
     const R cst = R(1.0) - uke;
     const R const1 = aN1 * cst;
 #define LB_PAIR(CD, IP, IM, TWO)                                         \
@@ -190,8 +235,8 @@ __device__ __forceinline__ void eq_bdist2(const R* dv, R rho0, R* dist) {
     const R even = const1 + haN1 * cdotu * cdotu;                        \
     const R odd = const1 * cdotu + aN1_6 * cdotu * cdotu * cdotu;        \
     if (TWO) {                                                           \
-      dist[IP] = R(2.0) * (even + odd);                                  \
-      dist[IM] = R(2.0) * (even - odd);                                  \
+      dist[IP] = twice<R>(even + odd);                                   \
+      dist[IM] = twice<R>(even - odd);                                   \
     } else {                                                             \
       dist[IP] = even + odd;                                             \
       dist[IM] = even - odd;                                             \
@@ -215,7 +260,7 @@ __device__ __forceinline__ void eq_bdist2(const R* dv, R rho0, R* dist) {
     const R holdit = R(1.0) / R(1.0 / 3.0);
     const R tux = dv[0], tuy = dv[1];
     const R tuxt = tux * holdit, tuyt = tuy * holdit;
-    const R uke = R(0.5) * (tux * tuxt + tuy * tuyt);
+    const R uke = halve<R>(tux * tuxt + tuy * tuyt);
     const R cst = R(1.0) - uke;
     const R const1 = aN1 * cst;
     LB_PAIR(tuxt, 1, 2, true)
@@ -237,18 +282,21 @@ __device__ __forceinline__ void eq_poly(const R* pop, const R* dv, R rho0, bool 
   const R css2 = R(2.0) * css;
   const R css2p2 = css2 * css;
   const R css6p3 = R(3.0) * css2p2 * css;
+  // the divisions by these constants, exact (integer arithmetic in double)
+  const Divisor<R> by_css(css), by_css2(css2), by_css2p2(css2p2), by_css6p3(css6p3);
   // rawVelocity(pop, rho0): sum_q pop_q c_q, then `vel[] /= density`, a D
   // array operation that druntime evaluates as a multiplication by 1/density
-  const R recip = R(1.0) / rho0;
+  const R recip = Divisor<R>(rho0).div(R(1.0));
   R v[3];
 #pragma unroll
   for (int vd = 0; vd < D; ++vd) v[vd] = dv[vd] + moment<Q, R>(pop, vd) * recip;
   R vdotv = v[0] * v[0];
   if (D >= 2) vdotv = vdotv + v[1] * v[1];
   if (D == 3) vdotv = vdotv + v[2] * v[2];
-  const R k2 = vdotv / css2;
-  dist[0] = rho0 * weight<Q, R>(0) * ((R(1.0) + R(0) / css + R(0) * R(0) / css2p2) - k2);
-  if (third) dist[0] = rho0 * weight<Q, R>(0) * ((((R(1.0) + R(0) / css + R(0) * R(0) / css2p2) - k2) + R(0)) - R(0));
+  const R k2 = by_css2.div(vdotv);
+  const R z1 = by_css.div(R(0)), z2 = by_css2p2.div(R(0) * R(0));  // v.c_0 = 0
+  dist[0] = rho0 * weight<Q, R>(0) * ((R(1.0) + z1 + z2) - k2);
+  if (third) dist[0] = rho0 * weight<Q, R>(0) * ((((R(1.0) + z1 + z2) - k2) + R(0)) - R(0));
 #pragma unroll
   for (int q = 1; q < Q; ++q) {
     const int b = Conn<Q>::bounce(q);
@@ -270,16 +318,16 @@ __device__ __forceinline__ void eq_poly(const R* pop, const R* dv, R rho0, bool 
       }
     }
     // v . c_b = -(v . c_q) exactly
-    const R A = vdc / css;
+    const R A = by_css.div(vdc);
     const R sq = vdc * vdc;
-    const R B = sq / css2p2;
+    const R B = by_css2p2.div(sq);
     const R w = weight<Q, R>(q);
     if (!third) {
       dist[q] = rho0 * w * (((R(1.0) + A) + B) - k2);
       dist[b] = rho0 * w * (((R(1.0) - A) + B) - k2);
     } else {
-      const R T3 = sq * vdc / css6p3;
-      const R T4 = vdotv * vdc / css2p2;
+      const R T3 = by_css6p3.div(sq * vdc);
+      const R T4 = by_css2p2.div(vdotv * vdc);
       dist[q] = rho0 * w * (((((R(1.0) + A) + B) - k2) + T3) - T4);
       dist[b] = rho0 * w * (((((R(1.0) - A) + B) - k2) - T3) + T4);
     }

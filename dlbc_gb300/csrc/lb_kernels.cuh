@@ -171,24 +171,6 @@ __global__ void __launch_bounds__(128) k_density_psi(const T* __restrict__ f, co
   }
 }
 
-// Division by one divisor b for several numerators: in double the integer
-// IEEE division (lbmath::div_rn, the same bits as a / b for far fewer FP64
-// operations), in float the plain division.
-template <typename R>
-struct Divisor;
-template <>
-struct Divisor<double> {
-  lbmath::DivRecip r;
-  __device__ __forceinline__ explicit Divisor(double b) : r(lbmath::div_recip(b)) {}
-  __device__ __forceinline__ double div(double a) const { return lbmath::div_rn(a, r); }
-};
-template <>
-struct Divisor<float> {
-  float b;
-  __device__ __forceinline__ explicit Divisor(float b_) : b(b_) {}
-  __device__ __forceinline__ float div(float a) const { return a / b; }
-};
-
 // ---------------------------------------------------------------------------
 // kernel 2: force + collision, writes the new populations
 // ---------------------------------------------------------------------------
