@@ -46,10 +46,12 @@ FusedParams make_fused_params(const StepParams& P, int ty) {
   for (int q = 0; q < 19; ++q) {
     F.qn[q] = uint32_t(int64_t(q) * P.n);
     for (int c = 0; c < 2; ++c) {
-      F.wrho[c][q] = weight<19, float>(q) * P.rho0[c];
-      F.wscale[c][q] = weight<19, float>(q) * P.scale[c];
-      F.inv_wscale[c][q] = 1.0f / F.wscale[c][q];
-      F.hoff[c][q] = -F.wrho[c][q] * F.inv_wscale[c][q];
+      // one value per weight class (q = 0, 1..6, 7..18)
+      const int k = Conn<19>::wclass(q);
+      F.wrho[c][k] = weight<19, float>(q) * P.rho0[c];
+      F.wscale[c][k] = weight<19, float>(q) * P.scale[c];
+      F.inv_wscale[c][k] = 1.0f / F.wscale[c][k];
+      F.hoff[c][k] = -F.wrho[c][k] * F.inv_wscale[c][k];
     }
   }
   return F;

@@ -64,10 +64,12 @@ struct FusedParams {
   float gcc[2][2], gwc[2], acc[3];
   float rho0[2], scale[2], inv_scale[2];
   uint32_t qn[19];         // q * n: population q's offset inside a component (19 n < 2^32)
-  float wrho[2][19];       // w_q * rho0_c (half storage: f_q = w_q rho0_c + w_q scale_c h)
-  float wscale[2][19];     // w_q * scale_c
-  float inv_wscale[2][19]; // 1 / (w_q * scale_c)
-  float hoff[2][19];       // -w_q rho0_c / (w_q scale_c): half value = v / (w_q scale_c) + hoff
+  // half storage, per component and weight class k of q (0 rest, 1 axis,
+  // 2 diagonal: these constants depend on q only through w_q):
+  float wrho[2][3];        // w_q * rho0_c (f_q = w_q rho0_c + w_q scale_c h)
+  float wscale[2][3];      // w_q * scale_c
+  float inv_wscale[2][3];  // 1 / (w_q * scale_c)
+  float hoff[2][3];        // -w_q rho0_c / (w_q scale_c): half value = v / (w_q scale_c) + hoff
   // per (x, tile) of TY = 8 tiles: 1 if a site of the tile or of its ring
   // in plane x has a solid neighbour (or is solid); planes without run the
   // wall-free code.  nullptr: every plane of a walled lattice is walled.
@@ -92,15 +94,15 @@ struct FStore<float> {
 template <>
 struct FStore<__half> {
   __device__ static __forceinline__ float load(const __half* p, int c, int q, const FusedParams& P) {
-    return fmaf(P.wscale[c][q], __half2float(__ldg(p)), P.wrho[c][q]);
+    return fmaf(P.wscale[c][Conn<19>::wclass(q)], __half2float(__ldg(p)), P.wrho[c][Conn<19>::wclass(q)]);
   }
   // opposite populations have equal weights (w_b = w_q), so either decodes
   // with q's constants
   __device__ static __forceinline__ float load2(const __half* p, int c, int q, int, bool, const FusedParams& P) {
-    return fmaf(P.wscale[c][q], __half2float(__ldg(p)), P.wrho[c][q]);
+    return fmaf(P.wscale[c][Conn<19>::wclass(q)], __half2float(__ldg(p)), P.wrho[c][Conn<19>::wclass(q)]);
   }
   __device__ static __forceinline__ void store(__half* p, float v, int c, int q, const FusedParams& P) {
-    *p = __float2half_rn(fmaf(v, P.inv_wscale[c][q], P.hoff[c][q]));
+    *p = __float2half_rn(fmaf(v, P.inv_wscale[c][Conn<19>::wclass(q)], P.hoff[c][Conn<19>::wclass(q)]));
   }
 };
 

@@ -68,7 +68,7 @@ __device__ __forceinline__ int wrap_any(int v, int n) {
 }
 
 __device__ __forceinline__ float dec_half(__half h, int c, int q, const FusedParams& P) {
-  return fmaf(P.wscale[c][q], __half2float(h), P.wrho[c][q]);
+  return fmaf(P.wscale[c][Conn<19>::wclass(q)], __half2float(h), P.wrho[c][Conn<19>::wclass(q)]);
 }
 
 // own population `src` of the site at (row, col) in plane d: in the slab
