@@ -631,8 +631,59 @@ void lbgpu_destroy(lbgpu_handle* h) {
       if (ev) cudaEventDestroy(ev);
     cudaStreamDestroy(h->copy_stream);
   }
+  if (h->copy_stream2) {
+    cudaStreamSynchronize(h->copy_stream2);
+    cudaStreamDestroy(h->copy_stream2);
+  }
+  for (auto ev : h->pipe_ev)
+    if (ev) cudaEventDestroy(ev);
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
   delete h;
+}
+
+// mask: int32 haloed -> uint8 physical (through the staging buffer, on
+// h->stream); dropped when nothing is solid
+static int upload_mask(lbgpu_handle* h, const int32_t* mask) {
+  cudaError_t e;
+  if (mask) {
+    if (!h->mask) {
+      e = cudaMalloc(&h->mask, size_t(h->n));
+      if (e != cudaSuccess) return h->cuda_fail(e, "mask allocation");
+      h->device_bytes += h->n;
+    }
+    // the solid-site counter lives in the last 256 bytes of the staging buffer
+    const size_t usable = h->staging_bytes - 256;
+    int* d_count = reinterpret_cast<int*>(reinterpret_cast<char*>(h->staging) + usable);
+    cudaMemsetAsync(d_count, 0, sizeof(int), h->stream);
+    const size_t plane_m = size_t(h->nyh) * h->nzh;
+    const int ppc = int(std::max<size_t>(1, usable / (plane_m * sizeof(int32_t))));
+    for (int xh0 = 0; xh0 < h->nxh; xh0 += ppc) {
+      const int np = std::min(ppc, h->nxh - xh0);
+      if (xh0 + np <= kHalo || xh0 >= h->nx + kHalo) continue;
+      e = cudaMemcpyAsync(h->staging, mask + size_t(xh0) * plane_m, size_t(np) * plane_m * sizeof(int32_t),
+                          cudaMemcpyHostToDevice, h->stream);
+      if (e != cudaSuccess) return h->cuda_fail(e, "mask copy");
+      const Geo g = geo_of(h);
+      const int64_t work = int64_t(g.ny) * g.nz * np;
+      k_upload_mask<<<unsigned(ceil_div(work, 256)), 256, 0, h->stream>>>(
+          reinterpret_cast<const int32_t*>(h->staging), h->mask, xh0, np, g, d_count);
+      h->launches++;
+    }
+    int nsolid = 0;
+    e = cudaMemcpyAsync(&nsolid, d_count, sizeof(int), cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return h->cuda_fail(e, "mask upload");
+    if (nsolid == 0) {
+      cudaFree(h->mask);
+      h->device_bytes -= h->n;
+      h->mask = nullptr;
+    }
+  } else if (h->mask) {
+    cudaFree(h->mask);
+    h->device_bytes -= h->n;
+    h->mask = nullptr;
+  }
+  return LBGPU_OK;
 }
 
 int lbgpu_upload(lbgpu_handle* h, const double* const* fluids, const int32_t* mask) {
@@ -718,45 +769,7 @@ int lbgpu_upload(lbgpu_handle* h, const double* const* fluids, const int32_t* ma
     }
   }
 
-  // mask: int32 haloed -> uint8 physical; dropped when nothing is solid
-  if (mask) {
-    if (!h->mask) {
-      e = cudaMalloc(&h->mask, size_t(h->n));
-      if (e != cudaSuccess) return h->cuda_fail(e, "mask allocation");
-      h->device_bytes += h->n;
-    }
-    // the solid-site counter lives in the last 256 bytes of the staging buffer
-    const size_t usable = h->staging_bytes - 256;
-    int* d_count = reinterpret_cast<int*>(reinterpret_cast<char*>(h->staging) + usable);
-    cudaMemsetAsync(d_count, 0, sizeof(int), h->stream);
-    const size_t plane_m = size_t(h->nyh) * h->nzh;
-    const int ppc = int(std::max<size_t>(1, usable / (plane_m * sizeof(int32_t))));
-    for (int xh0 = 0; xh0 < h->nxh; xh0 += ppc) {
-      const int np = std::min(ppc, h->nxh - xh0);
-      if (xh0 + np <= kHalo || xh0 >= h->nx + kHalo) continue;
-      e = cudaMemcpyAsync(h->staging, mask + size_t(xh0) * plane_m, size_t(np) * plane_m * sizeof(int32_t),
-                          cudaMemcpyHostToDevice, h->stream);
-      if (e != cudaSuccess) return h->cuda_fail(e, "mask copy");
-      const Geo g = geo_of(h);
-      const int64_t work = int64_t(g.ny) * g.nz * np;
-      k_upload_mask<<<unsigned(ceil_div(work, 256)), 256, 0, h->stream>>>(
-          reinterpret_cast<const int32_t*>(h->staging), h->mask, xh0, np, g, d_count);
-      h->launches++;
-    }
-    int nsolid = 0;
-    e = cudaMemcpyAsync(&nsolid, d_count, sizeof(int), cudaMemcpyDeviceToHost, h->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
-    if (e != cudaSuccess) return h->cuda_fail(e, "mask upload");
-    if (nsolid == 0) {
-      cudaFree(h->mask);
-      h->device_bytes -= h->n;
-      h->mask = nullptr;
-    }
-  } else if (h->mask) {
-    cudaFree(h->mask);
-    h->device_bytes -= h->n;
-    h->mask = nullptr;
-  }
+  if (int rc = upload_mask(h, mask)) return rc;
   if (int rc = lb_update_nbmask(h)) return rc;
   e = cudaStreamSynchronize(h->stream);
   if (e != cudaSuccess) return h->cuda_fail(e, "upload");
@@ -909,6 +922,190 @@ int lbgpu_download(lbgpu_handle* h, double* const* fluids) {
   e = cudaStreamSynchronize(h->copy_stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
   if (e != cudaSuccess) return h->cuda_fail(e, "download");
+  return LBGPU_OK;
+}
+
+// --------------------------------------------------------------------------
+// lbgpu_step_host: upload, one timestep and download in one call
+// --------------------------------------------------------------------------
+namespace {
+
+constexpr int kWavePlanes = 8;  // x-planes per chunk of the wavefront
+
+// the largest |c_x| of the connectivity (D1Q5 reaches x +- 2)
+int reach_x(int Q) { return Q == 5 ? 2 : 1; }
+
+cudaError_t wave_setup(lbgpu_handle* h) {
+  cudaError_t e = xfer_setup(h);
+  if (e == cudaSuccess && !h->copy_stream2) e = cudaStreamCreateWithFlags(&h->copy_stream2, cudaStreamNonBlocking);
+  for (int i = 0; i < 9 && e == cudaSuccess; ++i)
+    if (!h->pipe_ev[i]) e = cudaEventCreateWithFlags(&h->pipe_ev[i], cudaEventDisableTiming);
+  return e;
+}
+
+// x-planes per chunk of the wavefront, 0 when the lattice is too small or
+// too wide for it (then the call runs upload, step and download in turn)
+int wave_planes(const lbgpu_handle* h) {
+  const size_t plane_bytes = size_t(h->nyh) * h->nzh * h->Q * sizeof(double);
+  const size_t slot_bytes = (h->staging_bytes / 8) & ~size_t(255);
+  const int k = int(std::min<size_t>(kWavePlanes, slot_bytes / plane_bytes));
+  return (k >= 1 && h->nx >= 2 * k + 4 * reach_x(h->Q)) ? k : 0;
+}
+
+// The FP64 timestep as a wavefront over chunks of K x-planes, so that the
+// input copies, the kernels and the output copies overlap.  Chunk j (physical
+// planes [a, b) of every component): copy_stream copies the whole haloed
+// planes into upload slot j % 2 of the staging buffer; h->stream transposes
+// them into the population buffer, runs k_density_psi on the planes whose
+// x +- R neighbours are now present and k_collide on the planes whose x +- R
+// densities are done, and transposes the finished planes into a download
+// slot; copy_stream2 copies those to the host.  Planes 0 .. 2R-1 need the
+// last planes (periodic wrap) and finish after the last chunk.  The per-site
+// arithmetic is lbgpu_step's, so the result is the same bits.  A plane's
+// input copy completes before its output copy starts, so `out` may alias
+// `in`.  Staging slots: [0, 4) upload (parity, component), [4, 8) download.
+// Events: 0 start, 1-2 upload slot filled, 3-4 upload slot free, 5-6
+// download slot filled, 7-8 download slot free.
+int step_host_wave(lbgpu_handle* h, const double* const* in, double* const* out, int K) {
+  const Geo g = geo_of(h);
+  const size_t plane_vals = size_t(h->nyh) * h->nzh * h->Q;
+  const size_t plane_bytes = plane_vals * sizeof(double);
+  const int64_t plane_sites = int64_t(h->ny) * h->nz;
+  const size_t slot_bytes = (h->staging_bytes / 8) & ~size_t(255);
+  auto slot = [&](int k) {
+    return reinterpret_cast<double*>(reinterpret_cast<char*>(h->staging) + size_t(k) * slot_bytes);
+  };
+  cudaEvent_t* ev = h->pipe_ev;
+  const int R = reach_x(h->Q);
+  const int nx = h->nx;
+  double* fin = static_cast<double*>(h->f[h->cur]);
+  const double* fout = static_cast<const double*>(h->f[1 - h->cur]);
+  lbk::StepBuffers b;
+  b.f = h->f[h->cur];
+  b.fout = h->f[1 - h->cur];
+  b.mask = h->mask;
+  b.rho = h->rho;
+  b.psi = h->psi;
+  b.force = h->force;
+  cudaError_t e;
+
+  // work queued earlier on h->stream (the mask upload, moments that use the
+  // staging buffer) precedes the copies into the staging buffer
+  cudaEventRecord(ev[0], h->stream);
+  cudaStreamWaitEvent(h->copy_stream, ev[0], 0);
+  cudaStreamWaitEvent(h->copy_stream2, ev[0], 0);
+
+  auto part = [&](int which, int x0, int x1) -> cudaError_t {
+    if (x1 <= x0) return cudaSuccess;
+    StepParams P = h->P;
+    P.record_force = h->record_force ? 1 : 0;
+    P.s_begin = int64_t(x0) * plane_sites;
+    P.s_end = int64_t(x1) * plane_sites;
+    return lbk::launch_part_f64(which, h->Q, h->C, b, P, h->stream, &h->launches);
+  };
+  int nd = 0;  // download chunks queued
+  // haloed planes [xh0, xh1), all of them finished
+  auto download = [&](int xh0, int xh1) -> cudaError_t {
+    for (int a = xh0; a < xh1; a += K) {
+      const int np = std::min(K, xh1 - a);
+      const int p = nd & 1;
+      if (nd >= 2) cudaStreamWaitEvent(h->stream, ev[7 + p], 0);  // the slot's previous copies are done
+      const int64_t work = int64_t(g.nyh) * g.nzh * np;
+      for (int c = 0; c < h->C; ++c) {
+        if (!out[c]) continue;
+        k_download<double><<<unsigned(ceil_div(work, 256)), 256, 0, h->stream>>>(slot(4 + 2 * p + c), fout, c, a,
+                                                                                  np, g, h->P);
+        h->launches++;
+      }
+      cudaError_t le = cudaGetLastError();
+      if (le != cudaSuccess) return le;
+      cudaEventRecord(ev[5 + p], h->stream);
+      cudaStreamWaitEvent(h->copy_stream2, ev[5 + p], 0);
+      for (int c = 0; c < h->C; ++c) {
+        if (!out[c]) continue;
+        le = cudaMemcpyAsync(out[c] + size_t(a) * plane_vals, slot(4 + 2 * p + c), size_t(np) * plane_bytes,
+                             cudaMemcpyDeviceToHost, h->copy_stream2);
+        if (le != cudaSuccess) return le;
+      }
+      cudaEventRecord(ev[7 + p], h->copy_stream2);
+      ++nd;
+    }
+    return cudaSuccess;
+  };
+
+  int dn = R, cn = 2 * R;  // k_density_psi done on planes [R, dn), k_collide (and download) on [2R, cn)
+  int j = 0;
+  for (int a = 0; a < nx; a += K, ++j) {
+    const int bnd = std::min(nx, a + K);
+    const int p = j & 1;
+    if (j >= 2) cudaStreamWaitEvent(h->copy_stream, ev[3 + p], 0);  // the slot's previous transposes are done
+    for (int c = 0; c < h->C; ++c) {
+      e = cudaMemcpyAsync(slot(2 * p + c), in[c] + size_t(a + kHalo) * plane_vals, size_t(bnd - a) * plane_bytes,
+                          cudaMemcpyHostToDevice, h->copy_stream);
+      if (e != cudaSuccess) return h->cuda_fail(e, "step_host input copy");
+    }
+    cudaEventRecord(ev[1 + p], h->copy_stream);
+    cudaStreamWaitEvent(h->stream, ev[1 + p], 0);
+    const int64_t work = plane_sites * (bnd - a);
+    for (int c = 0; c < h->C; ++c) {
+      k_upload<double><<<unsigned(ceil_div(work, 256)), 256, 0, h->stream>>>(slot(2 * p + c), fin, c, a + kHalo,
+                                                                            bnd - a, g, h->P);
+      h->launches++;
+    }
+    if ((e = cudaGetLastError()) != cudaSuccess) return h->cuda_fail(e, "step_host input transpose");
+    cudaEventRecord(ev[3 + p], h->stream);
+    const bool last = bnd == nx;
+    const int dnew = last ? nx : bnd - R;
+    if ((e = part(lbk::kPartDensityPsi, dn, dnew)) != cudaSuccess) return h->cuda_fail(e, "step_host density");
+    dn = std::max(dn, dnew);
+    if (last && (e = part(lbk::kPartDensityPsi, 0, R)) != cudaSuccess) return h->cuda_fail(e, "step_host density");
+    const int cnew = last ? nx : dn - R;
+    if ((e = part(lbk::kPartCollide, cn, cnew)) != cudaSuccess) return h->cuda_fail(e, "step_host collide");
+    if (!last) {
+      if (cnew > cn && (e = download(cn + kHalo, cnew + kHalo)) != cudaSuccess)
+        return h->cuda_fail(e, "step_host output");
+      cn = std::max(cn, cnew);
+    } else {
+      if ((e = part(lbk::kPartCollide, 0, 2 * R)) != cudaSuccess) return h->cuda_fail(e, "step_host collide");
+      // physical planes [cn, nx) with the images of planes 0 and 1, then the
+      // images of planes nx-2 and nx-1 with physical planes [0, 2R)
+      if ((e = download(cn + kHalo, nx + 2 * kHalo)) != cudaSuccess) return h->cuda_fail(e, "step_host output");
+      if ((e = download(0, 2 * R + kHalo)) != cudaSuccess) return h->cuda_fail(e, "step_host output");
+    }
+  }
+  e = cudaStreamSynchronize(h->copy_stream2);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->copy_stream);
+  if (e != cudaSuccess) return h->cuda_fail(e, "step_host");
+  h->cur = 1 - h->cur;
+  if (h->record_force) h->force_valid = 1;
+  return LBGPU_OK;
+}
+
+}  // namespace
+
+int lbgpu_step_host(lbgpu_handle* h, const double* const* fluids_in, const int32_t* mask, double* const* fluids_out) {
+  if (!h || !fluids_in || !fluids_out) return LBGPU_E_INVALID;
+  for (int c = 0; c < h->C; ++c)
+    if (!fluids_in[c]) return h->fail(LBGPU_E_INVALID, "null fluid array");
+  if (h->lite || !h->rho) return h->fail(LBGPU_E_INVALID, "batch members step with their batch");
+  if (h->advected) return h->fail(LBGPU_E_NOTREADY, "lbgpu_step_host between lbgpu_advect and lbgpu_collide");
+  const int K = (h->cfg.precision == LBGPU_FP64 && !h->profiling) ? wave_planes(h) : 0;
+  if (K == 0) {
+    // the other forms (the FP16 scale needs the whole input first), profiled
+    // handles and lattices too small for the wavefront: one after another
+    if (int rc = lbgpu_upload(h, fluids_in, mask)) return rc;
+    if (int rc = lbgpu_step(h, 1)) return rc;
+    return lbgpu_download(h, fluids_out);
+  }
+  cudaSetDevice(h->cfg.device);
+  cudaError_t e = wave_setup(h);
+  if (e != cudaSuccess) return h->cuda_fail(e, "transfer streams");
+  if (int rc = upload_mask(h, mask)) return rc;
+  if (int rc = lb_update_nbmask(h)) return rc;
+  h->force_valid = 0;
+  if (int rc = step_host_wave(h, fluids_in, fluids_out, K)) return rc;
+  h->uploaded = true;
   return LBGPU_OK;
 }
 

@@ -43,6 +43,11 @@ struct lbgpu_handle {
   // (events: [0..1] half filled, [2..3] half free again)
   cudaStream_t copy_stream = nullptr;
   cudaEvent_t xfer_ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  // lbgpu_step_host: device-to-host copies on their own stream, so that both
+  // directions of the host link carry data at once; events of its wavefront
+  // (created on first use)
+  cudaStream_t copy_stream2 = nullptr;
+  cudaEvent_t pipe_ev[9] = {};
   bool owns_staging = true;         // false: borrowed from a batch
   bool lite = false;                // batch member: no rho/psi scratch (fused step only)
   double* moments = nullptr;        // device scratch for lbgpu_moments / lbgpu_reduce

@@ -26,6 +26,10 @@ namespace lbk {
 struct StepParams {
   int32_t nx, ny, nz;
   int64_t n;              // sites
+  // sites [s_begin, s_end) of one launch of the two-kernel step (whole
+  // x-planes, for host transfers that overlap the step); s_end == 0: all n
+  int64_t s_begin;
+  int64_t s_end;
   int32_t shan_chen;
   int32_t psi_form;
   int32_t eq_form;
@@ -153,8 +157,8 @@ __device__ __forceinline__ void load_local(const T* __restrict__ f, int64_t s, i
 template <typename T, typename R, int Q, int C, bool WALLS, bool STREAM = true>
 __global__ void __launch_bounds__(128) k_density_psi(const T* __restrict__ f, const uint8_t* __restrict__ mask,
                                                      R* __restrict__ rho, R* __restrict__ psi, StepParams P) {
-  const int64_t s = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (s >= P.n) return;
+  const int64_t s = P.s_begin + int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (s >= (P.s_end ? P.s_end : P.n)) return;
   const Site S = make_site(s, P);
   const bool solid = WALLS && mask[s];
 #pragma unroll
@@ -182,8 +186,8 @@ __global__ void __launch_bounds__(128, 3) k_collide(const T* __restrict__ f, T* 
                                                  const R* __restrict__ psi, double* __restrict__ force_out,
                                                  StepParams P) {
   constexpr int D = Conn<Q>::D;
-  const int64_t s = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (s >= P.n) return;
+  const int64_t s = P.s_begin + int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (s >= (P.s_end ? P.s_end : P.n)) return;
   const bool solid = WALLS && mask[s];
 
   R den[C];

@@ -36,6 +36,17 @@ cudaError_t launch_step_f32(int q, int c, const StepBuffers& b, const StepParams
 cudaError_t launch_step_f16(int q, int c, const StepBuffers& b, const StepParams& P, cudaStream_t stream,
                             int64_t* launches, const StepEvents* ev);
 
+// One kernel of the FP64 timestep over the x-planes whose sites are
+// [P.s_begin, P.s_end): the step as a wavefront over plane ranges, for host
+// transfers that overlap it.  A plane range of k_density_psi needs the
+// populations of its planes and R planes either side (R = the largest |c_x|,
+// periodic); one of k_collide needs those and the densities/psi of R planes
+// either side.
+constexpr int kPartDensityPsi = 1;
+constexpr int kPartCollide = 2;
+cudaError_t launch_part_f64(int part, int q, int c, const StepBuffers& b, const StepParams& P, cudaStream_t stream,
+                            int64_t* launches);
+
 // The timestep split at the reference's hook points (advection, then
 // density/force/collision), for host code that runs hooks in between.
 constexpr int kPhaseAdvect = 1;

@@ -43,6 +43,47 @@ cudaError_t dispatch_step(int q, int c, const StepBuffers& b, const StepParams& 
   return cudaErrorInvalidValue;
 }
 
+// One kernel of the timestep over the sites [P.s_begin, P.s_end) (whole
+// x-planes): part kPartDensityPsi queues k_density_psi, kPartCollide
+// k_collide.  The per-site arithmetic is that of launch_step_t.
+template <typename T, typename R, int Q, int C, bool W>
+cudaError_t launch_part_t(int part, const StepBuffers& b, const StepParams& P, cudaStream_t st, int64_t* launches) {
+  const int64_t count = P.s_end - P.s_begin;
+  if (P.s_end <= 0 || count <= 0 || P.s_begin < 0 || P.s_end > P.n) return cudaErrorInvalidValue;
+  const unsigned blocks = unsigned((count + kStepThreads - 1) / kStepThreads);
+  if (part == kPartDensityPsi)
+    k_density_psi<T, R, Q, C, W><<<blocks, kStepThreads, 0, st>>>(static_cast<const T*>(b.f), b.mask,
+                                                                   static_cast<R*>(b.rho), static_cast<R*>(b.psi), P);
+  else if (part == kPartCollide)
+    k_collide<T, R, Q, C, W><<<blocks, kStepThreads, 0, st>>>(static_cast<const T*>(b.f), static_cast<T*>(b.fout),
+                                                               b.mask, static_cast<const R*>(b.rho),
+                                                               static_cast<const R*>(b.psi), b.force, P);
+  else
+    return cudaErrorInvalidValue;
+  *launches += 1;
+  return cudaGetLastError();
+}
+
+template <typename T, typename R>
+cudaError_t dispatch_part(int part, int q, int c, const StepBuffers& b, const StepParams& P, cudaStream_t st,
+                          int64_t* launches) {
+  const bool w = b.mask != nullptr;
+#define LB_CASE(QQ, CC)                                                 \
+  if (q == QQ && c == CC)                                               \
+    return w ? launch_part_t<T, R, QQ, CC, true>(part, b, P, st, launches) \
+             : launch_part_t<T, R, QQ, CC, false>(part, b, P, st, launches);
+  LB_CASE(19, 2)
+  LB_CASE(19, 1)
+  LB_CASE(9, 2)
+  LB_CASE(9, 1)
+  LB_CASE(3, 2)
+  LB_CASE(3, 1)
+  LB_CASE(5, 2)
+  LB_CASE(5, 1)
+#undef LB_CASE
+  return cudaErrorInvalidValue;
+}
+
 // One phase of the split timestep: kPhaseAdvect queues k_advect (f -> fout),
 // kPhaseCollide the two kernels without streaming (f is already advected).
 template <typename T, typename R, int Q, int C, bool W>

@@ -92,6 +92,7 @@ int lbgpu_advect(lbgpu_handle* h);
 int lbgpu_collide(lbgpu_handle* h);
 int lbgpu_init_fields(lbgpu_handle* h, const(lbgpu_init)* ini);
 int lbgpu_download(lbgpu_handle* h, double** fluids);
+int lbgpu_step_host(lbgpu_handle* h, const(double*)* fluidsIn, const(int)* mask, double** fluidsOut);
 int lbgpu_moments(lbgpu_handle* h, double** density, double** velocity, double* colour);
 int lbgpu_set_record_force(lbgpu_handle* h, int enable);
 int lbgpu_force(lbgpu_handle* h, double** force);

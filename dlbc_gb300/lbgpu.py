@@ -26,7 +26,7 @@ ERRORS = {0: "OK", -1: "LBGPU_E_INVALID", -2: "LBGPU_E_NOMEM", -3: "LBGPU_E_CUDA
 
 EXPORTED = ["lbgpu_abi_version", "lbgpu_create", "lbgpu_destroy", "lbgpu_upload", "lbgpu_step",
             "lbgpu_advect", "lbgpu_collide",
-            "lbgpu_download", "lbgpu_moments", "lbgpu_set_record_force", "lbgpu_force", "lbgpu_reduce",
+            "lbgpu_download", "lbgpu_step_host", "lbgpu_moments", "lbgpu_set_record_force", "lbgpu_force", "lbgpu_reduce",
             "lbgpu_synchronize", "lbgpu_set_stream", "lbgpu_profile", "lbgpu_kernel_time",
             "lbgpu_launch_count", "lbgpu_device_bytes", "lbgpu_last_error"]
 
@@ -66,6 +66,7 @@ def lib() -> C.CDLL:
         L.lbgpu_advect.argtypes = [H]
         L.lbgpu_collide.argtypes = [H]
         L.lbgpu_download.argtypes = [H, PP]
+        L.lbgpu_step_host.argtypes = [H, PP, C.c_void_p, PP]
         L.lbgpu_moments.argtypes = [H, PP, PP, C.c_void_p]
         L.lbgpu_set_record_force.argtypes = [H, C.c_int32]
         L.lbgpu_force.argtypes = [H, PP]
@@ -180,6 +181,30 @@ class GPULattice:
 
     def step(self, n: int = 1) -> None:
         self._check(lib().lbgpu_step(self.h, int(n)), "lbgpu_step")
+
+    def step_host(self, fluids: List, mask=None, out: Optional[List] = None) -> List:
+        """One timestep from host fields to host fields (``lbgpu_step_host``):
+        the same as upload(fluids, mask), step(1), download(out).  ``out``
+        may be ``fluids`` itself."""
+        if out is None:
+            out = [np.empty(self.nH + (self.p.q,), np.float64) for _ in range(self.p.components)]
+        pin = (C.c_void_p * MAXC)()
+        for i, a in enumerate(fluids):
+            if isinstance(a, np.ndarray):
+                assert a.dtype == np.float64 and a.flags.c_contiguous and a.shape == self.nH + (self.p.q,)
+            pin[i] = _ptr_of(a)
+        pout = (C.c_void_p * MAXC)()
+        for i, a in enumerate(out):
+            if isinstance(a, np.ndarray):
+                assert a.dtype == np.float64 and a.flags.c_contiguous and a.shape == self.nH + (self.p.q,)
+            pout[i] = _ptr_of(a)
+        m = None
+        if mask is not None:
+            if isinstance(mask, np.ndarray):
+                assert mask.dtype == np.int32 and mask.flags.c_contiguous and mask.shape == self.nH
+            m = _ptr_of(mask)
+        self._check(lib().lbgpu_step_host(self.h, pin, m, pout), "lbgpu_step_host")
+        return out
 
     def advect(self) -> None:
         """First phase of a timestep (streaming); :meth:`collide` completes it."""

@@ -154,6 +154,18 @@ int lbgpu_init_fields(lbgpu_handle* h, const lbgpu_init* ini);
  * are filled with their periodic images, as after exchangeHalo). */
 int lbgpu_download(lbgpu_handle* h, double* const* fluids);
 
+/* One timestep with the fields on the host on both sides: the same result as
+ * lbgpu_upload(h, fluids_in, mask), lbgpu_step(h, 1), lbgpu_download(h,
+ * fluids_out), bit for bit, for a host that keeps L.fluids as the state and
+ * runs hooks on it between steps (runTimeloop's body, src/main.d:179-195,
+ * with pre/postAdvection and pre/postCollision hooks registered through
+ * src/dlbc/hooks.d:57-118).  In the FP64 form the input copies, the kernels
+ * and the output copies run as a wavefront over chunks of x-planes, so both
+ * directions of the host link carry data at once.  fluids_out may alias
+ * fluids_in; a NULL fluids_out[c] skips component c's output. */
+int lbgpu_step_host(lbgpu_handle* h, const double* const* fluids_in, const int32_t* mask,
+                    double* const* fluids_out);
+
 /* Fields as dumpLBData writes them (src/dlbc/lb/io.d:56-101), over the
  * physical lattice, row-major [x][y][z] (+ vector component fastest):
  *   density[c]   N doubles  (densityField, src/dlbc/lb/density.d:89)
