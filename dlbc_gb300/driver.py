@@ -324,6 +324,18 @@ class Simulation:
     def step_once(self) -> None:
         """One iteration of ``runTimeloop``'s body (src/main.d:175-199) with
         the hook points of advectFields / collideFields."""
+        mid = len(self.postAdvectionHooks) or len(self.preCollisionHooks)
+        if not mid and len(self.postCollisionHooks):
+            # the host fields go through the timestep in one call
+            # (lbgpu_step_host: upload, step and download overlapped) and
+            # come back for the post-collision hooks
+            self.sync_to_host()
+            self.preAdvectionHooks.execute(self)
+            self.lattice.step_host(self.fluids, self.mask if self._walls() else None, self.fluids)
+            self.postCollisionHooks.execute(self)
+            self.sync_to_device()
+            self._host_valid = True  # the device holds what the hooks left
+            return
         self._host_valid = False
         self._run_hooks([self.preAdvectionHooks])
         if len(self.postAdvectionHooks) or len(self.preCollisionHooks):

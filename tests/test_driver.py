@@ -45,6 +45,11 @@ class OracleLattice:
     def step(self, n=1):
         self.o.run(n)
 
+    def step_host(self, fluids, mask=None, out=None):
+        self.upload(fluids, mask)
+        self.step(1)
+        return self.download(out)
+
     def advect(self):
         pass
 
@@ -229,6 +234,57 @@ def _restart_case(tmp_path, monkeypatch, lattice_cls, hooks=False):
 
 def test_restore_continues_exactly_cpu(tmp_path, monkeypatch):
     _restart_case(tmp_path, monkeypatch, OracleLattice)
+
+
+def hook_paths_case(tmp_path, monkeypatch, lattice_cls):
+    """Hooks that change the host fields before advection and after
+    collision: the one-call path (lbgpu_step_host, taken when no hook sits
+    between advection and collision) and the split path (forced here by a
+    no-op post-advection hook) write the same populations."""
+    monkeypatch.chdir(tmp_path)
+    inp = tmp_path / "hp.in"
+    inp.write_text("\n".join([
+        "[lattice]", "gn = [24, 10, 8]",
+        "[lb]", "timesteps = 4", "components = 2", 'fieldNames = ["red", "blue"]', "tau = [1.0, 0.9]",
+        "eqdist.eqDistForm = BDist2", "force.enableShanChen = true", "force.gcc = [[0.0, 3.6], [3.6, 0.0]]",
+        "force.psiForm = Exponential", "force.globalAcc = [1e-5, 0.0, 0.0]",
+        "init.fluidInit = [EqDistPerturb, EqDistPerturb]", "init.fluidDensities = [[0.7], [0.7]]",
+        "init.fluidPerturb = [0.02, 0.02]", "io.populationFreq = 4",
+        "mask.maskInit = Walls", "mask.dimensionHasWall = [[false, false], [false, false], [true, true]]",
+        "[io]", "simulationName = hp", "outputPath = out",
+        "[random]", "seed = 5"]))
+
+    def pre(sim):
+        sim.fluids[0][..., 0] *= 1.001
+
+    def post(sim):
+        sim.fluids[1][..., 1] *= 0.999
+
+    runs = {}
+    for name, split in (("one", False), ("split", True)):
+        sim = driver.Simulation([str(inp)], sim_id=name, lattice_cls=lattice_cls)
+        sim.preAdvectionHooks.registerFunction(pre, "pre")
+        sim.postCollisionHooks.registerFunction(post, "post")
+        if split:
+            sim.postAdvectionHooks.registerFunction(lambda s: None, "noop")
+        sim.setup()
+        sim.run()
+        sim.close()
+        runs[name] = [h5.read_field(f"out/population-{c}-hp-{name}-t00000004.h5") for c in ("red", "blue")]
+    for a, b in zip(runs["one"], runs["split"]):
+        assert np.array_equal(a, b)
+
+
+def test_hook_paths_agree_cpu(tmp_path, monkeypatch):
+    calls = []
+
+    class Counting(OracleLattice):
+        def step_host(self, fluids, mask=None, out=None):
+            calls.append(1)
+            return super().step_host(fluids, mask, out)
+
+    hook_paths_case(tmp_path, monkeypatch, Counting)
+    assert len(calls) == 4  # the one-call run used it every step, the split run never
 
 
 # ---------------------------------------------------------------------------

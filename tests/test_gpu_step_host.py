@@ -13,6 +13,7 @@ import pytest
 
 from dlbc_gb300 import init, lbgpu
 from lbcases import droplet_channel, spinodal
+from test_driver import hook_paths_case
 from test_gpu_parity import _lattice_1d
 
 pytestmark = pytest.mark.gpu
@@ -113,3 +114,9 @@ def test_step_host_rejects_bad_calls():
     ref = seq.download()
     for c in range(2):
         assert np.array_equal(out[c], ref[c])
+
+
+def test_driver_hook_paths_agree_gpu(tmp_path, monkeypatch):
+    """The driver's one-call path (host hooks before advection and after
+    collision) and its split path write the same populations on the GPU."""
+    hook_paths_case(tmp_path, monkeypatch, lbgpu.GPULattice)
