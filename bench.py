@@ -147,16 +147,35 @@ def time_form(p, fluids, mask, precision, steps, warmup, device, torch):
     return ms / steps, k2_ms / max(k2_n, 1), k1_ms / max(k1_n, 1), launches
 
 
+# FP64 operations per site of k_collide (D3Q19, two components, BDist2,
+# tau = 1, z walls): ncu counted 4.0 M DMUL + 3.9 M DADD warp instructions
+# (no DFMA: the reference's arithmetic without contraction) for the 524,288
+# sites of the 128x64x64 case of this workload, i.e. 7.9 M x 32 / 524,288
+# (profiles/k_collide_fp64_droplet_channel_128x64x64.md).
+K_COLLIDE_FP64_OPS_PER_SITE = 482
+# GB300's nominal FP64 rate, 1.25 TFLOP/s counting a DFMA as two: 0.625 T
+# FP64 instructions (DADD, DMUL or DFMA) per second
+FP64_INSTR_PEAK_G = 625.0
+
+
 def roofline(precision, sites, kernel_ms, peak, peak_kind, traffic=None):
     """HBM roofline of the dominant kernel: k_collide (FP64 two-kernel step)
-    or k_fused (the single-pass FP32 / FP16 step)."""
+    or k_fused (the single-pass FP32 / FP16 step).  k_collide is limited by
+    the FP64 pipe, not by HBM: its FP64 instruction rate against GB300's
+    nominal FP64 rate goes beside the HBM figures."""
     alg = bytes_per_site(precision) * sites
     achieved = alg / (kernel_ms * 1e-3) / 1e9
     from dlbc_gb300 import lbgpu
     kernel = "k_collide" if precision == lbgpu.FP64 else "k_fused"
-    return {"bound": "hbm", "kernel": kernel, "achieved": round(achieved, 1), "peak": peak,
-            "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
-            "traffic": traffic, "algorithmic_bytes": alg}
+    out = {"bound": "hbm", "kernel": kernel, "achieved": round(achieved, 1), "peak": peak,
+           "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
+           "traffic": traffic, "algorithmic_bytes": alg}
+    if precision == lbgpu.FP64:
+        g = K_COLLIDE_FP64_OPS_PER_SITE * sites / (kernel_ms * 1e-3) / 1e9
+        out["limiter"] = {"pipe": "fp64", "ops_per_site": K_COLLIDE_FP64_OPS_PER_SITE,
+                          "achieved": round(g, 1), "peak": FP64_INSTR_PEAK_G, "peak_kind": "nominal",
+                          "unit": "G FP64 instructions/s", "frac": round(g / FP64_INSTR_PEAK_G, 4)}
+    return out
 
 
 def read_traffic(form):
