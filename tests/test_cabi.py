@@ -50,3 +50,45 @@ def test_create_rejects_bad_configs_without_touching_the_gpu(libpath):
         rc = L.lbgpu_create(ctypes.byref(cfg), ctypes.byref(h))
         assert rc == -1 and not h.value
         assert L.lbgpu_last_error(None)
+
+
+C_CONSUMER = r"""
+#include <stdio.h>
+#include <string.h>
+#include "lbgpu.h"
+
+int main(void) {
+  lbgpu_config cfg;
+  lbgpu_handle* h = NULL;
+  memset(&cfg, 0, sizeof cfg);
+  cfg.d = 3;
+  cfg.q = 27; /* no such connectivity: refused before any device work */
+  cfg.gn[0] = cfg.gn[1] = cfg.gn[2] = 8;
+  cfg.components = 2;
+  cfg.tau[0] = cfg.tau[1] = 1.0;
+  int rc = lbgpu_create(&cfg, &h);
+  const char* msg = lbgpu_last_error(NULL);
+  printf("%d %d %d %s\n", lbgpu_abi_version(), rc, h == NULL, msg ? "msg" : "none");
+  return 0;
+}
+"""
+
+
+@pytest.mark.parametrize("lang", ["c", "c++"])
+def test_header_compiles_links_and_runs_from_c_and_cpp(libpath, tmp_path, lang):
+    """A C99 and a C++17 host include include/lbgpu.h, link liblbgpu.so and
+    call it: the ABI version and a configuration refused without a GPU."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc" if lang == "c" else "g++")
+    if cc is None:
+        pytest.skip(f"no {lang} compiler")
+    src = tmp_path / ("consumer.c" if lang == "c" else "consumer.cpp")
+    src.write_text(C_CONSUMER)
+    exe = tmp_path / "consumer"
+    libdir = os.path.dirname(libpath)
+    std = "-std=c99" if lang == "c" else "-std=c++17"
+    subprocess.run([cc, std, "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe),
+                    "-L", libdir, "-llbgpu", f"-Wl,-rpath,{libdir}"], check=True, capture_output=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()
+    assert out == ["1", "-1", "1", "msg"], out
