@@ -18,14 +18,17 @@
    whose hooks read or change the populations set $(D gpu.hostHooks = true):
    each step is then split at the hook points (lbgpu_advect, lbgpu_collide)
    and the fields are downloaded before and uploaded after every hook list.
+   Plugins whose hooks sit only before advection and after collision also
+   set $(D gpu.hooksAroundStep = true): each step is then one
+   $(D lbgpu_step_host) call on the D fields, which stay the state.
 
    Errors: a nonzero status from the library is fatal, through writeLogF
    (src/dlbc/logging.d:255), as every fatal error of the reference is.
 
    Usage: add this module (src/dlbc/gpu/gpu.d) and dlbc.gpu.lbgpu
    (src/dlbc/gpu/lbgpu.d); its @("param") variables are read from a [gpu]
-   section (enableGpu, precision, device, hostHooks) once the module is in
-   the parameter parser's module list (src/dlbc/parameters.d:366-370); link
+   section (enableGpu, precision, device, hostHooks, hooksAroundStep) once
+   the module is in the parameter parser's module list (src/dlbc/parameters.d:366-370); link
    liblbgpu.so, and in main (src/main.d:153) call
    ---
    if ( enableGpu ) L.runTimeloopGpu(); else L.runTimeloop();
@@ -60,6 +63,15 @@ import dlbc.logging;
 @("param") int device;
 /// Refresh the fields around every hook list each step.
 @("param") bool hostHooks;
+/**
+   With hostHooks: the plugins' hooks sit only on preAdvectionHooks and
+   postCollisionHooks.  Each step is then one lbgpu_step_host call (input
+   copies, kernels and output copies overlapped) between the two lists.  The
+   reference's own postAdvectionHooks (markDensitiesAsStale, markPsiAsStale,
+   src/dlbc/lb/density.d:338, src/dlbc/lb/force.d:131) run after the step,
+   where they mark the host's cached fields stale as before.
+*/
+@("param") bool hooksAroundStep;
 
 private lbgpu_handle* handle;
 
@@ -103,6 +115,17 @@ private void upload(T)(ref T L) {
   const(double)*[LBGPU_MAX_COMPONENTS] f;
   foreach(immutable i, ref e; L.fluids) f[i] = cast(const(double)*) e.arr._data.ptr;
   check(lbgpu_upload(handle, f.ptr, cast(const(int)*) L.mask.arr._data.ptr), "upload");
+}
+
+/// One timestep from the D fields to the D fields (lbgpu_step_host).
+private void stepHost(T)(ref T L) {
+  const(double)*[LBGPU_MAX_COMPONENTS] fin;
+  double*[LBGPU_MAX_COMPONENTS] fout;
+  foreach(immutable i, ref e; L.fluids) {
+    fin[i] = cast(const(double)*) e.arr._data.ptr;
+    fout[i] = cast(double*) e.arr._data.ptr;
+  }
+  check(lbgpu_step_host(handle, fin.ptr, cast(const(int)*) L.mask.arr._data.ptr, fout.ptr), "step_host");
 }
 
 private void download(T)(ref T L) {
@@ -164,7 +187,17 @@ void runTimeloopGpu(T)(ref T L) if ( isLattice!T ) {
   writeLogRN("Running the timestep on GPU %d (%s).", device, precision);
 
   while ( timestep < timesteps ) {
-    if ( hostHooks ) {
+    if ( hostHooks && hooksAroundStep ) {
+      // the D fields hold the state between steps: they go through the
+      // timestep in one call and come back for the post-collision hooks
+      ++timestep;
+      writeLogRN("Starting timestep %d", timestep);
+      preAdvectionHooks.execute(L);
+      stepHost(L);
+      postAdvectionHooks.execute(L);
+      postCollisionHooks.execute(L);
+    }
+    else if ( hostHooks ) {
       ++timestep;
       writeLogRN("Starting timestep %d", timestep);
       download(L);
