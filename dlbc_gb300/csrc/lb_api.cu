@@ -1114,14 +1114,16 @@ int lbgpu_moments(lbgpu_handle* h, double* const* density, double* const* veloci
   if (!h->uploaded) return h->fail(LBGPU_E_NOTREADY, "lbgpu_moments before lbgpu_upload");
   cudaSetDevice(h->cfg.device);
   if (int rc = lb_ensure_moments(h)) return rc;
-  // the staging buffer holds C*N*d doubles of velocity when large enough,
-  // else velocities go one component at a time through the moments buffer
+  // densities go through the moments buffer (C*N doubles), velocities
+  // through a temporary stream-ordered device buffer (C*N*d doubles)
   cudaError_t e;
   const size_t n = size_t(h->n);
   // densities (and colour) first
   const bool want_den = density != nullptr || colour != nullptr;
   if (want_den) {
-    double* col = h->staging;  // N doubles fit: staging >= one haloed plane... ensure below
+    // the colour goes through the staging buffer when N doubles fit in it,
+    // else it is formed on the host from the densities
+    double* col = h->staging;
     const bool col_fits = h->staging_bytes >= n * sizeof(double);
     std::vector<double> tmp;
     double* dcol = (colour && h->C > 1 && col_fits) ? col : nullptr;
@@ -1162,9 +1164,8 @@ int lbgpu_moments(lbgpu_handle* h, double* const* density, double* const* veloci
     if (e != cudaSuccess) return h->cuda_fail(e, "moments");
   }
   if (velocity) {
-    // d doubles per site per component: reuse the moments buffer (C*N
-    // doubles) one component-coordinate slab at a time is not possible in
-    // one kernel, so compute into a temporary device buffer
+    // d doubles per site per component do not fit the moments buffer (C*N
+    // doubles): one kernel writes them into a temporary device buffer
     double* dvel = nullptr;
     const size_t vbytes = size_t(h->C) * n * h->d * sizeof(double);
     e = cudaMallocAsync(reinterpret_cast<void**>(&dvel), vbytes, h->stream);
