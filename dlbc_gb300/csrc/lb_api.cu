@@ -988,6 +988,14 @@ int step_host_wave(lbgpu_handle* h, const double* const* in, double* const* out,
   b.psi = h->psi;
   b.force = h->force;
   cudaError_t e;
+  // on an error, let the copies already queued finish before returning: the
+  // caller may free or reuse its host arrays once the call returns
+  auto fail = [&](cudaError_t err, const char* what) {
+    cudaStreamSynchronize(h->copy_stream);
+    cudaStreamSynchronize(h->stream);
+    cudaStreamSynchronize(h->copy_stream2);
+    return h->cuda_fail(err, what);
+  };
 
   // work queued earlier on h->stream (the mask upload, moments that use the
   // staging buffer) precedes the copies into the staging buffer
@@ -1042,7 +1050,7 @@ int step_host_wave(lbgpu_handle* h, const double* const* in, double* const* out,
     for (int c = 0; c < h->C; ++c) {
       e = cudaMemcpyAsync(slot(2 * p + c), in[c] + size_t(a + kHalo) * plane_vals, size_t(bnd - a) * plane_bytes,
                           cudaMemcpyHostToDevice, h->copy_stream);
-      if (e != cudaSuccess) return h->cuda_fail(e, "step_host input copy");
+      if (e != cudaSuccess) return fail(e, "step_host input copy");
     }
     cudaEventRecord(ev[1 + p], h->copy_stream);
     cudaStreamWaitEvent(h->stream, ev[1 + p], 0);
@@ -1052,25 +1060,25 @@ int step_host_wave(lbgpu_handle* h, const double* const* in, double* const* out,
                                                                             bnd - a, g, h->P);
       h->launches++;
     }
-    if ((e = cudaGetLastError()) != cudaSuccess) return h->cuda_fail(e, "step_host input transpose");
+    if ((e = cudaGetLastError()) != cudaSuccess) return fail(e, "step_host input transpose");
     cudaEventRecord(ev[3 + p], h->stream);
     const bool last = bnd == nx;
     const int dnew = last ? nx : bnd - R;
-    if ((e = part(lbk::kPartDensityPsi, dn, dnew)) != cudaSuccess) return h->cuda_fail(e, "step_host density");
+    if ((e = part(lbk::kPartDensityPsi, dn, dnew)) != cudaSuccess) return fail(e, "step_host density");
     dn = std::max(dn, dnew);
-    if (last && (e = part(lbk::kPartDensityPsi, 0, R)) != cudaSuccess) return h->cuda_fail(e, "step_host density");
+    if (last && (e = part(lbk::kPartDensityPsi, 0, R)) != cudaSuccess) return fail(e, "step_host density");
     const int cnew = last ? nx : dn - R;
-    if ((e = part(lbk::kPartCollide, cn, cnew)) != cudaSuccess) return h->cuda_fail(e, "step_host collide");
+    if ((e = part(lbk::kPartCollide, cn, cnew)) != cudaSuccess) return fail(e, "step_host collide");
     if (!last) {
       if (cnew > cn && (e = download(cn + kHalo, cnew + kHalo)) != cudaSuccess)
-        return h->cuda_fail(e, "step_host output");
+        return fail(e, "step_host output");
       cn = std::max(cn, cnew);
     } else {
-      if ((e = part(lbk::kPartCollide, 0, 2 * R)) != cudaSuccess) return h->cuda_fail(e, "step_host collide");
+      if ((e = part(lbk::kPartCollide, 0, 2 * R)) != cudaSuccess) return fail(e, "step_host collide");
       // physical planes [cn, nx) with the images of planes 0 and 1, then the
       // images of planes nx-2 and nx-1 with physical planes [0, 2R)
-      if ((e = download(cn + kHalo, nx + 2 * kHalo)) != cudaSuccess) return h->cuda_fail(e, "step_host output");
-      if ((e = download(0, 2 * R + kHalo)) != cudaSuccess) return h->cuda_fail(e, "step_host output");
+      if ((e = download(cn + kHalo, nx + 2 * kHalo)) != cudaSuccess) return fail(e, "step_host output");
+      if ((e = download(0, 2 * R + kHalo)) != cudaSuccess) return fail(e, "step_host output");
     }
   }
   e = cudaStreamSynchronize(h->copy_stream2);
