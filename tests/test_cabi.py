@@ -43,7 +43,9 @@ def test_create_rejects_bad_configs_without_touching_the_gpu(libpath):
                            gwc=[0, 0], global_acc=[0, 0, 0])
     for mutate in (lambda c: setattr(c, "q", 27), lambda c: setattr(c, "components", 3),
                    lambda c: c.gn.__setitem__(0, 1), lambda c: setattr(c, "precision", 9),
-                   lambda c: c.tau.__setitem__(0, 0.0)):
+                   lambda c: c.tau.__setitem__(0, 0.0),
+                   # 4096 x 4096 x 256 = 2^32 sites: above the 2^31-site limit
+                   lambda c: [c.gn.__setitem__(i, v) for i, v in enumerate((4096, 4096, 256))]):
         cfg = lbgpu.make_config(base)
         mutate(cfg)
         h = ctypes.c_void_p()
