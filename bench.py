@@ -147,43 +147,127 @@ def time_form(p, fluids, mask, precision, steps, warmup, device, torch):
     return ms / steps, k2_ms / max(k2_n, 1), k1_ms / max(k1_n, 1), launches
 
 
-# FP64 operations per site of k_collide (D3Q19, two components, BDist2,
-# tau = 1, z walls): ncu counted 4.0 M DMUL + 3.9 M DADD warp instructions
-# (no DFMA: the reference's arithmetic without contraction) for the 524,288
-# sites of the 128x64x64 case of this workload, i.e. 7.9 M x 32 / 524,288
-# (profiles/k_collide_fp64_droplet_channel_128x64x64.md).
-K_COLLIDE_FP64_OPS_PER_SITE = 482
-# GB300's nominal FP64 rate, 1.25 TFLOP/s counting a DFMA as two: 0.625 T
-# FP64 instructions (DADD, DMUL or DFMA) per second
-FP64_INSTR_PEAK_G = 625.0
-
-
-def roofline(precision, sites, kernel_ms, peak, peak_kind, traffic=None):
-    """HBM roofline of the dominant kernel: k_collide (FP64 two-kernel step)
-    or k_fused (the single-pass FP32 / FP16 step).  k_collide is limited by
-    the FP64 pipe, not by HBM: its FP64 instruction rate against GB300's
-    nominal FP64 rate goes beside the HBM figures."""
-    alg = bytes_per_site(precision) * sites
-    achieved = alg / (kernel_ms * 1e-3) / 1e9
+def time_form_device(p, precision, steps, warmup, device, torch, seed=11):
+    """time_form for a lattice initialised on the device (lbgpu_init_fields):
+    no host copy of the fields, for lattices too large to build on the host."""
     from dlbc_gb300 import lbgpu
-    kernel = "k_collide" if precision == lbgpu.FP64 else "k_fused"
-    out = {"bound": "hbm", "kernel": kernel, "achieved": round(achieved, 1), "peak": peak,
-           "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
-           "traffic": traffic, "algorithmic_bytes": alg}
-    if precision == lbgpu.FP64:
-        g = K_COLLIDE_FP64_OPS_PER_SITE * sites / (kernel_ms * 1e-3) / 1e9
-        out["limiter"] = {"pipe": "fp64", "ops_per_site": K_COLLIDE_FP64_OPS_PER_SITE,
-                          "achieved": round(g, 1), "peak": FP64_INSTR_PEAK_G, "peak_kind": "nominal",
-                          "unit": "G FP64 instructions/s", "frac": round(g / FP64_INSTR_PEAK_G, 4)}
+    g = lbgpu.GPULattice(p, precision=precision, device=device)
+    g.init_device(seed)
+    stream = torch.cuda.Stream(device=device)
+    g.set_stream(stream.cuda_stream)
+    g.step(warmup)
+    g.synchronize()
+    g.profile(True)
+    start = torch.cuda.Event(enable_timing=True)
+    stop = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize(device)
+    n0 = g.launch_count
+    start.record(stream)
+    g.step(steps)
+    stop.record(stream)
+    stop.synchronize()
+    torch.cuda.synchronize(device)
+    ms = start.elapsed_time(stop)
+    launches = g.launch_count - n0
+    k1_ms, k1_n = g.kernel_time(0)
+    k2_ms, k2_n = g.kernel_time(1)
+    g.profile(False)
+    g.close()
+    return ms / steps, k2_ms / max(k2_n, 1), k1_ms / max(k1_n, 1), launches
+
+
+SPINODAL_N = 512
+SPINODAL_WORKLOAD = (f"periodic spinodal {SPINODAL_N}^3 D3Q19 two-component Shan-Chen, rho 0.7 +- 0.02, "
+                     f"tau 1, g 3.6, BDist2")
+
+
+def run_spinodal(device, torch, peak, peak_kind, fp64_peak, dist=None, n=SPINODAL_N):
+    """The precision-study lattice (512^3 periodic spinodal decomposition,
+    134 M sites) in every form, initialised on the device: MLUPS, ms/step and
+    the dominant kernel's HBM roofline per form."""
+    from dlbc_gb300 import lbgpu, precision_study, replicas
+    p = precision_study.spinodal_params(n, 0.02)
+    sites = n ** 3
+    world = dist.get_world_size() if dist is not None else 1
+    out = {"workload": SPINODAL_WORKLOAD.replace(str(SPINODAL_N), str(n)), "lattice": [n, n, n],
+           "init": "device (lbgpu_init_fields, counter-based noise)",
+           "l2": "inputs larger than L2 (FP16 populations alone 10.2 GB)", "forms": {}}
+    for name, prec, steps in (("fp64", lbgpu.FP64, 10), ("fp32", lbgpu.FP32, 40), ("fp16", lbgpu.FP16, 40)):
+        ms, k2, k1, launches = time_form_device(p, prec, steps, 3, device, torch)
+        ms = replicas.max_over_ranks(ms, dist, device=f"cuda:{device}")
+        out["forms"][name] = {
+            "value": round(world * sites / (ms * 1e-3) / 1e6, 1), "unit": UNIT, "ms_per_step": round(ms, 4),
+            "steps": steps, "warmup": 3, "gpu_launches": launches,
+            "roofline": roofline(prec, sites, k2, peak, peak_kind, read_traffic(f"spinodal{n}/{name}"),
+                                 fp64_peak, walls=False),
+            "step_roofline_frac": round(bytes_per_site(prec, False) * sites / (ms * 1e-3) / 1e9 / peak, 4)}
     return out
 
 
-def read_traffic(form):
-    """DRAM bytes per k_collide launch from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "traffic_droplet_channel.json")
+# FP64 operations per site of k_collide (D3Q19, two components, BDist2,
+# tau = 1, z walls): ncu counted 4.0 M DMUL + 3.9 M DADD warp instructions
+# (no DFMA: the reference's arithmetic without contraction) for the 524,288
+# sites of the 128x64x64 case of this workload, i.e. 7.9 M x 32 / 524,288.
+K_COLLIDE_FP64_OPS_PER_SITE = 482
+
+
+def fp64_rate(device):
+    """Measured FP64 instruction rate of this GPU (DADD, DMUL and DFMA
+    dependency chains over every SM, timed with CUDA events; the
+    microbenchmark in dlbc_gb300/csrc/peak_fp64.cu), in G thread operations
+    per second; None if it cannot run."""
+    import ctypes
+    from dlbc_gb300 import build
+    try:
+        L = ctypes.CDLL(build.PEAK_LIB)
+        L.peak_fp64_rates.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+        rates = (ctypes.c_double * 3)()
+        if L.peak_fp64_rates(device, 16384, rates) != 0:
+            return None
+        return {"dadd": rates[0] / 1e9, "dmul": rates[1] / 1e9, "dfma": rates[2] / 1e9}
+    except OSError:
+        return None
+
+
+def roofline(precision, sites, kernel_ms, peak, peak_kind, traffic=None, fp64_peak=None, walls=True,
+             kernel=None):
+    """HBM roofline of the dominant kernel: k_collide (FP64 two-kernel step)
+    or k_fused (the single-pass FP32 / FP16 step).  k_collide is limited by
+    the FP64 pipe, not by HBM: its FP64 instruction rate against the FP64
+    rate measured on this GPU goes beside the HBM figures."""
+    alg = bytes_per_site(precision, walls) * sites
+    achieved = alg / (kernel_ms * 1e-3) / 1e9
+    from dlbc_gb300 import lbgpu
+    if kernel is None:
+        kernel = "k_collide" if precision == lbgpu.FP64 else "k_fused"
+    out = {"bound": "hbm", "kernel": kernel, "achieved": round(achieved, 1), "peak": peak,
+           "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
+           "traffic": traffic["bytes"] if traffic else None,
+           "traffic_source": traffic["source"] if traffic else None, "algorithmic_bytes": alg,
+           "kernel_ms": round(kernel_ms, 5)}
+    if precision == lbgpu.FP64:
+        g = K_COLLIDE_FP64_OPS_PER_SITE * sites / (kernel_ms * 1e-3) / 1e9
+        lim = {"pipe": "fp64", "ops_per_site": K_COLLIDE_FP64_OPS_PER_SITE, "achieved": round(g, 1),
+               "unit": "G FP64 thread instructions/s"}
+        if fp64_peak:
+            # k_collide issues DADD and DMUL only (no contraction)
+            pk = 0.5 * (fp64_peak["dadd"] + fp64_peak["dmul"])
+            lim.update({"peak": round(pk, 1), "peak_kind": "measured (DADD/DMUL chains, peak_fp64.cu)",
+                        "frac": round(g / pk, 4), "measured_rates": {k: round(v, 1) for k, v in fp64_peak.items()}})
+        out["limiter"] = lim
+    return out
+
+
+def read_traffic(key):
+    """DRAM bytes (read + write) per launch of the dominant kernel for a
+    workload and form, from the one-pass ncu capture recorded in
+    profiles/traffic.json (with the commit the capture ran at), or None."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
     try:
         with open(path) as fh:
-            return json.load(fh).get(form)
+            d = json.load(fh)
+        e = d["captures"][key]
+        return {"bytes": e["bytes"], "source": f"ncu one-pass capture at commit {e['commit']} ({e['command']})"}
     except Exception:
         return None
 
@@ -377,6 +461,8 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-served", action="store_true")
+    ap.add_argument("--no-spinodal", action="store_true", help="skip the 512^3 spinodal block")
+    ap.add_argument("--spinodal-n", type=int, default=SPINODAL_N, help="edge of the spinodal lattice")
     ap.add_argument("--form", default="fp64", choices=["fp64", "fp32", "fp16"],
                     help="headline form (the others are reported under 'forms')")
     ap.add_argument("--lattice", default=None,
@@ -409,6 +495,7 @@ def main():
     fluids, mask = init.init_fields(p)
     sites = LATTICE[0] * LATTICE[1] * LATTICE[2]
     peak, peak_kind = measured_peaks()
+    fp64_peak = fp64_rate(device)
     forms_all = {"fp64": lbgpu.FP64, "fp32": lbgpu.FP32, "fp16": lbgpu.FP16}
     head = forms_all[args.form]
     dtype = {"fp64": "f64", "fp32": "f32", "fp16": "f16-storage/f32"}[args.form]
@@ -474,10 +561,14 @@ def main():
             forms[name] = {"value": round(world * sites / (f_ms * 1e-3) / 1e6, 1),
                            "ms_per_step": round(f_ms, 4),
                            "k_density_psi_ms": round(f_k1, 4), "k_collide_ms": round(f_k2, 4),
-                           "roofline": roofline(prec, sites, f_k2, peak, peak_kind, read_traffic(name)),
+                           "roofline": roofline(prec, sites, f_k2, peak, peak_kind,
+                                                read_traffic(f"channel{'x'.join(map(str, LATTICE))}/{name}"),
+                                                fp64_peak),
                            "step_roofline_frac": round(bytes_per_site(prec) * sites / (f_ms * 1e-3) / 1e9 / peak,
                                                        4)}
 
+    spinodal = None if args.no_spinodal else run_spinodal(device, torch, peak, peak_kind, fp64_peak, dist=dist,
+                                                            n=args.spinodal_n)
     batched = None if args.no_batched else run_batched(device, torch, dist=dist)
     served = None if args.no_served else run_served(device, dist=dist)
 
@@ -497,13 +588,15 @@ def main():
                        "lattice": list(LATTICE), "form": args.form, "eq_form": "BDist2",
                        "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                        "l2": l2_note},
-            "roofline": roofline(head, sites, k2_ms, peak, peak_kind, read_traffic(args.form)),
+            "roofline": roofline(head, sites, k2_ms, peak, peak_kind,
+                                 read_traffic(f"channel{'x'.join(map(str, LATTICE))}/{args.form}"), fp64_peak),
             "kernels_ms": {"k_density_psi": round(k1_ms, 4), "k_collide": round(k2_ms, 4)},
             "cpu_baseline": cpu,
             "e2e": e2e,
             "gpu_launches": launches,
             "clocks": clk.summary(),
             "forms": forms,
+            "spinodal512": spinodal,
             "batched": batched,
             "served": served,
         }

@@ -10,6 +10,9 @@ Translation units compiled in parallel with one ``-gencode``:
   explicit, so all its kernel variants give the same bits;
 * the two-kernel FP32 / FP16 step and the rest (``lb_step_lp.cu``,
   ``lb_batch.cu``, ``lb_noalloc.cu``) with contraction allowed.
+
+Beside it, ``_build/libpeak_fp64.so`` (``peak_fp64.cu``): the FP64
+instruction-rate microbenchmark the benchmark reports the FP64 form against.
 """
 from __future__ import annotations
 
@@ -23,6 +26,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "liblbgpu.so")
+PEAK_LIB = os.path.join(OUT, "libpeak_fp64.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
@@ -60,10 +64,14 @@ def _sources_mtime() -> float:
 
 def build(force: bool = False, verbose: bool = False) -> str:
     """Compile (if stale) and return the library path."""
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= _sources_mtime():
+    if (not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= _sources_mtime()
+            and os.path.exists(PEAK_LIB) and os.path.getmtime(PEAK_LIB) >= _sources_mtime()):
         return LIB
     os.makedirs(OUT, exist_ok=True)
     nv = nvcc()
+    peak = subprocess.Popen([nv, *ARCH, *COMMON, "-shared", os.path.join(CSRC, "peak_fp64.cu"), "-o",
+                             PEAK_LIB + ".tmp", "-lcudart"], stdout=subprocess.PIPE, stderr=subprocess.PIPE,
+                            text=True)
 
     def compile_unit(item):
         src, extra = item
@@ -84,6 +92,10 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")
     os.replace(tmp, LIB)
+    _, perr = peak.communicate()
+    if peak.returncode != 0:
+        raise RuntimeError(f"nvcc failed for peak_fp64.cu:\n{perr}")
+    os.replace(PEAK_LIB + ".tmp", PEAK_LIB)
     return LIB
 
 

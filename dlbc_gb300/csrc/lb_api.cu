@@ -380,10 +380,6 @@ int lb_handle_create(const lbgpu_config* cfg, bool lite, double* staging, size_t
     // the fused kernel indexes a component's populations with 32-bit offsets
     h->fused = cfg->precision != LBGPU_FP64 && cfg->q == 19 && !(tk && tk[0] == '1' && !lite) &&
                19 * h->n < (int64_t(1) << 32);
-    // LBGPU_STAGED=1 puts the half form on the cp.async-staged kernel
-    // (bit-identical, slower on GB300: kept for comparison)
-    const char* sg = getenv("LBGPU_STAGED");
-    h->staged = h->fused && !lite && cfg->precision == LBGPU_FP16 && (sg && sg[0] == '1');
   }
   if (lite && !h->fused) {
     *err = "batch members must be FP32/FP16 D3Q19 lattices below 2^32/19 sites";
@@ -403,7 +399,7 @@ int lb_handle_create(const lbgpu_config* cfg, bool lite, double* staging, size_t
   for (int c = 0; c < 2; ++c) {
     const double tau = c < h->C ? cfg->tau[c] : 1.0;
     P.tau[c] = tau;
-    P.omega[c] = 1.0 / tau;               // collision.d:199
+    P.omega[c] = 1.0 / tau;               // collision.d:99
     P.one_minus_omega[c] = 1.0 - P.omega[c];
     P.gwc[c] = c < h->C ? cfg->gwc[c] : 0.0;
     for (int c2 = 0; c2 < 2; ++c2) P.gcc[c][c2] = (c < h->C && c2 < h->C) ? cfg->gcc[c][c2] : 0.0;
@@ -873,7 +869,7 @@ int lbgpu_step(lbgpu_handle* h, int32_t nsteps) {
     else if (h->fused) {
       if (int rc = lb_sync_solids(h, h->cur, h->stream)) return rc;
       e = lbk::launch_fused(h->cfg.precision == LBGPU_FP16, h->C, b, P, h->stream, &h->launches, evp,
-                            h->cfg.device, h->staged);
+                            h->cfg.device);
     } else if (h->cfg.precision == LBGPU_FP32)
       e = lbk::launch_step_f32(h->Q, h->C, b, P, h->stream, &h->launches, evp);
     else

@@ -137,7 +137,7 @@ __device__ __forceinline__ R density(const R* a) {
 }
 
 // sum_q a_q * c_q[vd] in q order, starting from 0 (velocity.d:37-48,
-// collision.d:271-276)
+// collision.d:171-176)
 template <int Q, typename R>
 __device__ __forceinline__ R moment(const R* a, int vd) {
   R s = R(0);

@@ -25,8 +25,8 @@
 //
 // Per-site arithmetic restates the reference (addShanChenForcePsi
 // force.d:238-309, distributeForce force.d:179-197,
-// precalculateWeightedVelocity collision.d:256-296, collideFieldsKernel
-// collision.d:190-219, eqDist eqdist.d:61-278) in float, re-associated where
+// precalculateWeightedVelocity collision.d:156-196, collideFieldsKernel
+// collision.d:90-119, eqDist eqdist.d:61-278) in float, re-associated where
 // that saves work: the Shan-Chen sum of component c1 is
 // -psi_c1 * sum_c2 g_c1c2 * S_c2 with S_c2 = sum_q w_q psi_c2(x + c_q) c_q
 // (the same mathematical value as the reference's per-term products), and
@@ -135,7 +135,7 @@ __device__ __forceinline__ void stencil_acc(float (&acc)[3], int cx, int cy, int
 // Float arithmetic of the fused kernels.  Their translation units are
 // compiled without FMA contraction and every fused multiply-add is written
 // out with fmaf, so the same source expression gives the same bits in every
-// kernel variant (single lattice, batch, populations-free, staged, cluster).
+// kernel variant (single lattice, batch, populations-free).
 
 // S = w_axis * sum_axis + w_diag * sum_diag (w = 1/18, 1/36)
 __device__ __forceinline__ float stencil_weigh(float axis, float diag) {
@@ -229,27 +229,15 @@ __device__ __forceinline__ void fused_gather(const T* const (&fc)[2], const Fuse
 // Process plane-tiles [w0, w1) of one lattice (tile-major: w = tile*nx + x).
 // P may live in the constant bank (single lattice) or in shared memory
 // (batches); every thread of the CTA calls this with the same range.
-// Cluster helpers (the 2 x 2 cluster variant of fused_body, CL = true)
-__device__ __forceinline__ void cluster_sync_all() {
-  asm volatile("barrier.cluster.arrive.release;\n\tbarrier.cluster.wait.acquire;" ::: "memory");
-}
-__device__ __forceinline__ float dsmem_ld(const float* local, uint32_t cta) {
-  uint32_t a = static_cast<uint32_t>(__cvta_generic_to_shared(local)), r;
-  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(cta));
-  float v;
-  asm volatile("ld.shared::cluster.f32 %0, [%1];" : "=f"(v) : "r"(r) : "memory");
-  return v;
-}
-
+//
 // MOM: every tau is 1 and the equilibrium is BDist2, so the collision needs
 // only the density and momentum of each component, not the populations: the
 // gather keeps the three momentum components per component in the population
 // buffer instead of the 19 populations.
-template <typename T, int C, bool WALLS, int TY, bool CL = false, bool MOM = false>
+template <typename T, int C, bool WALLS, int TY, bool MOM = false>
 __device__ __forceinline__ void fused_body(const FusedParams& P, const T* __restrict__ f, T* __restrict__ fout,
                                            const uint32_t* __restrict__ nbmask, double* __restrict__ force_out,
-                                           int64_t w0, int64_t w1, FusedShared<TY, MOM ? 3 : 19>& sh,
-                                           int crank = 0) {
+                                           int64_t w0, int64_t w1, FusedShared<TY, MOM ? 3 : 19>& sh) {
   constexpr int kFusedTY = TY;
   const int t = threadIdx.x;
   const int ty = t / kFusedTZ, tz = t % kFusedTZ;
@@ -268,24 +256,13 @@ __device__ __forceinline__ void fused_body(const FusedParams& P, const T* __rest
     const bool active = ty < tyv && tz < tzv;
     // interior site offsets and this thread's ring site (if any)
     const YZ yz_in = make_yz(y0 + ty, z0 + tz, P);
-    // ring sites this CTA gathers: all of them, or in a 2 x 2 cluster only
-    // its outer row (above for cluster row 0, below for row 1) and outer
-    // column (left for cluster column 0, right for column 1); the rest of
-    // the ring is read from the neighbours' shared memory (share_ring)
-    const int cry = crank >> 1, crz = crank & 1;
-    const int ring = CL ? (tzv + 2) + tyv : 2 * (tzv + 2) + 2 * tyv;
+    // this thread's ring site: the row above, the row below, then the left
+    // and right columns
+    const int ring = 2 * (tzv + 2) + 2 * tyv;
     int rry = 0, rrz = 0;
     const bool has_ring = t < ring;
     if (has_ring) {
-      if (CL) {
-        if (t < tzv + 2) {
-          rry = cry == 0 ? -1 : tyv;
-          rrz = t - 1;
-        } else {
-          rry = t - (tzv + 2);
-          rrz = crz == 0 ? -1 : tzv;
-        }
-      } else if (t < tzv + 2) {
+      if (t < tzv + 2) {
         rry = -1;
         rrz = t - 1;
       } else if (t < 2 * (tzv + 2)) {
@@ -298,42 +275,6 @@ __device__ __forceinline__ void fused_body(const FusedParams& P, const T* __rest
       }
     }
     const YZ yz_ring = make_yz(wrap(y0 + rry, P.ny), wrap(z0 + rrz, P.nz), P);
-    // cluster: copy the ring positions this CTA did not gather (its inner row
-    // and column, with their corners) from the cluster CTA whose interior or
-    // own ring holds them; positions are (row, col) of the [TY+2][TZ+2] arrays
-    auto share_ring = [&](int slot) {
-      if constexpr (CL) {
-        constexpr int RZ = kFusedTZ + 2;
-        for (int k = t; k < 2 * RZ + 2 * TY; k += TY * kFusedTZ) {
-          int r, cc;
-          if (k < RZ) {
-            r = 0;
-            cc = k;
-          } else if (k < 2 * RZ) {
-            r = TY + 1;
-            cc = k - RZ;
-          } else {
-            const int m = k - 2 * RZ;
-            r = 1 + (m >> 1);
-            cc = (m & 1) ? RZ - 1 : 0;
-          }
-          const bool own_row = (cry == 0 && r == 0) || (cry == 1 && r == TY + 1);
-          const bool own_col = r >= 1 && r <= TY && ((crz == 0 && cc == 0) || (crz == 1 && cc == RZ - 1));
-          if (own_row || own_col) continue;
-          // offset from the cluster's origin, the owner and its position
-          const int gy = cry * TY + r - 1, gz = crz * kFusedTZ + cc - 1;
-          const int oy = gy < 0 ? 0 : (gy >= 2 * TY ? 1 : gy / TY);
-          const int oz = gz < 0 ? 0 : (gz >= 2 * kFusedTZ ? 1 : gz / kFusedTZ);
-          const int lr = gy - oy * TY + 1, lc = gz - oz * kFusedTZ + 1;
-          const uint32_t owner = uint32_t(oy * 2 + oz);
-#pragma unroll
-          for (int c = 0; c < C; ++c) {
-            sh.psi[slot][c][r][cc] = dsmem_ld(&sh.psi[slot][c][lr][lc], owner);
-            sh.rho[slot][c][r][cc] = dsmem_ld(&sh.rho[slot][c][lr][lc], owner);
-          }
-        }
-      }
-    };
     // neighbour masks of this thread's interior site at the gathered plane
     // (nbm_next) and at the plane being collided (nbm_cur)
     uint32_t nbm_next = 0, nbm_cur = 0;
@@ -409,11 +350,6 @@ __device__ __forceinline__ void fused_body(const FusedParams& P, const T* __rest
     prefetch(wrap(xs - 1, P.nx));
     gather_plane(0, wrap(xs - 1, P.nx), -1, xs);
     gather_plane(1, xs, 0, wrap(xs + 1, P.nx));
-    if constexpr (CL) {
-      cluster_sync_all();  // the neighbours' psi of xs-1 and xs are complete
-      share_ring(0);
-      share_ring(1);
-    }
     int cur = 0;
     for (int k = 0; k < run; ++k) {
       const int x = xs + k;
@@ -422,10 +358,6 @@ __device__ __forceinline__ void fused_body(const FusedParams& P, const T* __rest
       pw_cur = pw_next;
       __syncthreads();  // psi slot sp and pops buffer 1-cur are free
       gather_plane(sp, wrap(x + 1, P.nx), 1 - cur, wrap(x + 2, P.nx));
-      if constexpr (CL) {
-        cluster_sync_all();  // every cluster CTA's psi of x+1 is complete
-        share_ring(sp);
-      }
       __syncthreads();
       // the collision of plane x, with or without the wall code
       auto collide = [&](auto wtag) {
@@ -510,7 +442,7 @@ __device__ __forceinline__ void fused_body(const FusedParams& P, const T* __rest
 #pragma unroll
             for (int vd = 0; vd < 3; ++vd) force_out[(size_t(c) * P.n + s) * 3 + vd] = double(F[c][vd]);
         }
-        // --- BDist2 weighted velocity (collision.d:256-296); the populations
+        // --- BDist2 weighted velocity (collision.d:156-196); the populations
         // of the last component stay in registers for its collision
         float pop[19];
         float wv[3] = {0.f, 0.f, 0.f};
@@ -585,7 +517,7 @@ __global__ void __launch_bounds__(TY * kFusedTZ, MOM ? (8 / TY) * mom_ctas<WALLS
   if (!P.work_counter) {
     const int64_t w0 = P.work * blockIdx.x / gridDim.x;
     const int64_t w1 = P.work * (blockIdx.x + 1) / gridDim.x;
-    fused_body<T, C, WALLS, TY, false, MOM>(P, f, fout, nbmask, force_out, w0, w1, sh);
+    fused_body<T, C, WALLS, TY, MOM>(P, f, fout, nbmask, force_out, w0, w1, sh);
     return;
   }
   // dynamic: runs of run_len planes of one tile taken from a counter, so
@@ -606,51 +538,8 @@ __global__ void __launch_bounds__(TY * kFusedTZ, MOM ? (8 / TY) * mom_ctas<WALLS
     const int ch = item / ntl, tile = item - ch * ntl;
     const int64_t w0 = int64_t(tile) * P.nx + int64_t(ch) * P.run_len;
     const int64_t w1 = min(w0 + P.run_len, int64_t(tile + 1) * P.nx);
-    fused_body<T, C, WALLS, TY, false, MOM>(P, f, fout, nbmask, force_out, w0, w1, sh);
+    fused_body<T, C, WALLS, TY, MOM>(P, f, fout, nbmask, force_out, w0, w1, sh);
   }
-}
-
-// The single-lattice step in 2 x 2 clusters of 8 x 32 tiles (a 16 x 64 cluster
-// tile; ny % 16 == 0, nz % 64 == 0): each CTA gathers only the outer half of
-// its ring and reads the inner half from its cluster neighbours' shared
-// memory.  Clusters take runs of run_len planes of one cluster tile from
-// `counter`, in step (a cluster barrier per plane).
-template <typename T, int C, bool WALLS>
-__global__ void __cluster_dims__(4, 1, 1) __launch_bounds__(8 * kFusedTZ, 2)
-    k_fused_cluster(const T* __restrict__ f, T* __restrict__ fout, const uint32_t* __restrict__ nbmask,
-                    double* __restrict__ force_out, FusedParams P, int* __restrict__ counter) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  FusedShared<8>& sh = *reinterpret_cast<FusedShared<8>*>(smem_raw);
-  __shared__ int s_item;
-  uint32_t crank;
-  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(crank));
-  const int ctz = P.tiles_z / 2, cty = P.tiles_y / 2;
-  const int nch = (P.nx + P.run_len - 1) / P.run_len;
-  const int units = cty * ctz * nch;
-  __shared__ int s_mine;
-  for (;;) {
-    if (crank == 0 && threadIdx.x == 0) s_item = atomicAdd(counter, 1);
-    cluster_sync_all();
-    if (threadIdx.x == 0) {
-      const uint32_t a = static_cast<uint32_t>(__cvta_generic_to_shared(&s_item));
-      uint32_t r;
-      int v;
-      asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(0u));
-      asm volatile("ld.shared::cluster.s32 %0, [%1];" : "=r"(v) : "r"(r) : "memory");
-      s_mine = v;
-    }
-    cluster_sync_all();  // every CTA has its copy before rank 0 takes the next item
-    const int item = s_mine;
-    if (item >= units) break;
-    const int ncu = cty * ctz;
-    const int ch = item / ncu, cu = item - ch * ncu;  // x-chunk-major, as k_fused
-    const int tile = ((cu / ctz) * 2 + int(crank >> 1)) * P.tiles_z + (cu % ctz) * 2 + int(crank & 1);
-    const int xs = ch * P.run_len;
-    const int run = min(P.run_len, P.nx - xs);
-    const int64_t w0 = int64_t(tile) * P.nx + xs;
-    fused_body<T, C, WALLS, 8, true>(P, f, fout, nbmask, force_out, w0, w0 + run, sh, int(crank));
-  }
-  cluster_sync_all();  // no CTA leaves while a neighbour may still read its shared memory
 }
 
 // One simulation of a batch.  The step reads populations f[(parity + phase)
@@ -735,7 +624,7 @@ __global__ void __launch_bounds__(TY * kFusedTZ, 8 / TY * 2 > 4 ? 4 : 8 / TY * 2
     // tau = 1 BDist2 members take the populations-free collision (the same
     // bits as the general body, with fewer instructions)
     if (C == 2 && Ps.unit_tau && Ps.eq_form == 2)
-      fused_body<T, C, WALLS, TY, false, true>(Ps, fin, fout, sims[i].nbmask, sims[i].force_out, r0 - wb, r1 - wb,
+      fused_body<T, C, WALLS, TY, true>(Ps, fin, fout, sims[i].nbmask, sims[i].force_out, r0 - wb, r1 - wb,
                                                *reinterpret_cast<FusedShared<TY, 3>*>(smem_raw));
     else
       fused_body<T, C, WALLS, TY>(Ps, fin, fout, sims[i].nbmask, sims[i].force_out, r0 - wb, r1 - wb, sh);

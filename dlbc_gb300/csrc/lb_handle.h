@@ -58,9 +58,6 @@ struct lbgpu_handle {
   // FP32/FP16 D3Q19 run the fused single-pass kernel; LBGPU_TWO_KERNEL=1 in
   // the environment at lbgpu_create selects the two-kernel step instead
   bool fused = false;
-  // LBGPU_STAGED=1: the FP16 form uses the cp.async-staged kernel where the
-  // lattice qualifies
-  bool staged = false;
   // The fused step does not write solid sites, so both population buffers
   // must hold their (constant) populations: false after an upload, a device
   // initialisation or a mask change, until lb_sync_solids copies the

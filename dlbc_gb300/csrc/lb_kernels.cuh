@@ -9,7 +9,7 @@
 //                   BDist2 weighted velocity, BGK collision with force shift
 //                   (addShanChenForcePsi force.d:238-309, distributeForce
 //                    force.d:179-197, precalculateWeightedVelocity
-//                    collision.d:256-296, collideFieldsKernel collision.d:190-219)
+//                    collision.d:156-196, collideFieldsKernel collision.d:90-119)
 //
 // Storage is SoA: f[c][q][site], site = (x*NY + y)*NZ + z, z contiguous.
 // Solid sites are neither streamed nor collided: their populations are
@@ -287,7 +287,7 @@ __global__ void __launch_bounds__(128, 3) k_collide(const T* __restrict__ f, T* 
       load_local<T, R, Q>(f, s, c, P, pop[c]);
   }
 
-  // --- BDist2 weighted velocity (collision.d:256-296)
+  // --- BDist2 weighted velocity (collision.d:156-196)
   R wv[3] = {R(0), R(0), R(0)};
   const bool unit = P.unit_tau != 0;
   if (P.eq_form == 2) {
@@ -304,7 +304,7 @@ __global__ void __launch_bounds__(128, 3) k_collide(const T* __restrict__ f, T* 
     for (int vd = 0; vd < D; ++vd) wv[vd] = by_tot.div(wv[vd]);
   }
 
-  // --- collision (collision.d:198-218)
+  // --- collision (collision.d:98-118)
 #pragma unroll
   for (int c = 0; c < C; ++c) {
     const R tau = R(P.tau[c]);

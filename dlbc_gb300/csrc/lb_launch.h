@@ -63,12 +63,9 @@ cudaError_t launch_phase_f16(int phase, int q, int c, const StepBuffers& b, cons
 namespace lbk {
 
 // Fused single-pass D3Q19 step (lb_fused.cuh) for the float-arithmetic
-// forms.  `half_storage` selects half offsets instead of float storage;
-// `staged` lets the half form use the cp.async-staged kernel (lb_staged.cuh)
-// where the lattice qualifies (staged_eligible).
+// forms.  `half_storage` selects half offsets instead of float storage.
 cudaError_t launch_fused(bool half_storage, int c, const StepBuffers& b, const StepParams& P, cudaStream_t stream,
-                         int64_t* launches, const StepEvents* ev, int device, bool staged);
-bool staged_eligible(const StepParams& P, int c, bool half_storage);
+                         int64_t* launches, const StepEvents* ev, int device);
 
 }  // namespace lbk
 

@@ -12,6 +12,11 @@
 // scratch (the densities and psi values the Shan-Chen stencil reads) lives in
 // the file-scope array below.
 //
+// FP32 runs the two-kernel float step (the step lbgpu_create selects with
+// LBGPU_TWO_KERNEL=1), not the fused single-pass kernel lbgpu_step runs for
+// FP32 D3Q19 by default, so its FP32 populations agree with lbgpu_step's
+// within the FP32 form's rounding, not bit for bit; FP64 agrees bit for bit.
+//
 // Scratch: kNoallocScratchBytes (64 MiB) of static device memory.  Every GPU
 // that loads this library holds that array until the process exits.  The
 // timestep needs components * 2 values per site of the arithmetic type
@@ -120,6 +125,11 @@ extern "C" int lbgpu_step_noalloc(const lbgpu_config* cfg, const void* f_in, voi
   P.psi_form = cfg->psi_form;
   P.eq_form = cfg->eq_form;
   P.record_force = 0;
+  // every tau == 1: the relaxation is the equilibrium itself (the exact
+  // shortcut lbgpu_create enables for the same configuration)
+  P.unit_tau = 1;
+  for (int c = 0; c < C; ++c)
+    if (cfg->tau[c] != 1.0) P.unit_tau = 0;
   for (int c = 0; c < 2; ++c) {
     const double tau = c < C ? cfg->tau[c] : 1.0;
     P.tau[c] = tau;

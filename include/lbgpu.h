@@ -8,8 +8,8 @@
  *   L.resetForce();          // src/dlbc/lb/force.d:165
  *   L.addShanChenForce();    // src/dlbc/lb/force.d:223
  *   L.distributeForce();     // src/dlbc/lb/force.d:179
- *   L.prepareToCollide();    // src/dlbc/lb/collision.d:141
- *   L.collideFields(tau, globalAcc);   // src/dlbc/lb/collision.d:161
+ *   L.prepareToCollide();    // src/dlbc/lb/collision.d:41
+ *   L.collideFields(tau, globalAcc);   // src/dlbc/lb/collision.d:61
  *
  * lbgpu_step() replaces that whole sequence (halo exchange becomes periodic
  * index wrap on one in-GPU domain).  The lattice fields stay resident on the
@@ -209,10 +209,12 @@ int lbgpu_kernel_time(lbgpu_handle* h, int32_t which, double* total_ms, int64_t*
  * owns the GPU, or a caller that cannot take cudaMalloc's implicit device
  * synchronisation while its other streams run).  The caller passes device
  * pointers: f_in and f_out hold the populations in the kernels' SoA layout,
- * element [c][q][site] with site = (x*gn[1] + y)*gn[2] + z (D2Q9: x*gn[1] + y;
- * D1Q3/D1Q5: x),
- * as doubles (LBGPU_FP64) or floats (LBGPU_FP32); mask is uint8 [site]
- * (nonzero = solid) or NULL.  The work is queued on `stream` (a cudaStream_t,
+ * element [c][q][site] with site = (x*gn[1] + y)*gn[2] + z (D3Q19) or
+ * x*gn[1] + y (D2Q9; the only two connectivities accepted), as doubles
+ * (LBGPU_FP64) or floats (LBGPU_FP32); mask is uint8 [site] (nonzero =
+ * solid) or NULL.  FP64 gives lbgpu_step's populations bit for bit; FP32 runs
+ * the two-kernel float step, so it agrees with lbgpu_step's fused FP32 step
+ * within the FP32 form's rounding, not bit for bit.  The work is queued on `stream` (a cudaStream_t,
  * NULL for the legacy default stream) and `cfg->device` is used.
  * The psi/density scratch is a 64 MiB static device array that every GPU
  * loading this library holds until exit, so at most 64 MiB /

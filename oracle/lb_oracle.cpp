@@ -298,7 +298,7 @@ void forces(or_lattice& L) {
   });
 }
 
-// precalculateWeightedVelocity (src/dlbc/lb/collision.d:256-296)
+// precalculateWeightedVelocity (src/dlbc/lb/collision.d:156-196)
 void weighted_velocity(or_lattice& L) {
   const int q = L.q, d = L.d, C = L.C;
   for_physical(L, [&](long, long, long, long i) {
@@ -429,7 +429,7 @@ void eq_dist(const or_lattice& L, const double* pop, const double* dv, double rh
   }
 }
 
-// collideFieldsKernel (src/dlbc/lb/collision.d:190-219)
+// collideFieldsKernel (src/dlbc/lb/collision.d:90-119)
 void collide(or_lattice& L) {
   const int q = L.q, d = L.d;
   for (int f = 0; f < L.C; ++f) {
@@ -751,7 +751,7 @@ void or_run(or_lattice* L, int nsteps) {
     advect(*L);                  // main.d:182
     densities_and_psi(*L);       // precalculatePsi inside addShanChenForcePsi (force.d:250)
     forces(*L);                  // main.d:188-191
-    if (L->cfg.eq_form == 2) weighted_velocity(*L);  // prepareToCollide (collision.d:141-151)
+    if (L->cfg.eq_form == 2) weighted_velocity(*L);  // prepareToCollide (collision.d:41-51)
     collide(*L);                 // main.d:195
   }
 }

@@ -1,9 +1,9 @@
 #!/usr/bin/env python3
 """Turn the reference's HDF5 golden files into small committed fixtures.
 
-Run from the repository root with the reference checkout available:
+Run from the repository root with the path of a reference checkout:
 
-    python tests/golden/make_fixtures.py /root/reference [case ...]
+    python tests/golden/make_fixtures.py <reference checkout> [case ...]
 
 For every case it stores, in ``tests/golden/<case>.npz``:
 
@@ -171,5 +171,7 @@ def main(ref: str, only=()):
 
 
 if __name__ == "__main__":
+    if len(sys.argv) < 2:
+        sys.exit("usage: make_fixtures.py <reference checkout> [case ...]")
     # optional further arguments: only these cases (the rest are left as they are)
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference", tuple(sys.argv[2:]))
+    main(sys.argv[1], tuple(sys.argv[2:]))

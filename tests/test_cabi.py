@@ -94,3 +94,27 @@ def test_header_compiles_links_and_runs_from_c_and_cpp(libpath, tmp_path, lang):
                     "-L", libdir, "-llbgpu", f"-Wl,-rpath,{libdir}"], check=True, capture_output=True)
     out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()
     assert out == ["1", "-1", "1", "msg"], out
+
+
+def test_noalloc_rejects_lattices_beyond_the_scratch(libpath):
+    """lbgpu_step_noalloc refuses a lattice whose scratch does not fit its
+    static 64 MiB array before any device work (so it runs without a GPU)."""
+    from lbcases import spinodal
+    fn = lbgpu.lib().lbgpu_step_noalloc
+    fn.argtypes = [ctypes.POINTER(lbgpu.LbgpuConfig), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                   ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t]
+    fn.restype = ctypes.c_int
+    err = ctypes.create_string_buffer(512)
+    # 256 x 128 x 128 two-component FP64 needs 128 MiB of scratch; 256 x 256 x 128 FP32 the same
+    cfg = lbgpu.make_config(spinodal((256, 128, 128)), precision=lbgpu.FP64, device=0)
+    rc = fn(ctypes.byref(cfg), ctypes.c_void_p(16), ctypes.c_void_p(32), None, None, err, len(err))
+    assert rc == -1
+    assert b"scratch" in err.value
+    cfg = lbgpu.make_config(spinodal((256, 256, 128)), precision=lbgpu.FP32, device=0)
+    rc = fn(ctypes.byref(cfg), ctypes.c_void_p(16), ctypes.c_void_p(32), None, None, err, len(err))
+    assert rc == -1
+    assert b"scratch" in err.value
+    # a configuration the entry point does not support is refused the same way
+    cfg = lbgpu.make_config(spinodal((8, 8, 8)), precision=lbgpu.FP16, device=0)
+    rc = fn(ctypes.byref(cfg), ctypes.c_void_p(16), ctypes.c_void_p(32), None, None, err, len(err))
+    assert rc == -1

@@ -294,116 +294,6 @@ def test_reduced_precision_through_phase_separation(precision):
     assert phase < 0.05, phase
 
 
-def _run_half(p, steps, staged, record_force=False):
-    import os
-    old = os.environ.get("LBGPU_STAGED")
-    os.environ["LBGPU_STAGED"] = "1" if staged else "0"
-    try:
-        fl, m = init.init_fields(p)
-        g = lbgpu.GPULattice(p, precision=lbgpu.FP16)
-    finally:
-        if old is None:
-            del os.environ["LBGPU_STAGED"]
-        else:
-            os.environ["LBGPU_STAGED"] = old
-    g.upload(fl, m)
-    if record_force:
-        g.set_record_force(True)
-    g.step(steps)
-    return g.population(), (g.force() if record_force else None)
-
-
-@pytest.mark.parametrize("case", ["spinodal", "walls", "wall-force", "small-y", "nz8", "nz40", "one-component"])
-def test_staged_half_kernel_matches_unstaged(case):
-    """The cp.async-staged FP16 kernel does the unstaged fused kernel's per-site
-    arithmetic on the same values: bit-identical populations and forces,
-    including periodic wrap of the staged rows (nz = 8, 40), partial tiles
-    and bounce-back next to walls."""
-    if case == "spinodal":
-        p = spinodal((24, 20, 64), perturb=0.03)
-    elif case == "walls":
-        p = droplet_channel((20, 18, 32), radius=5.0, acc=1e-3)
-    elif case == "wall-force":
-        p = droplet_channel((12, 10, 48), radius=3.0, acc=1e-3, gwc=(0.25, -0.15))
-    elif case == "small-y":
-        p = spinodal((9, 3, 16), perturb=0.03)
-    elif case == "nz8":
-        p = spinodal((6, 11, 8), perturb=0.03)
-    elif case == "nz40":
-        p = droplet_channel((10, 13, 40), radius=3.0, acc=1e-3)
-    else:
-        p = spinodal((10, 12, 32), perturb=0.03)
-        p.components = 1
-        p.field_names = p.field_names[:1]
-        p.tau = p.tau[:1]
-        p.gcc = [[0.0]]
-        p.gwc = p.gwc[:1]
-        p.fluid_init = p.fluid_init[:1]
-        p.fluid_densities = p.fluid_densities[:1]
-        p.fluid_perturb = p.fluid_perturb[:1]
-        p.random_reseed = p.random_reseed[:1]
-        p.random_seed = p.random_seed[:1]
-    a, fa = _run_half(p, 23, staged=True, record_force=True)
-    b, fb = _run_half(p, 23, staged=False, record_force=True)
-    for c in range(p.components):
-        assert np.array_equal(a[c], b[c]), (c, np.abs(a[c] - b[c]).max())
-        assert np.array_equal(fa[c], fb[c], equal_nan=True)
-
-
-def _run_env(p, steps, precision, env, record_force=True):
-    import os
-    old = {k: os.environ.get(k) for k in env}
-    os.environ.update(env)
-    try:
-        fl, m = init.init_fields(p)
-        g = lbgpu.GPULattice(p, precision=precision)
-        g.upload(fl, m)
-        if record_force:
-            g.set_record_force(True)
-        g.step(steps)
-        return g.population(), g.force()
-    finally:
-        for k, v in old.items():
-            if v is None:
-                del os.environ[k]
-            else:
-                os.environ[k] = v
-
-
-@pytest.mark.parametrize("precision", [lbgpu.FP32, lbgpu.FP16])
-@pytest.mark.parametrize("case", ["spinodal", "walls"])
-def test_cluster_kernel_matches_single_cta_kernel(precision, case):
-    """The 2 x 2 cluster variant of the fused step reads half of each tile's
-    ring from its neighbours' shared memory instead of gathering it: the same
-    values, so bit-identical populations and forces (periodic wrap of the
-    cluster's outer ring, walls and the wall force included)."""
-    import subprocess
-    import sys
-    if case == "spinodal":
-        p = spinodal((20, 32, 64), perturb=0.03)
-    else:
-        p = droplet_channel((18, 48, 128), radius=6.0, acc=1e-3, gwc=(0.25, -0.15))
-    # LBGPU_CLUSTER is read once per process: run the cluster form in a child
-    code = (
-        "import sys, numpy as np; sys.path[:0] = ['tests', '.']\n"
-        "from test_gpu_parity import _run_env, spinodal, droplet_channel, lbgpu\n"
-        f"p = spinodal((20, 32, 64), perturb=0.03) if {case!r} == 'spinodal' else "
-        "droplet_channel((18, 48, 128), radius=6.0, acc=1e-3, gwc=(0.25, -0.15))\n"
-        f"pop, fo = _run_env(p, 21, {precision}, {{}})\n"
-        "np.savez(sys.argv[1], *pop, *fo)\n")
-    import tempfile
-    with tempfile.TemporaryDirectory() as d:
-        out = f"{d}/cluster.npz"
-        env = dict(__import__("os").environ, LBGPU_CLUSTER="1")
-        subprocess.run([sys.executable, "-c", code, out], check=True, env=env)
-        z = np.load(out)
-        single = [z[f"arr_{i}"] for i in range(4)]
-    pop, fo = _run_env(p, 21, precision, {})  # this process: single-CTA tiles
-    for c in range(2):
-        assert np.array_equal(pop[c], single[c])
-        assert np.array_equal(fo[c], single[2 + c], equal_nan=True)
-
-
 @pytest.mark.parametrize("precision", [lbgpu.FP32, lbgpu.FP16])
 def test_fused_step_leaves_solid_sites_unchanged(precision):
     """The fused step writes fluid sites only; both population buffers hold
