@@ -17,6 +17,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <cmath>
 #include <string>
 #include <vector>
 
@@ -30,6 +31,24 @@ constexpr size_t kStagingBytes = size_t(256) << 20;
 thread_local std::string g_create_error;
 
 size_t storage_size(int precision) { return precision == LBGPU_FP64 ? 8 : precision == LBGPU_FP32 ? 4 : 2; }
+
+int storage_kind(int precision) {
+  return precision == LBGPU_FP16 ? lbk::kStoreF16 : precision == LBGPU_I16 ? lbk::kStoreI16 : lbk::kStoreF32;
+}
+
+}  // namespace
+
+// I16: 16-bit fixed point over offsets up to 3 max(rho0, initial spread)
+// from rho0, i.e. f/w from -2 rho0 to 4 rho0 for a lattice that starts near
+// rho0: phase separation (a Shan-Chen component's dense phase about twice
+// its mean density) and the force-shifted equilibrium's velocity terms stay
+// inside; values beyond saturate
+double i16_scale(double rho0, double maxdev) {
+  const double range = 3.0 * std::max(fabs(rho0), maxdev);
+  return range > 0.0 ? range / 32767.0 : 1.0 / 32767.0;
+}
+
+namespace {
 size_t arith_size(int precision) { return precision == LBGPU_FP64 ? 8 : 4; }
 
 }  // namespace
@@ -58,6 +77,13 @@ __device__ __forceinline__ __half to_storage<__half>(double v, int q, int c, con
   return __float2half_rn((float(v) * (1.0f / wq(Q, q)) - P.rho0[c]) * P.inv_scale[c]);
 }
 
+// I16: round((f/w - rho0) / scale), saturated to +-32767
+template <>
+__device__ __forceinline__ int16_t to_storage<int16_t>(double v, int q, int c, const StepParams& P, int Q) {
+  const int h = __float2int_rn((float(v) * (1.0f / wq(Q, q)) - P.rho0[c]) * P.inv_scale[c]);
+  return int16_t(h < -32767 ? -32767 : (h > 32767 ? 32767 : h));
+}
+
 template <typename T>
 __device__ __forceinline__ double from_storage(T v, int q, int c, const StepParams& P, int Q);
 template <>
@@ -72,6 +98,10 @@ template <>
 __device__ __forceinline__ double from_storage<__half>(__half v, int q, int c, const StepParams& P, int Q) {
   return double(wq(Q, q) * fmaf(P.scale[c], __half2float(v), P.rho0[c]));
 }
+template <>
+__device__ __forceinline__ double from_storage<int16_t>(int16_t v, int q, int c, const StepParams& P, int Q) {
+  return double(wq(Q, q) * fmaf(P.scale[c], float(v), P.rho0[c]));
+}
 
 struct Geo {
   int nx, ny, nz, nxh, nyh, nzh, hy, hz, Q;  // hy, hz: halo in y, z (0 where the lattice has no such axis)
@@ -79,9 +109,12 @@ struct Geo {
 };
 
 // AoS haloed staging (haloed x-planes [xh0, xh0 + nplanes)) -> SoA physical
+// AoS haloed staging -> SoA physical; with f_solid (and mask), solid sites are
+// written into f_solid as well (the fused steps do not write solid sites, so
+// both population buffers must hold them)
 template <typename T>
 __global__ void k_upload(const double* __restrict__ stage, T* __restrict__ f, int c, int xh0, int nplanes, Geo g,
-                         StepParams P) {
+                         StepParams P, T* __restrict__ f_solid = nullptr, const uint8_t* __restrict__ mask = nullptr) {
   const int64_t per_plane = int64_t(g.ny) * g.nz;
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= per_plane * nplanes) return;
@@ -94,7 +127,12 @@ __global__ void k_upload(const double* __restrict__ stage, T* __restrict__ f, in
   const double* src = stage + ((int64_t(pl) * g.nyh + (y + g.hy)) * g.nzh + (z + g.hz)) * g.Q;
   const int64_t site = (int64_t(x) * g.ny + y) * g.nz + z;
   T* fc = f + int64_t(c) * g.Q * g.n;
-  for (int q = 0; q < g.Q; ++q) fc[int64_t(q) * g.n + site] = to_storage<T>(src[q], q, c, P, g.Q);
+  T* fs = (f_solid && mask && mask[site]) ? f_solid + int64_t(c) * g.Q * g.n : nullptr;
+  for (int q = 0; q < g.Q; ++q) {
+    const T v = to_storage<T>(src[q], q, c, P, g.Q);
+    fc[int64_t(q) * g.n + site] = v;
+    if (fs) fs[int64_t(q) * g.n + site] = v;
+  }
 }
 
 // SoA physical -> AoS haloed staging (halo sites get periodic images)
@@ -312,8 +350,12 @@ int validate(const lbgpu_config* c, std::string* why) {
     *why = "lattice larger than 2^31 sites";
     return LBGPU_E_INVALID;
   }
-  if (c->precision < LBGPU_FP64 || c->precision > LBGPU_FP16) {
+  if (c->precision < LBGPU_FP64 || c->precision > LBGPU_I16) {
     *why = "unknown precision";
+    return LBGPU_E_INVALID;
+  }
+  if (c->precision == LBGPU_I16 && !(c->d == 3 && c->q == 19 && c->gn[2] % 2 == 0 && c->eq_form == LBGPU_EQ_BDIST2)) {
+    *why = "the I16 form runs D3Q19 lattices with an even z extent and the BDist2 equilibrium";
     return LBGPU_E_INVALID;
   }
   if (c->eq_form < 0 || c->eq_form > 2 || c->psi_form < 0 || c->psi_form > 1) {
@@ -378,8 +420,13 @@ int lb_handle_create(const lbgpu_config* cfg, bool lite, double* staging, size_t
   {
     const char* tk = getenv("LBGPU_TWO_KERNEL");
     // the fused kernel indexes a component's populations with 32-bit offsets
-    h->fused = cfg->precision != LBGPU_FP64 && cfg->q == 19 && !(tk && tk[0] == '1' && !lite) &&
-               19 * h->n < (int64_t(1) << 32);
+    h->fused = cfg->precision != LBGPU_FP64 && cfg->q == 19 &&
+               (cfg->precision == LBGPU_I16 || !(tk && tk[0] == '1' && !lite)) && 19 * h->n < (int64_t(1) << 32);
+  }
+  if (cfg->precision == LBGPU_I16 && !h->fused) {
+    *err = "the I16 form needs fewer than 2^32/19 sites";
+    delete h;
+    return LBGPU_E_INVALID;
   }
   if (lite && !h->fused) {
     *err = "batch members must be FP32/FP16 D3Q19 lattices below 2^32/19 sites";
@@ -472,8 +519,9 @@ int lb_handle_create(const lbgpu_config* cfg, bool lite, double* staging, size_t
 int64_t lb_member_bytes(const lbgpu_config* cfg) {
   int64_t n = 1;
   for (int i = 0; i < cfg->d; ++i) n *= cfg->gn[i];
-  // populations (two buffers), mask byte and 32-bit neighbour mask
-  return 2 * int64_t(cfg->components) * cfg->q * n * int64_t(storage_size(cfg->precision)) + 5 * n;
+  // populations (two buffers), mask byte, 32-bit neighbour mask and the
+  // pair step's row wall flags (at most one byte per two sites)
+  return 2 * int64_t(cfg->components) * cfg->q * n * int64_t(storage_size(cfg->precision)) + 5 * n + n / 2 + 1;
 }
 
 // Neighbour mask of every site: bit 0 the site's own solid flag, bit q the
@@ -520,6 +568,19 @@ __global__ void k_tile_walls(const uint32_t* __restrict__ nbm, uint8_t* __restri
   out[i] = any != 0;
 }
 
+// Wall flag of every (x, y, 64-site z segment) for the pair step: 1 if a
+// site of the segment has a nonzero neighbour mask.
+__global__ void k_row_walls(const uint32_t* __restrict__ nbm, uint8_t* __restrict__ out, Geo g, int segs) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= int64_t(g.nx) * g.ny * segs) return;
+  const int64_t row = i / segs;
+  const int z0 = int(i - row * segs) * lbk::kPairTZ;
+  const int z1 = min(z0 + lbk::kPairTZ, g.nz);
+  uint32_t any = 0;
+  for (int z = z0; z < z1; ++z) any |= nbm[row * g.nz + z];
+  out[i] = any != 0;
+}
+
 int lb_sync_solids(lbgpu_handle* h, int cur, cudaStream_t st) {
   if (!h->mask || !h->fused || h->solids_synced) return LBGPU_OK;
   cudaError_t e = cudaMemcpyAsync(h->f[1 - cur], h->f[cur], h->fbytes, cudaMemcpyDeviceToDevice, st);
@@ -533,7 +594,14 @@ int lb_update_nbmask(lbgpu_handle* h) {
   const bool want = h->mask && (h->fused || h->lite) && h->Q == 19;
   const int tiles_y = (h->ny + 7) / 8, tiles_z = (h->nz + 31) / 32;
   const int64_t nflags = int64_t(h->nx) * tiles_y * tiles_z;
+  const int segs = (h->nz + lbk::kPairTZ - 1) / lbk::kPairTZ;
+  const int64_t nrow = int64_t(h->nx) * h->ny * segs;
   if (!want) {
+    if (h->row_walls) {
+      cudaFree(h->row_walls);
+      h->device_bytes -= nrow;
+      h->row_walls = nullptr;
+    }
     if (h->nbmask) {
       cudaFree(h->nbmask);
       h->device_bytes -= 4 * h->n;
@@ -559,6 +627,19 @@ int lb_update_nbmask(lbgpu_handle* h) {
   h->launches++;
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return h->cuda_fail(e, "neighbour mask kernel");
+  if (!h->row_walls) {
+    e = cudaMalloc(&h->row_walls, size_t(nrow));
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      h->row_walls = nullptr;
+      return h->fail(LBGPU_E_NOMEM, "row wall flags allocation failed");
+    }
+    h->device_bytes += nrow;
+  }
+  k_row_walls<<<unsigned(ceil_div(nrow, 128)), 128, 0, h->stream>>>(h->nbmask, h->row_walls, geo_of(h), segs);
+  h->launches++;
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return h->cuda_fail(e, "row wall flags kernel");
   if (h->lite) return LBGPU_OK;  // batch members use other tile shapes
   if (!h->tile_walls) {
     e = cudaMalloc(&h->tile_walls, size_t(nflags));
@@ -615,6 +696,7 @@ void lbgpu_destroy(lbgpu_handle* h) {
   if (h->mask) cudaFree(h->mask);
   if (h->nbmask) cudaFree(h->nbmask);
   if (h->tile_walls) cudaFree(h->tile_walls);
+  if (h->row_walls) cudaFree(h->row_walls);
   if (h->work_counter) cudaFree(h->work_counter);
   if (h->force) cudaFree(h->force);
   for (auto& e : h->ev_pending)
@@ -690,8 +772,9 @@ int lbgpu_upload(lbgpu_handle* h, const double* const* fluids, const int32_t* ma
   cudaError_t e;
   const size_t plane_vals = size_t(h->nyh) * h->nzh * h->Q;
 
-  // FP16 offset storage: rest density and scale per component
-  if (h->cfg.precision == LBGPU_FP16) {
+  // FP16 / I16 offset storage: rest density and scale per component (unless
+  // the caller pinned them, lbgpu_set_storage_scale)
+  if ((h->cfg.precision == LBGPU_FP16 || h->cfg.precision == LBGPU_I16) && !h->scale_pinned) {
     for (int c = 0; c < h->C; ++c) {
       double rho0 = h->cfg.rho0[c];
       double maxdev = 0.0;
@@ -723,8 +806,13 @@ int lbgpu_upload(lbgpu_handle* h, const double* const* fluids, const int32_t* ma
       // range.  Offsets up to 64 * max(rho0, 4 * initial spread) stay finite,
       // so phase separation, which moves densities far beyond their initial
       // spread, cannot overflow; offsets below 6e-8 of that lose precision.
-      const double span = std::max(fabs(rho0), 4.0 * maxdev);
-      const double scale = span > 0.0 ? span / 1024.0 : 1.0 / 4096.0;
+      double scale;
+      if (h->cfg.precision == LBGPU_FP16) {
+        const double span = std::max(fabs(rho0), 4.0 * maxdev);
+        scale = span > 0.0 ? span / 1024.0 : 1.0 / 4096.0;
+      } else {
+        scale = i16_scale(rho0, maxdev);
+      }
       h->P.rho0[c] = float(rho0);
       h->P.scale[c] = float(scale);
       h->P.inv_scale[c] = float(1.0 / scale);
@@ -757,6 +845,8 @@ int lbgpu_upload(lbgpu_handle* h, const double* const* fluids, const int32_t* ma
         e = launch_upload<double>(h, stage, c, xh0, np);
       else if (h->cfg.precision == LBGPU_FP32)
         e = launch_upload<float>(h, stage, c, xh0, np);
+      else if (h->cfg.precision == LBGPU_I16)
+        e = launch_upload<int16_t>(h, stage, c, xh0, np);
       else
         e = launch_upload<__half>(h, stage, c, xh0, np);
       if (e != cudaSuccess) return h->cuda_fail(e, "upload kernel");
@@ -794,6 +884,8 @@ static int run_phase(lbgpu_handle* h, int phase) {
   if (!h) return LBGPU_E_INVALID;
   if (!h->uploaded) return h->fail(LBGPU_E_NOTREADY, "timestep phase before lbgpu_upload");
   if (h->lite || !h->rho) return h->fail(LBGPU_E_INVALID, "batch members step with their batch");
+  if (h->cfg.precision == LBGPU_I16)
+    return h->fail(LBGPU_E_INVALID, "the I16 form has no split timestep (use lbgpu_step)");
   if (phase == lbk::kPhaseAdvect && h->advected)
     return h->fail(LBGPU_E_NOTREADY, "lbgpu_advect twice: lbgpu_collide completes the timestep");
   if (phase == lbk::kPhaseCollide && !h->advected)
@@ -838,6 +930,7 @@ int lbgpu_step(lbgpu_handle* h, int32_t nsteps) {
     b.mask = h->mask;
     b.nbmask = h->nbmask;
     b.tile_walls = h->tile_walls;
+    b.row_walls = h->row_walls;
     b.work_counter = h->work_counter;
     b.rho = h->rho;
     b.psi = h->psi;
@@ -868,7 +961,7 @@ int lbgpu_step(lbgpu_handle* h, int32_t nsteps) {
       e = lbk::launch_step_f64(h->Q, h->C, b, P, h->stream, &h->launches, evp);
     else if (h->fused) {
       if (int rc = lb_sync_solids(h, h->cur, h->stream)) return rc;
-      e = lbk::launch_fused(h->cfg.precision == LBGPU_FP16, h->C, b, P, h->stream, &h->launches, evp,
+      e = lbk::launch_fused(storage_kind(h->cfg.precision), h->C, b, P, h->stream, &h->launches, evp,
                             h->cfg.device);
     } else if (h->cfg.precision == LBGPU_FP32)
       e = lbk::launch_step_f32(h->Q, h->C, b, P, h->stream, &h->launches, evp);
@@ -903,6 +996,8 @@ int lbgpu_download(lbgpu_handle* h, double* const* fluids) {
         e = launch_download<double>(h, stage, c, xh0, np);
       else if (h->cfg.precision == LBGPU_FP32)
         e = launch_download<float>(h, stage, c, xh0, np);
+      else if (h->cfg.precision == LBGPU_I16)
+        e = launch_download<int16_t>(h, stage, c, xh0, np);
       else
         e = launch_download<__half>(h, stage, c, xh0, np);
       if (e != cudaSuccess) return h->cuda_fail(e, "download kernel");
@@ -962,8 +1057,11 @@ int wave_planes(const lbgpu_handle* h) {
 // `in`.  Staging slots: [0, 4) upload (parity, component), [4, 8) download.
 // Events: 0 start, 1-2 upload slot filled, 3-4 upload slot free, 5-6
 // download slot filled, 7-8 download slot free.
+extern "C++" {
+template <typename T>
 int step_host_wave(lbgpu_handle* h, const double* const* in, double* const* out, int K) {
   const Geo g = geo_of(h);
+  const bool fp64 = h->cfg.precision == LBGPU_FP64;
   const size_t plane_vals = size_t(h->nyh) * h->nzh * h->Q;
   const size_t plane_bytes = plane_vals * sizeof(double);
   const int64_t plane_sites = int64_t(h->ny) * h->nz;
@@ -974,12 +1072,16 @@ int step_host_wave(lbgpu_handle* h, const double* const* in, double* const* out,
   cudaEvent_t* ev = h->pipe_ev;
   const int R = reach_x(h->Q);
   const int nx = h->nx;
-  double* fin = static_cast<double*>(h->f[h->cur]);
-  const double* fout = static_cast<const double*>(h->f[1 - h->cur]);
+  T* fin = static_cast<T*>(h->f[h->cur]);
+  T* fout = static_cast<T*>(h->f[1 - h->cur]);
   lbk::StepBuffers b;
   b.f = h->f[h->cur];
   b.fout = h->f[1 - h->cur];
   b.mask = h->mask;
+  b.nbmask = h->nbmask;
+  b.tile_walls = h->tile_walls;
+  b.row_walls = h->row_walls;
+  b.work_counter = h->work_counter;
   b.rho = h->rho;
   b.psi = h->psi;
   b.force = h->force;
@@ -1003,6 +1105,13 @@ int step_host_wave(lbgpu_handle* h, const double* const* in, double* const* out,
     if (x1 <= x0) return cudaSuccess;
     StepParams P = h->P;
     P.record_force = h->record_force ? 1 : 0;
+    if (!fp64) {
+      // the fused forms: one pair-kernel launch per plane range (it reads
+      // planes x0 - 2 .. x1 + 1, those the FP64 collide part needs)
+      if (which != lbk::kPartCollide) return cudaSuccess;
+      return lbk::launch_fused_range(storage_kind(h->cfg.precision), h->C, b, P, x0, x1, h->stream, &h->launches,
+                                     h->cfg.device);
+    }
     P.s_begin = int64_t(x0) * plane_sites;
     P.s_end = int64_t(x1) * plane_sites;
     return lbk::launch_part_f64(which, h->Q, h->C, b, P, h->stream, &h->launches);
@@ -1017,8 +1126,8 @@ int step_host_wave(lbgpu_handle* h, const double* const* in, double* const* out,
       const int64_t work = int64_t(g.nyh) * g.nzh * np;
       for (int c = 0; c < h->C; ++c) {
         if (!out[c]) continue;
-        k_download<double><<<unsigned(ceil_div(work, 256)), 256, 0, h->stream>>>(slot(4 + 2 * p + c), fout, c, a,
-                                                                                  np, g, h->P);
+        k_download<T><<<unsigned(ceil_div(work, 256)), 256, 0, h->stream>>>(slot(4 + 2 * p + c), fout, c, a, np, g,
+                                                                             h->P);
         h->launches++;
       }
       cudaError_t le = cudaGetLastError();
@@ -1052,8 +1161,8 @@ int step_host_wave(lbgpu_handle* h, const double* const* in, double* const* out,
     cudaStreamWaitEvent(h->stream, ev[1 + p], 0);
     const int64_t work = plane_sites * (bnd - a);
     for (int c = 0; c < h->C; ++c) {
-      k_upload<double><<<unsigned(ceil_div(work, 256)), 256, 0, h->stream>>>(slot(2 * p + c), fin, c, a + kHalo,
-                                                                            bnd - a, g, h->P);
+      k_upload<T><<<unsigned(ceil_div(work, 256)), 256, 0, h->stream>>>(
+          slot(2 * p + c), fin, c, a + kHalo, bnd - a, g, h->P, fp64 ? nullptr : fout, fp64 ? nullptr : h->mask);
       h->launches++;
     }
     if ((e = cudaGetLastError()) != cudaSuccess) return fail(e, "step_host input transpose");
@@ -1085,6 +1194,7 @@ int step_host_wave(lbgpu_handle* h, const double* const* in, double* const* out,
   if (h->record_force) h->force_valid = 1;
   return LBGPU_OK;
 }
+}  // extern "C++"
 
 }  // namespace
 
@@ -1094,10 +1204,15 @@ int lbgpu_step_host(lbgpu_handle* h, const double* const* fluids_in, const int32
     if (!fluids_in[c]) return h->fail(LBGPU_E_INVALID, "null fluid array");
   if (h->lite || !h->rho) return h->fail(LBGPU_E_INVALID, "batch members step with their batch");
   if (h->advected) return h->fail(LBGPU_E_NOTREADY, "lbgpu_step_host between lbgpu_advect and lbgpu_collide");
-  const int K = (h->cfg.precision == LBGPU_FP64 && !h->profiling) ? wave_planes(h) : 0;
+  // the wavefront: FP64, and the fused forms on the pair kernel (FP16 and I16
+  // once their offsets' scale is pinned: otherwise the upload derives it
+  // from the whole input first)
+  const bool fused_wave = h->fused && h->P.nz % 2 == 0 && h->P.eq_form == LBGPU_EQ_BDIST2 && h->work_counter &&
+                          (h->cfg.precision == LBGPU_FP32 || h->scale_pinned);
+  const int K = ((h->cfg.precision == LBGPU_FP64 || fused_wave) && !h->profiling) ? wave_planes(h) : 0;
   if (K == 0) {
-    // the other forms (the FP16 scale needs the whole input first), profiled
-    // handles and lattices too small for the wavefront: one after another
+    // the other forms, profiled handles and lattices too small for the
+    // wavefront: one after another
     if (int rc = lbgpu_upload(h, fluids_in, mask)) return rc;
     if (int rc = lbgpu_step(h, 1)) return rc;
     return lbgpu_download(h, fluids_out);
@@ -1108,8 +1223,41 @@ int lbgpu_step_host(lbgpu_handle* h, const double* const* fluids_in, const int32
   if (int rc = upload_mask(h, mask)) return rc;
   if (int rc = lb_update_nbmask(h)) return rc;
   h->force_valid = 0;
-  if (int rc = step_host_wave(h, fluids_in, fluids_out, K)) return rc;
+  int rc;
+  if (h->cfg.precision == LBGPU_FP64)
+    rc = step_host_wave<double>(h, fluids_in, fluids_out, K);
+  else if (h->cfg.precision == LBGPU_FP32)
+    rc = step_host_wave<float>(h, fluids_in, fluids_out, K);
+  else if (h->cfg.precision == LBGPU_FP16)
+    rc = step_host_wave<__half>(h, fluids_in, fluids_out, K);
+  else
+    rc = step_host_wave<int16_t>(h, fluids_in, fluids_out, K);
+  if (rc) return rc;
+  // the wavefront's upload wrote the solid sites into both buffers
+  if (h->fused) h->solids_synced = true;
   h->uploaded = true;
+  return LBGPU_OK;
+}
+
+int lbgpu_set_storage_scale(lbgpu_handle* h, const double* rho0, const double* scale) {
+  if (!h) return LBGPU_E_INVALID;
+  if (h->cfg.precision != LBGPU_FP16 && h->cfg.precision != LBGPU_I16)
+    return h->fail(LBGPU_E_INVALID, "the storage scale belongs to the FP16 and I16 forms");
+  if (!rho0 || !scale) {
+    h->scale_pinned = false;
+    return LBGPU_OK;
+  }
+  for (int c = 0; c < h->C; ++c)
+    if (!(scale[c] > 0.0) || !std::isfinite(scale[c]) || !std::isfinite(rho0[c]))
+      return h->fail(LBGPU_E_INVALID, "the storage scale must be positive and finite");
+  if (h->uploaded)
+    return h->fail(LBGPU_E_INVALID, "pin the storage scale before the first upload (the stored offsets use it)");
+  for (int c = 0; c < h->C; ++c) {
+    h->P.rho0[c] = float(rho0[c]);
+    h->P.scale[c] = float(scale[c]);
+    h->P.inv_scale[c] = float(1.0 / scale[c]);
+  }
+  h->scale_pinned = true;
   return LBGPU_OK;
 }
 
@@ -1135,6 +1283,8 @@ int lbgpu_moments(lbgpu_handle* h, double* const* density, double* const* veloci
       e = launch_moments<double>(h, h->moments, nullptr, dcol);
     else if (h->cfg.precision == LBGPU_FP32)
       e = launch_moments<float>(h, h->moments, nullptr, dcol);
+    else if (h->cfg.precision == LBGPU_I16)
+      e = launch_moments<int16_t>(h, h->moments, nullptr, dcol);
     else
       e = launch_moments<__half>(h, h->moments, nullptr, dcol);
     if (e != cudaSuccess) return h->cuda_fail(e, "moments kernel");
@@ -1178,6 +1328,8 @@ int lbgpu_moments(lbgpu_handle* h, double* const* density, double* const* veloci
       e = launch_moments<double>(h, nullptr, dvel, nullptr);
     else if (h->cfg.precision == LBGPU_FP32)
       e = launch_moments<float>(h, nullptr, dvel, nullptr);
+    else if (h->cfg.precision == LBGPU_I16)
+      e = launch_moments<int16_t>(h, nullptr, dvel, nullptr);
     else
       e = launch_moments<__half>(h, nullptr, dvel, nullptr);
     if (e != cudaSuccess) return h->cuda_fail(e, "velocity kernel");
@@ -1227,6 +1379,8 @@ int lbgpu_reduce(lbgpu_handle* h, double* mass, double* momentum) {
     e = launch_reduce<double>(h, partial, nblocks, per_block, out);
   else if (h->cfg.precision == LBGPU_FP32)
     e = launch_reduce<float>(h, partial, nblocks, per_block, out);
+  else if (h->cfg.precision == LBGPU_I16)
+    e = launch_reduce<int16_t>(h, partial, nblocks, per_block, out);
   else
     e = launch_reduce<__half>(h, partial, nblocks, per_block, out);
   if (e != cudaSuccess) return h->cuda_fail(e, "reduce kernel");

@@ -4,12 +4,16 @@
 // Members are lattice handles (lb_handle.h) that own only their population
 // buffers and mask; the batch owns the stream and a shared staging buffer for
 // host transfers, and admits members against a fixed device-memory budget.
-// A device table of FusedSim descriptors (one per member, in admission order)
-// drives k_fused_batch; it is rebuilt when members join or leave.  Steps are
-// replayed as a captured CUDA graph of two launches (the two buffer
-// parities).  The launch shape (tile height 4 or 8, resident CTAs per SM) is
-// chosen by timing the candidates on the batch itself: every candidate
-// computes the same per-site arithmetic, so tuning steps are ordinary steps.
+// Members run the kernel their lone lattice would run: those with an even z
+// extent and the BDist2 equilibrium the pair kernel (a device table of
+// PairSim descriptors drives k_pairs_batch), the others the
+// one-site-per-thread fused kernel (FusedSim descriptors, k_fused_batch);
+// the tables are rebuilt when members join or leave.  Steps are replayed as
+// a captured CUDA graph of two steps (the two buffer parities).  The launch
+// shape (the fused kernel's tile height and CTAs per SM, the pair kernel's
+// run length and CTAs per SM) is chosen by timing the candidates on the
+// batch itself: every candidate computes the same per-site arithmetic, so
+// tuning steps are ordinary steps.
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <stdlib.h>
@@ -23,17 +27,20 @@
 #include "../../include/lbgpu.h"
 #include "lb_fused.cuh"
 #include "lb_handle.h"
+#include "lb_pairs.cuh"
 
 namespace {
 
 constexpr size_t kBatchStaging = size_t(256) << 20;
 
 struct Shape {
-  int ty;
-  int ctas_per_sm;
+  int ty;           // fused kernel: tile height
+  int ctas_per_sm;  // fused kernel: resident CTAs per SM (0: as many as fit)
+  int prun;         // pair kernel: run length in planes
+  int pctas;        // pair kernel: resident CTAs per SM (0: as many as fit)
 };
 
-const Shape kCandidates[] = {{8, 2}, {8, 1}, {4, 4}, {4, 2}};
+const Shape kCandidates[] = {{8, 2, 32, 0}, {8, 1, 16, 0}, {4, 4, 32, 1}, {4, 2, 8, 0}};
 
 std::mutex g_tune_mu;
 std::map<std::string, Shape> g_tuned;  // member-size signature -> best shape
@@ -60,12 +67,19 @@ struct lbgpu_batch {
   int64_t total_units = 0;
   int* d_counters = nullptr;  // dynamic scheduling, one per buffer parity
   bool walls = false;
+  // pair-kernel members
+  lbk::PairSim* d_ptable = nullptr;
+  int ptable_cap = 0;
+  int ptable_n = 0;
+  int64_t ptotal_units = 0;
+  int* d_pcounters = nullptr;
+  bool pwalls = false;
   bool dirty = true;
   int64_t steps_since_build = 0;
   std::vector<int> table_ids;
   std::vector<int> table_phase;
   // launch shape
-  Shape shape{8, 0};
+  Shape shape{8, 0, 32, 0};
   int autotune = 1;
   bool shape_fixed = false;
   int use_graph = 1;
@@ -99,50 +113,91 @@ std::string signature(const lbgpu_batch* b) {
   return s;
 }
 
-// (re)build the descriptor table for tile height ty, with every member's
+// whether a member runs the pair kernel (the rule launch_fused applies to a
+// lone lattice)
+bool pair_member(const lbgpu_handle* h) { return h->nz % 2 == 0 && h->P.eq_form == 2; }
+
+template <typename D>
+int upload_table(lbgpu_batch* b, const std::vector<D>& tab, D** d_tab, int* cap) {
+  if (int(tab.size()) > *cap) {
+    if (*d_tab) cudaFree(*d_tab);
+    *d_tab = nullptr;
+    const int c = int(tab.size()) * 2;
+    cudaError_t e = cudaMalloc(d_tab, sizeof(D) * size_t(c));
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      *d_tab = nullptr;
+      *cap = 0;
+      return b->fail(LBGPU_E_NOMEM, "batch descriptor table allocation failed");
+    }
+    *cap = c;
+  }
+  if (!tab.empty()) {
+    cudaError_t e = cudaMemcpyAsync(*d_tab, tab.data(), sizeof(D) * tab.size(), cudaMemcpyHostToDevice, b->stream);
+    if (e != cudaSuccess) return b->cuda_fail(e, "batch table upload");
+  }
+  return LBGPU_OK;
+}
+
+// (re)build the descriptor tables for launch shape `sh`, with every member's
 // current input buffer as parity 0
-int build_table(lbgpu_batch* b, int ty) {
+int build_table(lbgpu_batch* b, const Shape& sh) {
   std::vector<lbk::FusedSim> tab;
+  std::vector<lbk::PairSim> ptab;
   b->table_ids.clear();
   b->table_phase.clear();
   b->total_work = 0;
   b->total_units = 0;
+  b->ptotal_units = 0;
   b->walls = false;
+  b->pwalls = false;
   for (size_t id = 0; id < b->sims.size(); ++id) {
     lbgpu_handle* h = b->sims[id];
     if (!h) continue;
-    lbk::FusedSim fs;
-    memset(&fs, 0, sizeof fs);
-    fs.P = lbk::make_fused_params(h->P, ty);
-    fs.f[0] = h->f[0];
-    fs.f[1] = h->f[1];
-    fs.nbmask = h->nbmask;
-    fs.force_out = nullptr;
-    fs.work_begin = b->total_work;
-    fs.phase = h->cur;
-    fs.P.run_len = h->nx < 64 ? h->nx : 32;
-    fs.nchunks = (h->nx + fs.P.run_len - 1) / fs.P.run_len;
-    fs.unit_begin = b->total_units;
-    b->total_units += int64_t(fs.P.tiles_y) * fs.P.tiles_z * fs.nchunks;
-    b->total_work += fs.P.work;
-    b->walls = b->walls || h->mask != nullptr;
-    tab.push_back(fs);
+    if (pair_member(h)) {
+      lbk::PairSim ps;
+      memset(&ps, 0, sizeof ps);
+      ps.P = lbk::make_fused_params(h->P, 8);
+      ps.P.tiles_y = (h->ny + lbk::kPairTY - 1) / lbk::kPairTY;
+      ps.P.tiles_z = (h->nz + lbk::kPairTZ - 1) / lbk::kPairTZ;
+      ps.P.work = int64_t(ps.P.tiles_y) * ps.P.tiles_z * h->nx;
+      ps.P.run_len = h->nx < sh.prun ? h->nx : sh.prun;
+      ps.f[0] = h->f[0];
+      ps.f[1] = h->f[1];
+      ps.nbmask = h->nbmask;
+      ps.row_walls = h->row_walls;
+      ps.force_out = nullptr;
+      ps.phase = h->cur;
+      ps.nchunks = (h->nx + ps.P.run_len - 1) / ps.P.run_len;
+      ps.unit_begin = b->ptotal_units;
+      b->ptotal_units += int64_t(ps.P.tiles_y) * ps.P.tiles_z * ps.nchunks;
+      b->pwalls = b->pwalls || h->mask != nullptr;
+      ptab.push_back(ps);
+    } else {
+      lbk::FusedSim fs;
+      memset(&fs, 0, sizeof fs);
+      fs.P = lbk::make_fused_params(h->P, sh.ty);
+      fs.f[0] = h->f[0];
+      fs.f[1] = h->f[1];
+      fs.nbmask = h->nbmask;
+      fs.force_out = nullptr;
+      fs.work_begin = b->total_work;
+      fs.phase = h->cur;
+      fs.P.run_len = h->nx < 64 ? h->nx : 32;
+      fs.nchunks = (h->nx + fs.P.run_len - 1) / fs.P.run_len;
+      fs.unit_begin = b->total_units;
+      b->total_units += int64_t(fs.P.tiles_y) * fs.P.tiles_z * fs.nchunks;
+      b->total_work += fs.P.work;
+      b->walls = b->walls || h->mask != nullptr;
+      tab.push_back(fs);
+    }
     b->table_ids.push_back(int(id));
     b->table_phase.push_back(h->cur);
   }
   b->table_n = int(tab.size());
-  if (b->table_n > b->table_cap) {
-    if (b->d_table) cudaFree(b->d_table);
-    b->d_table = nullptr;
-    const int cap = b->table_n * 2;
-    cudaError_t e = cudaMalloc(&b->d_table, sizeof(lbk::FusedSim) * size_t(cap));
-    if (e != cudaSuccess) {
-      cudaGetLastError();
-      b->table_cap = 0;
-      return b->fail(LBGPU_E_NOMEM, "batch descriptor table allocation failed");
-    }
-    b->table_cap = cap;
-  }
+  b->ptable_n = int(ptab.size());
+  if (int rc = upload_table(b, tab, &b->d_table, &b->table_cap)) return rc;
+  if (int rc = upload_table(b, ptab, &b->d_ptable, &b->ptable_cap)) return rc;
   if (!b->d_counters) {
     cudaError_t e = cudaMalloc(&b->d_counters, 2 * sizeof(int));
     if (e != cudaSuccess) {
@@ -151,17 +206,28 @@ int build_table(lbgpu_batch* b, int ty) {
     }
   }
   if (b->d_counters) cudaMemsetAsync(b->d_counters, 0, 2 * sizeof(int), b->stream);
-  if (b->table_n) {
-    cudaError_t e = cudaMemcpyAsync(b->d_table, tab.data(), sizeof(lbk::FusedSim) * tab.size(),
-                                    cudaMemcpyHostToDevice, b->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
-    if (e != cudaSuccess) return b->cuda_fail(e, "batch table upload");
+  if (b->ptable_n) {
+    if (!b->d_pcounters) {
+      cudaError_t e = cudaMalloc(&b->d_pcounters, 2 * sizeof(int));
+      if (e != cudaSuccess) {
+        cudaGetLastError();
+        b->d_pcounters = nullptr;
+        return b->fail(LBGPU_E_NOMEM, "batch counter allocation failed");
+      }
+    }
+    if (b->ptotal_units >= (int64_t(1) << 31)) return b->fail(LBGPU_E_INVALID, "batch too large for its work counter");
+    cudaMemsetAsync(b->d_pcounters, 0, 2 * sizeof(int), b->stream);
   }
+  cudaError_t e = cudaStreamSynchronize(b->stream);
+  if (e != cudaSuccess) return b->cuda_fail(e, "batch table upload");
   b->steps_since_build = 0;
   b->dirty = false;
   drop_graph(b);
   return LBGPU_OK;
 }
+
+// kernel launches per batch step
+int kernels_per_step(const lbgpu_batch* b) { return (b->table_n > 0 ? 1 : 0) + (b->ptable_n > 0 ? 1 : 0); }
 
 // members' current-buffer index after the steps since the last build
 void sync_members(lbgpu_batch* b) {
@@ -177,6 +243,16 @@ cudaError_t launch_one(lbgpu_batch* b, int parity) {
     const char* s = getenv("LBGPU_BATCH_STATIC");
     return s && s[0] == '1';
   }();
+  if (b->ptable_n) {
+    b->launches++;
+    const int kind = b->precision == LBGPU_FP16  ? lbk::kStoreF16
+                     : b->precision == LBGPU_I16 ? lbk::kStoreI16
+                                                 : lbk::kStoreF32;
+    cudaError_t e = lbk::launch_pairs_batch(kind, b->pwalls, b->d_ptable, b->ptable_n, parity, b->shape.pctas,
+                                            b->stream, b->device, b->ptotal_units, b->d_pcounters);
+    if (e != cudaSuccess) return e;
+  }
+  if (!b->table_n) return cudaSuccess;
   b->launches++;
   return lbk::launch_fused_batch(b->precision == LBGPU_FP16, b->shape.ty, b->walls, b->d_table, b->table_n,
                                  b->total_work, parity, b->shape.ctas_per_sm, b->stream, b->device,
@@ -186,7 +262,7 @@ cudaError_t launch_one(lbgpu_batch* b, int parity) {
 
 // advance n steps with the current table and shape
 int run_steps(lbgpu_batch* b, int n) {
-  if (b->table_n == 0 || n <= 0) return LBGPU_OK;
+  if ((b->table_n == 0 && b->ptable_n == 0) || n <= 0) return LBGPU_OK;
   // members with walls whose buffers do not both hold the solid sites yet
   for (size_t i = 0; i < b->table_ids.size(); ++i) {
     lbgpu_handle* h = b->sims[b->table_ids[i]];
@@ -216,9 +292,10 @@ int run_steps(lbgpu_batch* b, int n) {
       cudaGraph_t g = nullptr;
       e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
       if (e == cudaSuccess) {
+        const int64_t before = b->launches;
         cudaError_t e0 = launch_one(b, 0);
         cudaError_t e1 = launch_one(b, 1);
-        b->launches -= 2;  // counted when replayed
+        b->launches = before;  // counted when replayed
         e = cudaStreamEndCapture(b->stream, &g);
         if (e == cudaSuccess && e0 == cudaSuccess && e1 == cudaSuccess)
           e = cudaGraphInstantiate(&b->graph, g, 0);
@@ -235,7 +312,7 @@ int run_steps(lbgpu_batch* b, int n) {
     while (b->graph && n - done >= 2) {
       e = cudaGraphLaunch(b->graph, b->stream);
       if (e != cudaSuccess) return b->cuda_fail(e, "batch graph launch");
-      b->launches += 2;
+      b->launches += 2 * kernels_per_step(b);
       b->steps_since_build += 2;
       done += 2;
     }
@@ -258,10 +335,12 @@ int autotune(lbgpu_batch* b, int budget_steps, int* rc) {
     std::lock_guard<std::mutex> lock(g_tune_mu);
     auto it = g_tuned.find(sig);
     if (it != g_tuned.end()) {
-      if (it->second.ty != b->shape.ty || it->second.ctas_per_sm != b->shape.ctas_per_sm) {
+      const Shape& t = it->second;
+      if (t.ty != b->shape.ty || t.ctas_per_sm != b->shape.ctas_per_sm || t.prun != b->shape.prun ||
+          t.pctas != b->shape.pctas) {
         sync_members(b);
-        b->shape = it->second;
-        *rc = build_table(b, b->shape.ty);
+        b->shape = t;
+        *rc = build_table(b, b->shape);
       }
       return 0;
     }
@@ -280,7 +359,7 @@ int autotune(lbgpu_batch* b, int budget_steps, int* rc) {
   for (int i = 0; i < ncand; ++i) {
     sync_members(b);
     b->shape = kCandidates[i];
-    if ((*rc = build_table(b, b->shape.ty))) break;
+    if ((*rc = build_table(b, b->shape))) break;
     cudaEventRecord(e0, b->stream);
     if ((*rc = run_steps(b, per))) break;
     cudaEventRecord(e1, b->stream);
@@ -299,7 +378,7 @@ int autotune(lbgpu_batch* b, int budget_steps, int* rc) {
   if (*rc) return taken;
   sync_members(b);
   b->shape = best_shape;
-  *rc = build_table(b, b->shape.ty);
+  *rc = build_table(b, b->shape);
   std::lock_guard<std::mutex> lock(g_tune_mu);
   g_tuned[sig] = best_shape;
   return taken;
@@ -312,8 +391,8 @@ extern "C" {
 int lbgpu_batch_create(int32_t device, int32_t precision, int64_t hbm_budget_bytes, lbgpu_batch** out) {
   if (!out) return LBGPU_E_INVALID;
   *out = nullptr;
-  if (precision != LBGPU_FP32 && precision != LBGPU_FP16) {
-    g_batch_create_error = "batches run the FP32 or FP16 forms";
+  if (precision != LBGPU_FP32 && precision != LBGPU_FP16 && precision != LBGPU_I16) {
+    g_batch_create_error = "batches run the FP32, FP16 or I16 forms";
     return LBGPU_E_INVALID;
   }
   cudaError_t e = cudaSetDevice(device);
@@ -348,6 +427,8 @@ void lbgpu_batch_destroy(lbgpu_batch* b) {
   drop_graph(b);
   if (b->d_table) cudaFree(b->d_table);
   if (b->d_counters) cudaFree(b->d_counters);
+  if (b->d_ptable) cudaFree(b->d_ptable);
+  if (b->d_pcounters) cudaFree(b->d_pcounters);
   cudaFree(b->staging);
   if (b->own_stream) cudaStreamDestroy(b->own_stream);
   delete b;
@@ -422,7 +503,7 @@ int lbgpu_batch_step(lbgpu_batch* b, int32_t nsteps) {
   cudaSetDevice(b->device);
   if (b->dirty) {
     sync_members(b);
-    int rc = build_table(b, b->shape.ty);
+    int rc = build_table(b, b->shape);
     if (rc) return rc;
   }
   int remaining = nsteps;
@@ -472,7 +553,7 @@ int lbgpu_batch_set_tuning(lbgpu_batch* b, int32_t autotune, int32_t tile_height
   b->use_graph = use_graph;
   if (tile_height) {
     sync_members(b);
-    b->shape = Shape{tile_height, ctas_per_sm};
+    b->shape = Shape{tile_height, ctas_per_sm, 32, ctas_per_sm};
     b->shape_fixed = true;
     b->dirty = true;
   } else {

@@ -25,6 +25,8 @@ FusedParams make_fused_params(const StepParams& P, int ty) {
   F.tile_walls = nullptr;
   F.work_counter = nullptr;
   F.run_len = P.nx;
+  F.x_begin = 0;
+  F.x_end = P.nx;
   for (int c = 0; c < 2; ++c) {
     F.tau[c] = float(P.tau[c]);
     F.inv_tau[c] = float(1.0 / P.tau[c]);
@@ -52,7 +54,37 @@ FusedParams make_fused_params(const StepParams& P, int ty) {
 }
 
 
-cudaError_t launch_fused(bool half_storage, int c, const StepBuffers& b, const StepParams& P, cudaStream_t st,
+bool pairs_eligible(const StepParams& P, const StepBuffers& b) {
+  // aligned two-site words need an even z extent; the pair kernel computes
+  // the BDist2 equilibrium and schedules through the work counter
+  return P.nz % 2 == 0 && P.eq_form == 2 && b.work_counter != nullptr && (b.mask == nullptr || b.row_walls != nullptr);
+}
+
+// the pair step over planes [x0, x1) of every tile (the host transfers
+// wavefront): reads the populations of planes x0 - 2 .. x1 + 1 (periodic)
+cudaError_t launch_fused_range(int kind, int c, const StepBuffers& b, const StepParams& P, int x0, int x1,
+                               cudaStream_t st, int64_t* launches, int device) {
+  if (x1 <= x0) return cudaSuccess;
+  if (!pairs_eligible(P, b)) return cudaErrorInvalidValue;
+  FusedParams G = make_fused_params(P, 8);
+  G.tile_walls = b.tile_walls;
+  G.work_counter = b.work_counter;
+  G.tiles_y = (P.ny + 7) / 8;
+  G.tiles_z = (P.nz + kPairTZ - 1) / kPairTZ;
+  G.work = int64_t(G.tiles_y) * G.tiles_z * P.nx;
+  G.x_begin = x0;
+  G.x_end = x1;
+  cudaMemsetAsync(b.work_counter, 0, sizeof(int), st);
+  const bool w = b.mask != nullptr;
+  if (w && !b.nbmask) return cudaErrorInvalidValue;
+  const bool mom = P.unit_tau != 0;
+  *launches += 1;
+  return kind == kStoreF16   ? launch_pairs_single_f16(c, w, mom, b, G, st, device)
+         : kind == kStoreI16 ? launch_pairs_single_i16(c, w, mom, b, G, st, device)
+                             : launch_pairs_single_f32(c, w, mom, b, G, st, device);
+}
+
+cudaError_t launch_fused(int kind, int c, const StepBuffers& b, const StepParams& P, cudaStream_t st,
                          int64_t* launches, const StepEvents* ev, int device) {
   FusedParams F = make_fused_params(P, 8);
   F.tile_walls = b.tile_walls;
@@ -68,9 +100,24 @@ cudaError_t launch_fused(bool half_storage, int c, const StepBuffers& b, const S
     cudaEventRecord(ev->ev[0], st);
     cudaEventRecord(ev->ev[1], st);
   }
-  const bool mom = c == 2 && P.unit_tau && P.eq_form == 2;
-  const cudaError_t e = half_storage ? launch_fused_single_f16(c, w, mom, b, F, st, device)
-                                     : launch_fused_single_f32(c, w, mom, b, F, st, device);
+  cudaError_t e;
+  if (pairs_eligible(P, b)) {
+    // two z-adjacent sites per thread (lb_pairs.cuh): 8 x 64 tiles
+    FusedParams G = F;
+    G.tiles_y = (P.ny + 7) / 8;
+    G.tiles_z = (P.nz + kPairTZ - 1) / kPairTZ;
+    G.work = int64_t(G.tiles_y) * G.tiles_z * P.nx;
+    const bool mom = P.unit_tau != 0;
+    e = kind == kStoreF16   ? launch_pairs_single_f16(c, w, mom, b, G, st, device)
+        : kind == kStoreI16 ? launch_pairs_single_i16(c, w, mom, b, G, st, device)
+                            : launch_pairs_single_f32(c, w, mom, b, G, st, device);
+  } else if (kind == kStoreI16) {
+    e = cudaErrorInvalidValue;  // the I16 form runs on the pair kernel only
+  } else {
+    const bool mom = c == 2 && P.unit_tau && P.eq_form == 2;
+    e = kind == kStoreF16 ? launch_fused_single_f16(c, w, mom, b, F, st, device)
+                          : launch_fused_single_f32(c, w, mom, b, F, st, device);
+  }
   if (ev) cudaEventRecord(ev->ev[2], st);
   *launches += 1;
   return e;

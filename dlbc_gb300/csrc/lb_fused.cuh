@@ -78,6 +78,8 @@ struct FusedParams {
   // in planes; nullptr: static equal ranges
   int* work_counter;
   int32_t run_len;
+  // the pair kernel's plane range [x_begin, x_end) (the whole lattice: 0, nx)
+  int32_t x_begin, x_end;
 };
 
 template <typename T>

@@ -5,6 +5,7 @@
 #include "lb_fused.cuh"
 #include "lb_fused_launch.cuh"
 #include "lb_launch.h"
+#include "lb_pairs.cuh"
 
 namespace lbk {
 
@@ -27,7 +28,33 @@ cudaError_t go_batch(const FusedSim* sims, int nsims, int64_t total, int parity,
   return cudaGetLastError();
 }
 
+template <typename T, bool W>
+cudaError_t go_pairs_batch(const PairSim* sims, int nsims, int parity, int ctas_per_sm, cudaStream_t st, int device,
+                           int64_t total_units, int* counters) {
+  static KernelInfo info;
+  auto kern = k_pairs_batch<T, W>;
+  const int smem = int(sizeof(PairShared<2, W, false, T>));
+  int per_sm = 0;
+  cudaError_t e = kernel_setup(kern, smem, kPairThreads, device, info, &per_sm);
+  if (e != cudaSuccess) return e;
+  if (ctas_per_sm > 0 && ctas_per_sm < per_sm) per_sm = ctas_per_sm;
+  int64_t grid = int64_t(per_sm) * sm_count(device);
+  if (grid > total_units) grid = total_units;
+  if (grid < 1) return cudaSuccess;
+  kern<<<unsigned(grid), kPairThreads, smem, st>>>(sims, nsims, parity, total_units, counters);
+  return cudaGetLastError();
+}
+
 }  // namespace
+
+cudaError_t launch_pairs_batch(int kind, bool walls, const PairSim* sims, int nsims, int parity, int ctas_per_sm,
+                               cudaStream_t st, int device, int64_t total_units, int* counters) {
+#define LB_PBATCH(T, W) go_pairs_batch<T, W>(sims, nsims, parity, ctas_per_sm, st, device, total_units, counters)
+  if (kind == kStoreF16) return walls ? LB_PBATCH(__half, true) : LB_PBATCH(__half, false);
+  if (kind == kStoreI16) return walls ? LB_PBATCH(int16_t, true) : LB_PBATCH(int16_t, false);
+  return walls ? LB_PBATCH(float, true) : LB_PBATCH(float, false);
+#undef LB_PBATCH
+}
 
 cudaError_t launch_fused_batch(bool half_storage, int ty, bool walls, const FusedSim* sims, int nsims,
                                int64_t total_work, int parity, int ctas_per_sm, cudaStream_t st, int device,

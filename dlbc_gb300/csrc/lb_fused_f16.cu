@@ -1,10 +1,12 @@
-// The single-lattice fused step with half-offset populations.
+// The single-lattice fused step with half-offset populations, and the pair
+// step with half or 16-bit fixed-point offsets.
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include "lb_fused.cuh"
 #include "lb_fused_launch.cuh"
 #include "lb_launch.h"
+#include "lb_pairs.cuh"
 
 namespace lbk {
 
@@ -42,6 +44,16 @@ cudaError_t launch_fused_single_f16(int c, bool w, bool mom, const StepBuffers& 
     return w ? go_single<__half, 2, true, 8, true>(b, F, st, device) : go_single<__half, 2, false, 8, true>(b, F, st, device);
   if (c == 2) return w ? go_single<__half, 2, true, 8>(b, F, st, device) : go_single<__half, 2, false, 8>(b, F, st, device);
   return w ? go_single<__half, 1, true, 8>(b, F, st, device) : go_single<__half, 1, false, 8>(b, F, st, device);
+}
+
+cudaError_t launch_pairs_single_f16(int c, bool w, bool mom, const StepBuffers& b, const FusedParams& F,
+                                    cudaStream_t st, int device) {
+  return launch_pairs<__half>(c, w, mom, b, F, st, device);
+}
+
+cudaError_t launch_pairs_single_i16(int c, bool w, bool mom, const StepBuffers& b, const FusedParams& F,
+                                    cudaStream_t st, int device) {
+  return launch_pairs<int16_t>(c, w, mom, b, F, st, device);
 }
 
 }  // namespace lbk

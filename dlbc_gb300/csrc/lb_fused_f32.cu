@@ -5,6 +5,7 @@
 #include "lb_fused.cuh"
 #include "lb_fused_launch.cuh"
 #include "lb_launch.h"
+#include "lb_pairs.cuh"
 
 namespace lbk {
 
@@ -42,6 +43,11 @@ cudaError_t launch_fused_single_f32(int c, bool w, bool mom, const StepBuffers& 
     return w ? go_single<float, 2, true, 8, true>(b, F, st, device) : go_single<float, 2, false, 8, true>(b, F, st, device);
   if (c == 2) return w ? go_single<float, 2, true, 8>(b, F, st, device) : go_single<float, 2, false, 8>(b, F, st, device);
   return w ? go_single<float, 1, true, 8>(b, F, st, device) : go_single<float, 1, false, 8>(b, F, st, device);
+}
+
+cudaError_t launch_pairs_single_f32(int c, bool w, bool mom, const StepBuffers& b, const FusedParams& F,
+                                    cudaStream_t st, int device) {
+  return launch_pairs<float>(c, w, mom, b, F, st, device);
 }
 
 }  // namespace lbk

@@ -30,6 +30,7 @@ struct lbgpu_handle {
   uint8_t* mask = nullptr;
   uint32_t* nbmask = nullptr;       // neighbour masks for the fused step (walls only)
   uint8_t* tile_walls = nullptr;    // per (x, 8x32 tile) wall flags for the fused step
+  uint8_t* row_walls = nullptr;     // per (x, y, 64-site z segment) wall flags for the pair step
   int* work_counter = nullptr;      // the fused step's dynamic scheduling counter
   void* rho = nullptr;
   void* psi = nullptr;
@@ -63,6 +64,10 @@ struct lbgpu_handle {
   // initialisation or a mask change, until lb_sync_solids copies the
   // current buffer over the other one.
   bool solids_synced = false;
+  // FP16 / I16: rest density and scale of the stored offsets fixed by
+  // lbgpu_set_storage_scale (uploads keep them instead of deriving them
+  // from the input)
+  bool scale_pinned = false;
   // per-kernel event timing (lbgpu_profile)
   bool profiling = false;
   std::vector<lbk::StepEvents> ev_pending, ev_pool;
@@ -93,6 +98,9 @@ int64_t lb_member_bytes(const lbgpu_config* cfg);
 int lb_ensure_moments(lbgpu_handle* h);
 // (re)build or drop the neighbour masks after the mask changed
 int lb_update_nbmask(lbgpu_handle* h);
+// scale of the I16 form's fixed point for a component with rest density
+// rho0 and largest initial |f_q / w_q - rho0| maxdev
+double i16_scale(double rho0, double maxdev);
 // copy buffer cur over the other one when the fused step needs the solid
 // sites in both (see solids_synced)
 int lb_sync_solids(lbgpu_handle* h, int cur, cudaStream_t st);

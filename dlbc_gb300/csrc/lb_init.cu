@@ -261,6 +261,13 @@ __device__ __forceinline__ __half encode<__half>(double v, int Q, int q, int c, 
   return __float2half_rn((float(v) * (1.0f / w) - P.rho0[c]) * P.inv_scale[c]);
 }
 
+template <>
+__device__ __forceinline__ int16_t encode<int16_t>(double v, int Q, int q, int c, const StepParams& P) {
+  const float w = float(lbk::weight_of(Q, q));
+  const int h = __float2int_rn((float(v) * (1.0f / w) - P.rho0[c]) * P.inv_scale[c]);
+  return int16_t(h < -32767 ? -32767 : (h > 32767 ? 32767 : h));
+}
+
 template <typename T>
 __global__ void k_init_write(InitDev I, int64_t n, StepParams P, T* __restrict__ f, uint8_t* __restrict__ mask,
                              int* __restrict__ nsolid) {
@@ -399,7 +406,7 @@ extern "C" int lbgpu_init_fields(lbgpu_handle* h, const lbgpu_init* ini) {
   double* d_partial = h->staging;
   double* d_rho0 = h->staging + size_t(nblocks) * 2;
   int* d_count = reinterpret_cast<int*>(h->staging + size_t(nblocks) * 2 + 2);
-  if (h->cfg.precision == LBGPU_FP16) {
+  if ((h->cfg.precision == LBGPU_FP16 || h->cfg.precision == LBGPU_I16) && !h->scale_pinned) {
     double sums[2], maxdev[2];
     if (int rc = reduce_stats(h, I, 1, d_rho0, d_partial, nblocks, sums, false)) return rc;
     double rho0[2];
@@ -412,9 +419,15 @@ extern "C" int lbgpu_init_fields(lbgpu_handle* h, const lbgpu_init* ini) {
     if (e != cudaSuccess) return h->cuda_fail(e, "init statistics");
     if (int rc = reduce_stats(h, I, 2, d_rho0, d_partial, nblocks, maxdev, true)) return rc;
     for (int c = 0; c < h->C; ++c) {
-      // same rule as lbgpu_upload: offsets up to 64 * max(rho0, 4 * spread)
-      const double span = std::max(fabs(rho0[c]), 4.0 * maxdev[c]);
-      const double scale = span > 0.0 ? span / 1024.0 : 1.0 / 4096.0;
+      // same rules as lbgpu_upload: FP16 offsets up to 64 * max(rho0,
+      // 4 * spread); I16 fixed point over 3 max(rho0, spread)
+      double scale;
+      if (h->cfg.precision == LBGPU_FP16) {
+        const double span = std::max(fabs(rho0[c]), 4.0 * maxdev[c]);
+        scale = span > 0.0 ? span / 1024.0 : 1.0 / 4096.0;
+      } else {
+        scale = i16_scale(rho0[c], maxdev[c]);
+      }
       h->P.rho0[c] = float(rho0[c]);
       h->P.scale[c] = float(scale);
       h->P.inv_scale[c] = float(1.0 / scale);
@@ -439,6 +452,9 @@ extern "C" int lbgpu_init_fields(lbgpu_handle* h, const lbgpu_init* ini) {
   else if (h->cfg.precision == LBGPU_FP32)
     k_init_write<float><<<blocks, kInitThreads, 0, h->stream>>>(I, h->n, h->P, static_cast<float*>(h->f[0]), m,
                                                                  d_count);
+  else if (h->cfg.precision == LBGPU_I16)
+    k_init_write<int16_t><<<blocks, kInitThreads, 0, h->stream>>>(I, h->n, h->P, static_cast<int16_t*>(h->f[0]), m,
+                                                                   d_count);
   else
     k_init_write<__half><<<blocks, kInitThreads, 0, h->stream>>>(I, h->n, h->P, static_cast<__half*>(h->f[0]), m,
                                                                   d_count);

@@ -15,12 +15,21 @@ struct StepEvents {
   cudaEvent_t ev[3];
 };
 
+// z sites per tile row of the pair step (lb_pairs.cuh): 32 lanes x 2
+constexpr int kPairTZ = 64;
+
+// storage of the float-arithmetic forms
+constexpr int kStoreF32 = 0;  // float populations
+constexpr int kStoreF16 = 1;  // half offsets (LBGPU_FP16)
+constexpr int kStoreI16 = 2;  // 16-bit fixed-point offsets (LBGPU_I16)
+
 struct StepBuffers {
   const void* f;        // populations in
   void* fout;           // populations out
   const uint8_t* mask;  // nullptr: no walls
   const uint32_t* nbmask = nullptr;  // neighbour masks (fused step; set iff mask is)
   const uint8_t* tile_walls = nullptr;  // per (x, 8x32 tile) wall flags (fused step)
+  const uint8_t* row_walls = nullptr;   // per (x, y, 64-site z segment) wall flags (pair step)
   int* work_counter = nullptr;          // dynamic scheduling counter (fused step)
   void* rho;            // C*N (double for FP64, float otherwise)
   void* psi;            // C*N
@@ -63,9 +72,16 @@ cudaError_t launch_phase_f16(int phase, int q, int c, const StepBuffers& b, cons
 namespace lbk {
 
 // Fused single-pass D3Q19 step (lb_fused.cuh) for the float-arithmetic
-// forms.  `half_storage` selects half offsets instead of float storage.
-cudaError_t launch_fused(bool half_storage, int c, const StepBuffers& b, const StepParams& P, cudaStream_t stream,
+// forms; `kind` is the storage (kStoreF32 / kStoreF16 / kStoreI16; I16 runs
+// on the pair kernel only).
+cudaError_t launch_fused(int kind, int c, const StepBuffers& b, const StepParams& P, cudaStream_t stream,
                          int64_t* launches, const StepEvents* ev, int device);
+// whether launch_fused runs the pair kernel (lb_pairs.cuh) for this lattice
+bool pairs_eligible(const StepParams& P, const StepBuffers& b);
+// the pair step over the planes [x0, x1) only (every tile), for the host
+// transfers' wavefront; it reads the populations of planes x0 - 2 .. x1 + 1
+cudaError_t launch_fused_range(int kind, int c, const StepBuffers& b, const StepParams& P, int x0, int x1,
+                               cudaStream_t stream, int64_t* launches, int device);
 
 }  // namespace lbk
 
@@ -73,6 +89,7 @@ namespace lbk {
 
 struct FusedParams;
 struct FusedSim;
+struct PairSim;
 
 // float parameters of the fused kernel for tiles of height ty (4 or 8)
 FusedParams make_fused_params(const StepParams& P, int ty);
@@ -84,5 +101,9 @@ FusedParams make_fused_params(const StepParams& P, int ty);
 cudaError_t launch_fused_batch(bool half_storage, int ty, bool walls, const FusedSim* sims, int nsims,
                                int64_t total_work, int parity, int ctas_per_sm, cudaStream_t stream, int device,
                                int64_t total_units, int* counters);
+// The pair-kernel batch (lb_pairs.cuh): members with an even z extent and the
+// BDist2 equilibrium; counters as above (required).
+cudaError_t launch_pairs_batch(int kind, bool walls, const PairSim* sims, int nsims, int parity, int ctas_per_sm,
+                               cudaStream_t stream, int device, int64_t total_units, int* counters);
 
 }  // namespace lbk

@@ -39,6 +39,7 @@ enum int LBGPU_PSI_EXPONENTIAL = 1;
 enum int LBGPU_FP64 = 0;
 enum int LBGPU_FP32 = 1;
 enum int LBGPU_FP16 = 2;
+enum int LBGPU_I16 = 3;
 
 enum int LBGPU_KERNEL_DENSITY_PSI = 0;
 enum int LBGPU_KERNEL_COLLIDE = 1;
@@ -93,6 +94,7 @@ int lbgpu_collide(lbgpu_handle* h);
 int lbgpu_init_fields(lbgpu_handle* h, const(lbgpu_init)* ini);
 int lbgpu_download(lbgpu_handle* h, double** fluids);
 int lbgpu_step_host(lbgpu_handle* h, const(double*)* fluidsIn, const(int)* mask, double** fluidsOut);
+int lbgpu_set_storage_scale(lbgpu_handle* h, const(double)* rho0, const(double)* scale);
 int lbgpu_moments(lbgpu_handle* h, double** density, double** velocity, double* colour);
 int lbgpu_set_record_force(lbgpu_handle* h, int enable);
 int lbgpu_force(lbgpu_handle* h, double** force);

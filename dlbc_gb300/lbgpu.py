@@ -17,8 +17,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liblbgpu.so")
 
-FP64, FP32, FP16 = 0, 1, 2
-PRECISIONS = {"fp64": FP64, "fp32": FP32, "fp16": FP16}
+FP64, FP32, FP16, I16 = 0, 1, 2, 3
+PRECISIONS = {"fp64": FP64, "fp32": FP32, "fp16": FP16, "i16": I16}
 MAXC = 2
 
 ERRORS = {0: "OK", -1: "LBGPU_E_INVALID", -2: "LBGPU_E_NOMEM", -3: "LBGPU_E_CUDA", -4: "LBGPU_E_BUDGET",
@@ -28,7 +28,7 @@ EXPORTED = ["lbgpu_abi_version", "lbgpu_create", "lbgpu_destroy", "lbgpu_upload"
             "lbgpu_advect", "lbgpu_collide",
             "lbgpu_download", "lbgpu_step_host", "lbgpu_moments", "lbgpu_set_record_force", "lbgpu_force", "lbgpu_reduce",
             "lbgpu_synchronize", "lbgpu_set_stream", "lbgpu_profile", "lbgpu_kernel_time",
-            "lbgpu_launch_count", "lbgpu_device_bytes", "lbgpu_last_error"]
+            "lbgpu_launch_count", "lbgpu_device_bytes", "lbgpu_last_error", "lbgpu_set_storage_scale"]
 
 
 class LbgpuConfig(C.Structure):
@@ -75,6 +75,7 @@ def lib() -> C.CDLL:
         L.lbgpu_set_stream.argtypes = [H, C.c_void_p]
         L.lbgpu_profile.argtypes = [H, C.c_int32]
         L.lbgpu_kernel_time.argtypes = [H, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_int64)]
+        L.lbgpu_set_storage_scale.argtypes = [H, C.c_void_p, C.c_void_p]
         L.lbgpu_launch_count.argtypes = [H]
         L.lbgpu_launch_count.restype = C.c_int64
         L.lbgpu_device_bytes.argtypes = [H]
@@ -178,6 +179,16 @@ class GPULattice:
             ptrs[i] = _ptr_of(a)
         self._check(lib().lbgpu_download(self.h, ptrs), "lbgpu_download")
         return out
+
+    def set_storage_scale(self, rho0: Optional[Sequence[float]], scale: Optional[Sequence[float]]) -> None:
+        """FP16 / I16: pin the stored offsets' rest density and scale (None
+        unpins); before the first upload."""
+        if rho0 is None or scale is None:
+            self._check(lib().lbgpu_set_storage_scale(self.h, None, None), "lbgpu_set_storage_scale")
+            return
+        r = np.ascontiguousarray(rho0, dtype=np.float64)
+        s = np.ascontiguousarray(scale, dtype=np.float64)
+        self._check(lib().lbgpu_set_storage_scale(self.h, r.ctypes.data, s.ctypes.data), "lbgpu_set_storage_scale")
 
     def step(self, n: int = 1) -> None:
         self._check(lib().lbgpu_step(self.h, int(n)), "lbgpu_step")

@@ -1,5 +1,5 @@
-"""Precision study: FP32 and FP16-offset storage against FP64 on a large
-spinodal decomposition.
+"""Precision study: FP32, FP16-offset and 16-bit fixed-point (I16) storage
+against FP64 on a large spinodal decomposition.
 
 Two-component D3Q19 Shan-Chen, periodic, rho = 0.7 +- `perturb` per site and
 component (device-side counter-based noise, the same initial state for every
@@ -83,7 +83,7 @@ def main():
                           f"{args.steps} steps, BDist2, g 3.6",
               "fp64": {"time_s": round(t64, 2), "mlups": round(sites * args.steps / t64 / 1e6, 1),
                        "mass_drift": {cp: ref[cp][2] for cp in cps}}}
-    forms = [("fp32", lbgpu.FP32, (0.0, 0.0)), ("fp16", lbgpu.FP16, (0.0, 0.0))]
+    forms = [("fp32", lbgpu.FP32, (0.0, 0.0)), ("fp16", lbgpu.FP16, (0.0, 0.0)), ("i16", lbgpu.I16, (0.0, 0.0))]
     forms += [(f"fp16 origin {v:g}", lbgpu.FP16, (v, v)) for v in args.fp16_origin]
     for name, prec, rho0 in forms:
         res, t = run_form(p, prec, args.steps, cps, args.seed, rho0=rho0)

@@ -1,14 +1,21 @@
 """Serving loop: continuous batching of lattice-Boltzmann requests on one GPU.
 
 Requests (droplet-in-channel simulations of random size and length) arrive
-as a Poisson stream.  A request waits in FIFO order until the batch can admit
-it within the device-memory budget (lbgpu_batch_add_init: its initial
-fields are computed on the device, so nothing but the parameters crosses the
-bus); admitted requests step together in one persistent launch per timestep
-(lbgpu_batch_step); a request leaves the batch the moment it has done its
-steps, which frees its memory for the next waiting request.  The clock is
-real: arrivals are replayed at their times, and a request's latency is its
-completion time minus its arrival time (queueing included).
+as a Poisson stream and wait until the batch can admit them within the
+device-memory budget (lbgpu_batch_add_init: the initial fields are computed
+on the device, so nothing but the parameters crosses the bus).  Admission
+is fit-first with aging: waiting requests are scanned in arrival order and
+every one that fits is admitted, so a large request at the head does not
+hold back smaller ones behind it, until the head has waited longer than
+`age_limit_s`; from then on nothing overtakes it.  Admitted requests step
+together in one persistent launch per timestep (lbgpu_batch_step), in
+chunks of steps that end when the first member finishes and, while the
+budget has room, near the next arrival (estimated from the measured step
+rate), so that a new request joins within a fraction of a chunk; a request
+leaves the batch the moment it has done its steps, which frees its memory
+for the next waiting request.  The clock is real: arrivals are replayed at
+their times, and a request's latency is its completion time minus its
+arrival time (queueing included).
 
 Every member computes exactly what it would compute alone (the batch kernel's
 per-site arithmetic does not depend on the other members), so a request's
@@ -86,11 +93,13 @@ class Server:
     """Continuous-batching loop over one lbgpu batch."""
 
     def __init__(self, precision: int = lbgpu.FP16, budget_bytes: float = 120e9, device: int = 0,
-                 max_chunk: int = 500, keep_state: bool = False):
+                 max_chunk: int = 500, min_chunk: int = 25, age_limit_s: float = 5.0, keep_state: bool = False):
         self.batch = lbgpu.Batch(precision=precision, device=device, hbm_budget_bytes=int(budget_bytes))
         # memberships change constantly: one fixed launch shape, graph replay
         self.batch.set_tuning(autotune=False, tile_height=8, ctas_per_sm=0, use_graph=True)
         self.max_chunk = max_chunk
+        self.min_chunk = min_chunk
+        self.age_limit_s = age_limit_s
         self.keep_state = keep_state
 
     def run(self, requests: List[Request], realtime: bool = True) -> Dict:
@@ -103,6 +112,7 @@ class Server:
         peak_bytes = 0
         t0 = time.perf_counter()
         site_steps = 0
+        step_rate = 0.0  # steps per second of the last chunk
         while pending or waiting or active:
             now = time.perf_counter() - t0
             if not realtime:
@@ -110,16 +120,26 @@ class Server:
                     waiting.append(pending.popleft())
             while pending and pending[0].arrival <= now:
                 waiting.append(pending.popleft())
+            # fit-first admission with aging
+            kept: collections.deque = collections.deque()
+            blocked = False
             while waiting:
-                r = waiting[0]
+                r = waiting.popleft()
+                if blocked:
+                    kept.append(r)
+                    continue
                 try:
                     sid = b.add_device(r.p)
                 except lbgpu.BudgetExceeded:
                     if not active:
                         raise
-                    break
+                    kept.append(r)
+                    # the oldest waiting request has aged: nothing overtakes it
+                    if len(kept) == 1 and now - r.arrival > self.age_limit_s:
+                        blocked = True
+                    continue
                 active[sid] = [r, r.steps, time.perf_counter() - t0]
-                waiting.popleft()
+            waiting = kept
             peak_members = max(peak_members, len(active))
             peak_bytes = max(peak_bytes, b.device_bytes)
             if not active:
@@ -127,9 +147,18 @@ class Server:
                     time.sleep(max(0.0, pending[0].arrival - (time.perf_counter() - t0)))
                 continue
             k = min(self.max_chunk, min(v[1] for v in active.values()))
-            # do not step past the next arrival by much when requests wait for a slot
+            # while nothing waits (the budget had room for every request so
+            # far), end the chunk near the next arrival so that it joins soon;
+            # while requests wait for room, chunks end when a member finishes
+            if pending and not waiting and step_rate > 0.0:
+                until = pending[0].arrival - (time.perf_counter() - t0)
+                k = max(min(k, self.min_chunk), min(k, int(until * step_rate)))
+            t_launch = time.perf_counter()
             b.step(k)
             b.synchronize()
+            dt = time.perf_counter() - t_launch
+            if dt > 0.0:
+                step_rate = k / dt
             site_steps += k * sum(v[0].sites for v in active.values())
             done_t = time.perf_counter() - t0
             for sid in [s for s, v in active.items() if v[1] - k == 0]:
@@ -167,7 +196,7 @@ def main():
     ap.add_argument("--rate", type=float, default=50.0)
     ap.add_argument("--step-scale", type=float, default=1.0)
     ap.add_argument("--budget-gb", type=float, default=120.0)
-    ap.add_argument("--precision", default="fp16", choices=["fp32", "fp16"])
+    ap.add_argument("--precision", default="fp16", choices=["fp32", "fp16", "i16"])
     ap.add_argument("--seed", type=int, default=2024)
     args = ap.parse_args()
     reqs = request_stream(args.requests, args.rate, args.seed, args.step_scale)

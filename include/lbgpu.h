@@ -57,6 +57,8 @@ extern "C" {
 #define LBGPU_FP64 0        /* double storage + double arithmetic: the reference's numbers */
 #define LBGPU_FP32 1        /* float storage + float arithmetic */
 #define LBGPU_FP16 2        /* half storage of f - w_q*rho0 (scaled) + float arithmetic */
+#define LBGPU_I16 3         /* 16-bit fixed-point storage of f/w_q - rho0 (scaled) + float arithmetic;
+                             * D3Q19 with an even z extent and the BDist2 equilibrium only */
 
 typedef struct lbgpu_config {
   int32_t d, q;               /* 3/19 (D3Q19), 2/9 (D2Q9), 1/3 (D1Q3) or 1/5 (D1Q5): gconn
@@ -66,14 +68,14 @@ typedef struct lbgpu_config {
   int32_t shan_chen;          /* lb.force.enableShanChen */
   int32_t psi_form;           /* lb.force.psiForm */
   int32_t eq_form;            /* lb.eqdist.eqDistForm */
-  int32_t precision;          /* LBGPU_FP64 / LBGPU_FP32 / LBGPU_FP16 */
+  int32_t precision;          /* LBGPU_FP64 / LBGPU_FP32 / LBGPU_FP16 / LBGPU_I16 */
   int32_t device;             /* CUDA device ordinal */
   double tau[LBGPU_MAX_COMPONENTS];                        /* lb.tau */
   double gcc[LBGPU_MAX_COMPONENTS][LBGPU_MAX_COMPONENTS];  /* lb.force.gcc */
   double gwc[LBGPU_MAX_COMPONENTS];                        /* lb.force.gwc */
   double global_acc[3];                                    /* lb.force.globalAcc */
-  double rho0[LBGPU_MAX_COMPONENTS];  /* LBGPU_FP16: rest density of the stored offsets
-                                         f_q - w_q*rho0 (0: use the mean density at upload) */
+  double rho0[LBGPU_MAX_COMPONENTS];  /* LBGPU_FP16 / LBGPU_I16: rest density of the stored
+                                         offsets f_q - w_q*rho0 (0: use the mean density at upload) */
 } lbgpu_config;
 
 typedef struct lbgpu_handle lbgpu_handle;
@@ -159,12 +161,25 @@ int lbgpu_download(lbgpu_handle* h, double* const* fluids);
  * fluids_out), bit for bit, for a host that keeps L.fluids as the state and
  * runs hooks on it between steps (runTimeloop's body, src/main.d:179-195,
  * with pre/postAdvection and pre/postCollision hooks registered through
- * src/dlbc/hooks.d:57-118).  In the FP64 form the input copies, the kernels
- * and the output copies run as a wavefront over chunks of x-planes, so both
- * directions of the host link carry data at once.  fluids_out may alias
- * fluids_in; a NULL fluids_out[c] skips component c's output. */
+ * src/dlbc/hooks.d:57-118).  The input copies, the kernels and the output
+ * copies run as a wavefront over chunks of x-planes, so both directions of
+ * the host link carry data at once: in the FP64 form, in FP32, and in FP16 /
+ * I16 once lbgpu_set_storage_scale has pinned their offsets' scale (for
+ * D3Q19 lattices with an even z extent and BDist2; other lattices run the
+ * three calls in turn).  fluids_out may alias fluids_in; a NULL
+ * fluids_out[c] skips component c's output. */
 int lbgpu_step_host(lbgpu_handle* h, const double* const* fluids_in, const int32_t* mask,
                     double* const* fluids_out);
+
+/* FP16 / I16 forms: fix the rest density rho0[c] and the scale[c] of the
+ * stored offsets (f_q = w_q (rho0 + scale h_q), h the stored half or 16-bit
+ * integer) instead of deriving them from each upload's input (mean density,
+ * largest offset).  Call before the first upload or device initialisation;
+ * NULL arrays unpin.  With the scale pinned, lbgpu_upload skips its scan of
+ * the input and lbgpu_step_host of these forms runs as the same wavefront
+ * as FP32 and FP64.  No counterpart in the reference (its fields are double).
+ * LBGPU_E_INVALID for other forms, non-positive scales, or after an upload. */
+int lbgpu_set_storage_scale(lbgpu_handle* h, const double* rho0, const double* scale);
 
 /* Fields as dumpLBData writes them (src/dlbc/lb/io.d:56-101), over the
  * physical lattice, row-major [x][y][z] (+ vector component fastest):

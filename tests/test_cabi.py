@@ -118,3 +118,16 @@ def test_noalloc_rejects_lattices_beyond_the_scratch(libpath):
     cfg = lbgpu.make_config(spinodal((8, 8, 8)), precision=lbgpu.FP16, device=0)
     rc = fn(ctypes.byref(cfg), ctypes.c_void_p(16), ctypes.c_void_p(32), None, None, err, len(err))
     assert rc == -1
+
+
+def test_i16_rejects_lattices_off_the_pair_kernel(libpath):
+    """The 16-bit fixed-point form (LBGPU_I16) runs only on the pair kernel:
+    D3Q19, an even z extent and BDist2.  Other lattices are refused at
+    creation, before any device work."""
+    from lbcases import spinodal
+    L = lbgpu.lib()
+    for p in (spinodal((8, 8, 9)), spinodal((8, 8, 8), eq="SecondOrder"), spinodal((8, 8), d=2)):
+        cfg = lbgpu.make_config(p, precision=lbgpu.I16)
+        h = ctypes.c_void_p()
+        assert L.lbgpu_create(ctypes.byref(cfg), ctypes.byref(h)) == -1 and not h.value
+        assert b"I16" in L.lbgpu_last_error(None)

@@ -28,8 +28,11 @@ def two_spheres(L, tau=1.0, g=3.6, radius=None):
 
 
 def members():
+    # even z extents run the pair kernel, the odd one (21) the one-site-per-
+    # thread fused kernel: one batch step launches both
     return [two_spheres(32, tau=0.9, g=3.5), spinodal((24, 20, 40)), two_spheres(48, tau=1.1, g=3.9),
-            droplet_channel((20, 18, 36), radius=5.0, acc=1e-3, gwc=(0.2, -0.1))]
+            droplet_channel((20, 18, 36), radius=5.0, acc=1e-3, gwc=(0.2, -0.1)),
+            droplet_channel((14, 12, 21), radius=3.0, acc=1e-3, tau=(0.9, 0.9))]
 
 
 def alone(p, precision, steps):
@@ -40,10 +43,12 @@ def alone(p, precision, steps):
     return g.population()
 
 
-@pytest.mark.parametrize("precision", [lbgpu.FP32, lbgpu.FP16])
+@pytest.mark.parametrize("precision", [lbgpu.FP32, lbgpu.FP16, lbgpu.I16])
 @pytest.mark.parametrize("shape", ["autotune", (8, 2), (4, 4), "nograph"])
 def test_batch_members_step_like_lone_lattices(precision, shape):
     ps = members()
+    if precision == lbgpu.I16:  # the I16 form needs an even z extent
+        ps = [p for p in ps if p.gn[2] % 2 == 0]
     steps = 23
     b = lbgpu.Batch(precision=precision)
     if shape == "nograph":

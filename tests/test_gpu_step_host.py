@@ -2,11 +2,14 @@
 sequence it stands for, lbgpu_upload + lbgpu_step(1) + lbgpu_download: the
 same bits, step after step, with the output array used as the next input.
 
-The FP64 form runs as a wavefront over chunks of x-planes (copies in,
-kernels, copies out overlapping); lattices too small for it, profiled
-handles and the FP32/FP16 forms run the three calls in turn.  The launch
-counts tell the two apart: the wavefront launches the step kernels once per
-chunk, the fallback exactly as the sequence does.
+The FP64 form, the FP32 form and (with their storage scale pinned) the
+FP16 and I16 forms run as a wavefront over chunks of x-planes (copies in,
+kernels, copies out overlapping; the reduced forms on the pair kernel, for
+D3Q19 lattices with an even z extent and BDist2); lattices too small for
+it, profiled handles, other reduced-form lattices and unpinned FP16/I16 run
+the three calls in turn.  The launch counts tell the two apart: the
+wavefront launches the step kernels once per chunk, the fallback exactly as
+the sequence does.
 """
 import numpy as np
 import pytest
@@ -30,10 +33,13 @@ def _cases():
     }
 
 
-def _compare(p, precision, steps, wave, pinned=False, record_force=False):
+def _compare(p, precision, steps, wave, pinned=False, record_force=False, scale=None):
     fl, m = init.init_fields(p)
     seq = lbgpu.GPULattice(p, precision=precision)
     one = lbgpu.GPULattice(p, precision=precision)
+    if scale is not None:
+        seq.set_storage_scale(*scale)
+        one.set_storage_scale(*scale)
     if record_force:
         seq.set_record_force(True)
         one.set_record_force(True)
@@ -85,10 +91,33 @@ def test_step_host_pinned_host_arrays():
     _compare(p, lbgpu.FP64, 3, True, pinned=True)
 
 
+# pinned offsets: rest density and scale per component
+SCALES = {lbgpu.FP16: ((0.5, 0.5), (1.0 / 1024, 1.0 / 1024)), lbgpu.I16: ((0.5, 0.5), (3.0 / 32767, 3.0 / 32767))}
+
+
+@pytest.mark.parametrize("precision", [lbgpu.FP32, lbgpu.FP16, lbgpu.I16])
+@pytest.mark.parametrize("pin", [False, True])
+def test_step_host_reduced_forms(precision, pin):
+    """FP32 runs the wavefront; FP16 and I16 run it once their scale is
+    pinned, the three calls otherwise (the upload derives the scale from the
+    whole input).  Walls with the wall force: the wavefront's upload writes
+    the solid sites into both population buffers."""
+    if precision == lbgpu.FP32 and pin:
+        pytest.skip("FP32 has no storage scale")
+    p = droplet_channel((40, 12, 14), radius=4.0, acc=1e-3, gwc=(0.3, -0.2))
+    _compare(p, precision, 3, precision == lbgpu.FP32 or pin, record_force=True,
+             scale=SCALES[precision] if pin else None)
+
+
+def test_step_host_fp32_off_the_pair_kernel_runs_the_sequence():
+    p = spinodal((37, 10, 9))  # odd z extent: the one-site-per-thread kernel
+    _compare(p, lbgpu.FP32, 3, False)
+
+
 @pytest.mark.parametrize("precision", [lbgpu.FP32, lbgpu.FP16])
-def test_step_host_reduced_forms_run_the_sequence(precision):
-    p = droplet_channel((40, 12, 14), radius=4.0, acc=1e-3)
-    _compare(p, precision, 3, False)
+def test_step_host_full_size_channel_reduced(precision):
+    p = droplet_channel((256, 128, 128), radius=24.0, acc=1e-6)
+    _compare(p, precision, 2, True, pinned=True, scale=SCALES.get(precision))
 
 
 def test_step_host_full_size_channel():
