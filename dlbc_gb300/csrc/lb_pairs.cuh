@@ -250,6 +250,10 @@ struct PairShared {
   float rho[WALLS ? 4 : 1][C][kPairTY + 2][WALLS ? kPairRZ : 1];  // the wall force reads solid neighbours' density
   // tau != 1: the row warps' gathered words of the next plane, [buffer][c][q][row][lane]
   typename PairIO<T>::W pops[MOM ? 1 : 2][C][MOM ? 1 : 19][MOM ? 1 : kPairTY][32];
+  // tau = 1: the row warps' density and momentum of the next plane,
+  // [buffer][c][rho, jx, jy, jz][row][lane] (kept here rather than in
+  // registers across the gather of the following plane)
+  float2 mom[MOM ? 2 : 1][C][4][MOM ? kPairTY : 1][32];
 };
 
 // BDist2 equilibrium constants of one component for one pair: value_q =
@@ -352,7 +356,6 @@ __device__ __forceinline__ void pair_body(const FusedParams& P, const T* __restr
     // moments, psi and neighbour masks of the plane the row warp collides
     // next (cur) and of the plane it gathers (nxt)
     PairMom<float2> m_cur[C], m_nxt[C];
-    float2 psi_cur[C], psi_nxt[C];
     uint2 nb_cur = make_uint2(0u, 0u), nb_nxt = make_uint2(0u, 0u);
     bool wr_cur = false, wr_nxt = false;
 
@@ -405,6 +408,9 @@ __device__ __forceinline__ void pair_body(const FusedParams& P, const T* __restr
           }
           if (!MOM && keep >= 0 && !ring_warp) sh.pops[keep][c][q][warp][lane] = word;
           v[q] = IO::val(word);
+#ifdef LB_PAIRS_SPLIT_LOADS
+          if (q == 9) __syncwarp();
+#endif
         }
         m[c] = pair_moments<OFF>(v, s36[c], P.rho0[c]);
         ps2[c] = make_float2(pair_psi(m[c].rho.x, P.psi_form), pair_psi(m[c].rho.y, P.psi_form));
@@ -412,12 +418,21 @@ __device__ __forceinline__ void pair_body(const FusedParams& P, const T* __restr
           *reinterpret_cast<float2*>(&sh.psi[ps][c][r][2 + 2 * lane]) = ps2[c];
           if (WALLS) *reinterpret_cast<float2*>(&sh.rho[ps][c][r][2 + 2 * lane]) = m[c].rho;
         }
+        // one component's loads in flight at a time: the next component's
+        // loads are not hoisted above this point, which bounds the live
+        // registers (two components' 38 words would spill)
+        __syncwarp();
       }
       if (keep >= 0 && !ring_warp) {
 #pragma unroll
         for (int c = 0; c < C; ++c) {
-          m_nxt[c] = m[c];
-          psi_nxt[c] = ps2[c];
+          if (MOM) {
+            sh.mom[keep][c][0][warp][lane] = m[c].rho;
+#pragma unroll
+            for (int vd = 0; vd < 3; ++vd) sh.mom[keep][c][1 + vd][warp][lane] = m[c].j[vd];
+          } else {
+            m_nxt[c] = m[c];
+          }
         }
         nb_nxt = nb;
         wr_nxt = walled;
@@ -466,10 +481,9 @@ __device__ __forceinline__ void pair_body(const FusedParams& P, const T* __restr
     for (int k = 0; k < run; ++k) {
       const int x = xs + k;
       const int sm = k % 4, s0 = (k + 1) % 4, sp = (k + 2) % 4;  // psi slots of x-1, x, x+1
+      if (!MOM) {
 #pragma unroll
-      for (int c = 0; c < C; ++c) {
-        m_cur[c] = m_nxt[c];
-        psi_cur[c] = psi_nxt[c];
+        for (int c = 0; c < C; ++c) m_cur[c] = m_nxt[c];
       }
       nb_cur = nb_nxt;
       wr_cur = wr_nxt;
@@ -485,11 +499,21 @@ __device__ __forceinline__ void pair_body(const FusedParams& P, const T* __restr
         // ------------------------------------------------------------------
         const uint32_t own = uint32_t(x) * plane_sz + r3[1];
         const int zi = 2 + 2 * lane;
+        if (MOM) {
+#pragma unroll
+          for (int c = 0; c < C; ++c) {
+            m_cur[c].rho = sh.mom[cur][c][0][warp][lane];
+#pragma unroll
+            for (int vd = 0; vd < 3; ++vd) m_cur[c].j[vd] = sh.mom[cur][c][1 + vd][warp][lane];
+          }
+        }
         const int slot[3] = {sm, s0, sp};  // by c_x + 1
         const bool walled = WALLS && wr_cur;
         uint32_t any = 0u;
         if (walled) any = __reduce_or_sync(__activemask(), nb_cur.x | nb_cur.y);
         const bool solid0 = WALLS && (nb_cur.x & 1u), solid1 = WALLS && (nb_cur.y & 1u);
+        // psi of this lane's own sites (written by its own gather of plane x)
+        auto psi_own = [&](int c) { return *reinterpret_cast<const float2*>(&sh.psi[s0][c][r][zi]); };
         // --- Shan-Chen: S_c = sum_q w_q psi_c(x + c_q) c_q
         float2 F[C][3];
 #pragma unroll
@@ -519,8 +543,9 @@ __device__ __forceinline__ void pair_body(const FusedParams& P, const T* __restr
                 v = make_float2(Lv(cx, cy), m.x);
               }
               if (walled && ((any >> q) & 1u)) {
-                if ((nb_cur.x >> q) & 1u) v.x = psi_cur[c].x;
-                if ((nb_cur.y >> q) & 1u) v.y = psi_cur[c].y;
+                const float2 own_psi = psi_own(c);
+                if ((nb_cur.x >> q) & 1u) v.x = own_psi.x;
+                if ((nb_cur.y >> q) & 1u) v.y = own_psi.y;
               }
               return v;
             };
@@ -547,7 +572,8 @@ __device__ __forceinline__ void pair_body(const FusedParams& P, const T* __restr
 #pragma unroll
               for (int vd = 0; vd < 3; ++vd) g[vd] = vfma(cc, S[f2][vd], g[vd]);
             }
-            const float2 mp = make_float2(-psi_cur[f1].x, -psi_cur[f1].y);
+            const float2 own_psi = psi_own(f1);
+            const float2 mp = make_float2(-own_psi.x, -own_psi.y);
 #pragma unroll
             for (int vd = 0; vd < 3; ++vd) F[f1][vd] = vmul(mp, g[vd]);
             if (walled && P.gwc[f1] != 0.f && any != 0u) {
@@ -569,7 +595,7 @@ __device__ __forceinline__ void pair_body(const FusedParams& P, const T* __restr
                 if (cz > 0) acc[2] = vadd(acc[2], v);
                 if (cz < 0) acc[2] = vsub(acc[2], v);
               }
-              const float2 wc = vmul(psi_cur[f1], splat<float2>(P.gwc[f1]));
+              const float2 wc = vmul(own_psi, splat<float2>(P.gwc[f1]));
 #pragma unroll
               for (int vd = 0; vd < 3; ++vd)
                 F[f1][vd] = vsub(F[f1][vd],
