@@ -57,7 +57,8 @@ import dlbc.logging;
 
 /// Run the timestep on the GPU.
 @("param") bool enableGpu;
-/// Arithmetic form: "fp64" (the reference's numbers), "fp32" or "fp16".
+/// Arithmetic form: "fp64" (the reference's numbers), "fp32", "fp16" or
+/// "i16" (16-bit fixed-point storage; D3Q19, even z extent, BDist2).
 @("param") string precision = "fp64";
 /// CUDA device ordinal.
 @("param") int device;
@@ -97,7 +98,8 @@ lbgpu_config makeConfig(T)(ref T L) if ( isLattice!T ) {
   case "fp64": c.precision = LBGPU_FP64; break;
   case "fp32": c.precision = LBGPU_FP32; break;
   case "fp16": c.precision = LBGPU_FP16; break;
-  default: writeLogF("gpu.precision must be fp64, fp32 or fp16, not `%s'.", precision);
+  case "i16": c.precision = LBGPU_I16; break;
+  default: writeLogF("gpu.precision must be fp64, fp32, fp16 or i16, not `%s'.", precision);
   }
   c.device = device;
   foreach(immutable f; 0..components) {
