@@ -369,15 +369,11 @@ __device__ __forceinline__ void pair_body(const FusedParams& P, const T* __restr
       const uint32_t own = p3[1] + r3[1];
       bool walled = false;
       uint2 nb = make_uint2(0u, 0u);
-      uint32_t any = 0u;
       // (a batch runs its wall-free members in the walled kernel too: no
       // flags, no masks)
       if (WALLS && row_walls) {
         walled = __ldg(row_walls + (size_t(xg) * P.ny + size_t(y)) * P.tiles_z + ztile) != 0;
-        if (walled) {
-          nb = active ? __ldg(reinterpret_cast<const uint2*>(nbmask + own)) : make_uint2(0u, 0u);
-          any = __reduce_or_sync(0xffffffffu, nb.x | nb.y);
-        }
+        if (walled && active) nb = __ldg(reinterpret_cast<const uint2*>(nbmask + own));
       }
       const bool solid0 = nb.x & 1u, solid1 = nb.y & 1u;
       PairMom<float2> m[C];
@@ -392,18 +388,22 @@ __device__ __forceinline__ void pair_body(const FusedParams& P, const T* __restr
           W word = IO::ld(fc[c] + off);
           if (cz == 1) word = IO::up(word, lane0, fc[c] + (off + uint32_t(dl)));
           if (cz == -1) word = IO::down(word, lastl, fc[c] + (off + uint32_t(dr)));
+          // walls, per lane and without branches, so that these loads are
+          // in flight together with the others (a branch per population
+          // would wait for each load in turn)
           if (WALLS && walled && q > 0) {
             // bounce-back: x - c_q = x + c_b solid, the site fluid
             const int b = Conn<19>::bounce(q);
-            if ((any >> b) & 1u) {
-              const W mine = IO::ld(fc[c] + (own + P.qn[b]));
-              word = IO::sel(word, mine, ((nb.x >> b) & 1u) && !solid0, ((nb.y >> b) & 1u) && !solid1);
-            }
+            const bool t0 = ((nb.x >> b) & 1u) && !solid0, t1 = ((nb.y >> b) & 1u) && !solid1;
+            W mine = word;
+            if (t0 || t1) mine = IO::ld(fc[c] + (own + P.qn[b]));
+            word = IO::sel(word, mine, t0, t1);
           }
-          if (WALLS && walled && need_solid && (any & 1u)) {
+          if (WALLS && walled && need_solid) {
             // solid sites keep their own populations (their density is the
             // wall force's wall density)
-            const W mine = IO::ld(fc[c] + (own + P.qn[q]));
+            W mine = word;
+            if (solid0 || solid1) mine = IO::ld(fc[c] + (own + P.qn[q]));
             word = IO::sel(word, mine, solid0, solid1);
           }
           if (!MOM && keep >= 0 && !ring_warp) sh.pops[keep][c][q][warp][lane] = word;
@@ -528,8 +528,9 @@ __device__ __forceinline__ void pair_body(const FusedParams& P, const T* __restr
             };
             auto Lv = [&](int dx, int dy) { return sh.psi[slot[dx + 1]][c][r + dy][zi - 1]; };
             auto Rv = [&](int dx, int dy) { return sh.psi[slot[dx + 1]][c][r + dy][zi + 2]; };
+            const float2 own_psi = walled ? psi_own(c) : make_float2(0.f, 0.f);
             // psi_c(x + c_q) at both sites, a solid neighbour replaced by the
-            // site's own psi
+            // site's own psi (per lane, without branches)
             auto nbv = [&](int q) -> float2 {
               const int cx = Conn<19>::cx(q), cy = Conn<19>::cy(q), cz = Conn<19>::cz(q);
               float2 v;
@@ -542,10 +543,9 @@ __device__ __forceinline__ void pair_body(const FusedParams& P, const T* __restr
                 const float2 m = M(cx, cy);
                 v = make_float2(Lv(cx, cy), m.x);
               }
-              if (walled && ((any >> q) & 1u)) {
-                const float2 own_psi = psi_own(c);
-                if ((nb_cur.x >> q) & 1u) v.x = own_psi.x;
-                if ((nb_cur.y >> q) & 1u) v.y = own_psi.y;
+              if (walled) {
+                v.x = ((nb_cur.x >> q) & 1u) ? own_psi.x : v.x;
+                v.y = ((nb_cur.y >> q) & 1u) ? own_psi.y : v.y;
               }
               return v;
             };
