@@ -112,6 +112,10 @@ struct PairIO<float> {
   static constexpr int kLeftEdge = 0;
   __device__ static __forceinline__ W ld(const float* p) { return __ldg(reinterpret_cast<const float2*>(p)); }
   __device__ static __forceinline__ float ld1(const float* p) { return __ldg(p); }
+  // one site's stored value, and a word from two of them
+  using R = float;
+  __device__ static __forceinline__ R ldraw(const float* p) { return __ldg(p); }
+  __device__ static __forceinline__ W pack(R lo, R hi) { return make_float2(lo, hi); }
   // (f(z-1), f(z)) from the pair (f(z), f(z+1)): the lane below's upper site,
   // or at the warp's left edge one load at edge_p (the site z0 - 1)
   __device__ static __forceinline__ W up(W w, bool lane0, const float* edge_p) {
@@ -146,6 +150,9 @@ struct PairIO16 {
   static constexpr bool kOffsets = true;
   static constexpr int kLeftEdge = -1;
   __device__ static __forceinline__ W ld(const T* p) { return __ldg(reinterpret_cast<const unsigned int*>(p)); }
+  using R = unsigned short;
+  __device__ static __forceinline__ R ldraw(const T* p) { return __ldg(reinterpret_cast<const unsigned short*>(p)); }
+  __device__ static __forceinline__ W pack(R lo, R hi) { return uint32_t(lo) | (uint32_t(hi) << 16); }
   __device__ static __forceinline__ W up(W w, bool lane0, const T* edge_p) {
     W prev = __shfl_up_sync(0xffffffffu, w, 1);
     if (lane0) prev = __ldg(reinterpret_cast<const unsigned int*>(edge_p));
@@ -336,6 +343,10 @@ __device__ __forceinline__ void pair_body(const FusedParams& P, const T* __restr
     const int zleft = z0 > 0 ? z0 - 1 : P.nz - 1;
     const int zright = z0 + tzv < P.nz ? z0 + tzv : 0;
     const int dl = zleft + IO::kLeftEdge - zl, dr = zright - zl;
+    // walled rows' per-site loads: source z - c_z of the sites zl and zl + 1
+    // relative to zl, indexed by 1 - c_z (periodic)
+    const uint32_t zd0[3] = {uint32_t(zl > 0 ? -1 : P.nz - 1), 0u, 1u};
+    const uint32_t zd1[3] = {0u, 1u, uint32_t(zl + 2 < P.nz ? 2 : 2 - P.nz)};
     const uint32_t r3[3] = {uint32_t(wrap(y - 1, P.ny)) * uint32_t(P.nz) + uint32_t(zl),
                             uint32_t(y) * uint32_t(P.nz) + uint32_t(zl),
                             uint32_t(wrap(y + 1, P.ny)) * uint32_t(P.nz) + uint32_t(zl)};
@@ -385,26 +396,27 @@ __device__ __forceinline__ void pair_body(const FusedParams& P, const T* __restr
         for (int q = 0; q < 19; ++q) {
           const int cx = Conn<19>::cx(q), cy = Conn<19>::cy(q), cz = Conn<19>::cz(q);
           const uint32_t off = p3[1 - cx] + r3[1 - cy] + P.qn[q];
-          W word = IO::ld(fc[c] + off);
-          if (cz == 1) word = IO::up(word, lane0, fc[c] + (off + uint32_t(dl)));
-          if (cz == -1) word = IO::down(word, lastl, fc[c] + (off + uint32_t(dr)));
-          // walls, per lane and without branches, so that these loads are
-          // in flight together with the others (a branch per population
-          // would wait for each load in turn)
-          if (WALLS && walled && q > 0) {
-            // bounce-back: x - c_q = x + c_b solid, the site fluid
-            const int b = Conn<19>::bounce(q);
-            const bool t0 = ((nb.x >> b) & 1u) && !solid0, t1 = ((nb.y >> b) & 1u) && !solid1;
-            W mine = word;
-            if (t0 || t1) mine = IO::ld(fc[c] + (own + P.qn[b]));
-            word = IO::sel(word, mine, t0, t1);
-          }
-          if (WALLS && walled && need_solid) {
-            // solid sites keep their own populations (their density is the
-            // wall force's wall density)
-            W mine = word;
-            if (solid0 || solid1) mine = IO::ld(fc[c] + (own + P.qn[q]));
-            word = IO::sel(word, mine, solid0, solid1);
+          W word;
+          if (WALLS && walled) {
+            // rows next to a wall: one load per site, its address chosen
+            // per site without branches (bounce-back: x - c_q = x + c_b
+            // solid and the site fluid, the site's own population b; a solid
+            // site its own population, whose density the wall force reads)
+            uint32_t o0 = off + zd0[1 - cz], o1 = off + zd1[1 - cz];
+            if (q > 0) {
+              const int b = Conn<19>::bounce(q);
+              if (((nb.x >> b) & 1u) && !solid0) o0 = own + P.qn[b];
+              if (((nb.y >> b) & 1u) && !solid1) o1 = own + 1u + P.qn[b];
+            }
+            if (need_solid) {
+              if (solid0) o0 = own + P.qn[q];
+              if (solid1) o1 = own + 1u + P.qn[q];
+            }
+            word = IO::pack(IO::ldraw(fc[c] + o0), IO::ldraw(fc[c] + o1));
+          } else {
+            word = IO::ld(fc[c] + off);
+            if (cz == 1) word = IO::up(word, lane0, fc[c] + (off + uint32_t(dl)));
+            if (cz == -1) word = IO::down(word, lastl, fc[c] + (off + uint32_t(dr)));
           }
           if (!MOM && keep >= 0 && !ring_warp) sh.pops[keep][c][q][warp][lane] = word;
           v[q] = IO::val(word);
@@ -833,12 +845,12 @@ cudaError_t go_pairs(const StepBuffers& b, const FusedParams& F, cudaStream_t st
   if (e != cudaSuccess) return e;
   int64_t grid = int64_t(per_sm) * sm_count(device);
   FusedParams G = F;
-  // runs of 32 planes, halved while there would be fewer than two runs per
+  // runs of 32 planes, halved while there would be fewer than 1.5 runs per
   // CTA (each run gathers two extra planes to warm up)
   const int64_t tiles = int64_t(G.tiles_y) * G.tiles_z;
   const int span = G.x_end - G.x_begin;
   int rl = 32;
-  while (rl > 4 && tiles * ((span + rl - 1) / rl) < 2 * grid) rl /= 2;
+  while (rl > 4 && 2 * tiles * ((span + rl - 1) / rl) < 3 * grid) rl /= 2;
   G.run_len = rl < span ? rl : span;
   const int64_t units = tiles * ((span + G.run_len - 1) / G.run_len);
   if (grid > units) grid = units;

@@ -136,6 +136,23 @@ def test_pairs_translation_invariant_bitwise(precision, shift):
 
 
 @pytest.mark.parametrize("precision", [lbgpu.FP32, lbgpu.FP16, lbgpu.I16])
+@pytest.mark.parametrize("shift", [(3, 5, 0), (1, 8, 0)])
+def test_pairs_walled_channel_translation_invariant_bitwise(precision, shift):
+    """The same with z walls (shifted along x and y only): rows next to a
+    wall take their populations one site at a time (bounce-back chosen per
+    site), the wall force reads the solid sites' densities, and still every
+    site computes the same bits wherever it sits."""
+    p = droplet_channel((12, 20, 70), radius=4.0, acc=1e-3, gwc=(0.2, -0.1))
+    fl, m = init.init_fields(p)
+    a, fa = _run(p, 15, precision, fields=(fl, m), rho0=(0.5, 0.5))
+    fs, ms = _shifted(fl, m, shift)
+    b, fb = _run(p, 15, precision, fields=(fs, ms), rho0=(0.5, 0.5))
+    for c in range(2):
+        assert np.array_equal(np.roll(a[c], shift, axis=(0, 1, 2)), b[c]), c
+        assert np.array_equal(np.roll(fa[c], shift, axis=(0, 1, 2)), fb[c], equal_nan=True), c
+
+
+@pytest.mark.parametrize("precision", [lbgpu.FP32, lbgpu.FP16, lbgpu.I16])
 def test_pairs_conserve_mass_over_phase_separation(precision):
     """A spinodal decomposition through phase separation: the total mass of
     each component drifts by rounding only, the total momentum stays at its
