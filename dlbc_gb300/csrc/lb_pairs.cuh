@@ -111,12 +111,11 @@ struct PairIO<float> {
   // FP32 loads the neighbour's value itself
   static constexpr int kLeftEdge = 0;
   __device__ static __forceinline__ W ld(const float* p) { return __ldg(reinterpret_cast<const float2*>(p)); }
-  // one site's value (element off of the array at base)
-  __device__ static __forceinline__ float ld1(const float* base, uint32_t off) { return __ldg(base + off); }
-  // a word from two sites' elements o0 and o1
-  __device__ static __forceinline__ W ld2(const float* base, uint32_t o0, uint32_t o1) {
-    return make_float2(__ldg(base + o0), __ldg(base + o1));
-  }
+  __device__ static __forceinline__ float ld1(const float* p) { return __ldg(p); }
+  // one site's stored value, and a word from two of them
+  using R = float;
+  __device__ static __forceinline__ R ldraw(const float* p) { return __ldg(p); }
+  __device__ static __forceinline__ W pack(R lo, R hi) { return make_float2(lo, hi); }
   // (f(z-1), f(z)) from the pair (f(z), f(z+1)): the lane below's upper site,
   // or at the warp's left edge one load at edge_p (the site z0 - 1)
   __device__ static __forceinline__ W up(W w, bool lane0, const float* edge_p) {
@@ -151,20 +150,9 @@ struct PairIO16 {
   static constexpr bool kOffsets = true;
   static constexpr int kLeftEdge = -1;
   __device__ static __forceinline__ W ld(const T* p) { return __ldg(reinterpret_cast<const unsigned int*>(p)); }
-  // single elements come from the aligned 32-bit word holding them (every
-  // array starts on a 4-byte boundary: q n is even when nz is), not from
-  // 16-bit loads, which the memory pipeline serves far more slowly here
-  __device__ static __forceinline__ uint32_t word_of(const T* base, uint32_t off) {
-    return __ldg(reinterpret_cast<const unsigned int*>(base + (off & ~1u)));
-  }
-  // the 16 bits of element off
-  __device__ static __forceinline__ uint32_t bits1(const T* base, uint32_t off) {
-    return __byte_perm(word_of(base, off), 0u, (off & 1u) ? 0x4432u : 0x4410u);
-  }
-  __device__ static __forceinline__ W ld2(const T* base, uint32_t o0, uint32_t o1) {
-    const uint32_t sel = ((o0 & 1u) ? 0x32u : 0x10u) | ((o1 & 1u) ? 0x7600u : 0x5400u);
-    return __byte_perm(word_of(base, o0), word_of(base, o1), sel);
-  }
+  using R = unsigned short;
+  __device__ static __forceinline__ R ldraw(const T* p) { return __ldg(reinterpret_cast<const unsigned short*>(p)); }
+  __device__ static __forceinline__ W pack(R lo, R hi) { return uint32_t(lo) | (uint32_t(hi) << 16); }
   __device__ static __forceinline__ W up(W w, bool lane0, const T* edge_p) {
     W prev = __shfl_up_sync(0xffffffffu, w, 1);
     if (lane0) prev = __ldg(reinterpret_cast<const unsigned int*>(edge_p));
@@ -184,10 +172,7 @@ struct PairIO16 {
 
 template <>
 struct PairIO<__half> : PairIO16<__half> {
-  __device__ static __forceinline__ float ld1(const __half* base, uint32_t off) {
-    const unsigned short b = static_cast<unsigned short>(bits1(base, off));
-    return __half2float(__ushort_as_half(b));
-  }
+  __device__ static __forceinline__ float ld1(const __half* p) { return __half2float(__ldg(p)); }
   __device__ static __forceinline__ float2 val(W w) {
     __half2 h;
     *reinterpret_cast<W*>(&h) = w;
@@ -213,9 +198,7 @@ __device__ __forceinline__ uint32_t pack_s16x2(float a, float b) {
 
 template <>
 struct PairIO<int16_t> : PairIO16<int16_t> {
-  __device__ static __forceinline__ float ld1(const int16_t* base, uint32_t off) {
-    return float(int16_t(bits1(base, off)));
-  }
+  __device__ static __forceinline__ float ld1(const int16_t* p) { return float(__ldg(p)); }
   __device__ static __forceinline__ float2 val(W w) {
     return make_float2(float(int16_t(w & 0xffffu)), float(int16_t(w >> 16)));
   }
@@ -429,7 +412,7 @@ __device__ __forceinline__ void pair_body(const FusedParams& P, const T* __restr
               if (solid0) o0 = own + P.qn[q];
               if (solid1) o1 = own + 1u + P.qn[q];
             }
-            word = IO::ld2(fc[c], o0, o1);
+            word = IO::pack(IO::ldraw(fc[c] + o0), IO::ldraw(fc[c] + o1));
           } else {
             word = IO::ld(fc[c] + off);
             if (cz == 1) word = IO::up(word, lane0, fc[c] + (off + uint32_t(dl)));
@@ -490,7 +473,7 @@ __device__ __forceinline__ void pair_body(const FusedParams& P, const T* __restr
             if (bb) off = own + P.qn[b];
             if (solid && need_solid) off = own + P.qn[q];
           }
-          v[q] = IO::ld1(fc[c], off);
+          v[q] = IO::ld1(fc[c] + off);
         }
         const PairMom<float> m = pair_moments<OFF>(v, s36[c], P.rho0[c]);
         sh.psi[ps][c][lane][zr_i] = pair_psi(m.rho, P.psi_form);
