@@ -1204,11 +1204,10 @@ int lbgpu_step_host(lbgpu_handle* h, const double* const* fluids_in, const int32
     if (!fluids_in[c]) return h->fail(LBGPU_E_INVALID, "null fluid array");
   if (h->lite || !h->rho) return h->fail(LBGPU_E_INVALID, "batch members step with their batch");
   if (h->advected) return h->fail(LBGPU_E_NOTREADY, "lbgpu_step_host between lbgpu_advect and lbgpu_collide");
-  // the wavefront: FP64, and the fused forms on the pair kernel (FP16 and I16
-  // once their offsets' scale is pinned: otherwise the upload derives it
-  // from the whole input first)
-  const bool fused_wave = h->fused && h->P.nz % 2 == 0 && h->P.eq_form == LBGPU_EQ_BDIST2 && h->work_counter &&
-                          (h->cfg.precision == LBGPU_FP32 || h->scale_pinned);
+  // the wavefront: FP64, and the fused forms (FP16 and I16 once their
+  // offsets' scale is pinned: otherwise the upload derives it from the whole
+  // input first)
+  const bool fused_wave = h->fused && h->work_counter && (h->cfg.precision == LBGPU_FP32 || h->scale_pinned);
   const int K = ((h->cfg.precision == LBGPU_FP64 || fused_wave) && !h->profiling) ? wave_planes(h) : 0;
   if (K == 0) {
     // the other forms, profiled handles and lattices too small for the

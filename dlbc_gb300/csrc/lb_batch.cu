@@ -114,8 +114,11 @@ std::string signature(const lbgpu_batch* b) {
 }
 
 // whether a member runs the pair kernel (the rule launch_fused applies to a
-// lone lattice)
-bool pair_member(const lbgpu_handle* h) { return h->nz % 2 == 0 && h->P.eq_form == 2; }
+// lone lattice, lbk::pairs_eligible)
+bool pair_member(const lbgpu_handle* h) {
+  if (!(h->nz % 2 == 0 && h->P.eq_form == 2)) return false;
+  return h->cfg.precision == LBGPU_I16 || (h->P.unit_tau != 0 && h->mask == nullptr);
+}
 
 template <typename D>
 int upload_table(lbgpu_batch* b, const std::vector<D>& tab, D** d_tab, int* cap) {

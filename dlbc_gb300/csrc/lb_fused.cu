@@ -54,34 +54,47 @@ FusedParams make_fused_params(const StepParams& P, int ty) {
 }
 
 
-bool pairs_eligible(const StepParams& P, const StepBuffers& b) {
+bool pairs_eligible(int kind, const StepParams& P, const StepBuffers& b) {
   // aligned two-site words need an even z extent; the pair kernel computes
   // the BDist2 equilibrium and schedules through the work counter
-  return P.nz % 2 == 0 && P.eq_form == 2 && b.work_counter != nullptr && (b.mask == nullptr || b.row_walls != nullptr);
+  if (!(P.nz % 2 == 0 && P.eq_form == 2 && b.work_counter != nullptr && (b.mask == nullptr || b.row_walls != nullptr)))
+    return false;
+  // I16 runs on the pair kernel only; FP32 and FP16 where it is the faster
+  // kernel: every tau = 1 and no solid site (measured on GB300: walls and
+  // the relaxation's shared-memory populations favour one site per thread)
+  return kind == kStoreI16 || (P.unit_tau != 0 && b.mask == nullptr);
 }
 
-// the pair step over planes [x0, x1) of every tile (the host transfers
-// wavefront): reads the populations of planes x0 - 2 .. x1 + 1 (periodic)
+// the fused step over planes [x0, x1) of every tile (the host transfers
+// wavefront; the pair kernel or the one-site-per-thread kernel, whichever
+// launch_fused would run): reads the populations of planes x0 - 2 .. x1 + 1
+// (periodic)
 cudaError_t launch_fused_range(int kind, int c, const StepBuffers& b, const StepParams& P, int x0, int x1,
                                cudaStream_t st, int64_t* launches, int device) {
   if (x1 <= x0) return cudaSuccess;
-  if (!pairs_eligible(P, b)) return cudaErrorInvalidValue;
+  if (!b.work_counter) return cudaErrorInvalidValue;
   FusedParams G = make_fused_params(P, 8);
   G.tile_walls = b.tile_walls;
   G.work_counter = b.work_counter;
-  G.tiles_y = (P.ny + 7) / 8;
-  G.tiles_z = (P.nz + kPairTZ - 1) / kPairTZ;
-  G.work = int64_t(G.tiles_y) * G.tiles_z * P.nx;
   G.x_begin = x0;
   G.x_end = x1;
   cudaMemsetAsync(b.work_counter, 0, sizeof(int), st);
   const bool w = b.mask != nullptr;
   if (w && !b.nbmask) return cudaErrorInvalidValue;
-  const bool mom = P.unit_tau != 0;
   *launches += 1;
-  return kind == kStoreF16   ? launch_pairs_single_f16(c, w, mom, b, G, st, device)
-         : kind == kStoreI16 ? launch_pairs_single_i16(c, w, mom, b, G, st, device)
-                             : launch_pairs_single_f32(c, w, mom, b, G, st, device);
+  if (pairs_eligible(kind, P, b)) {
+    G.tiles_y = (P.ny + 7) / 8;
+    G.tiles_z = (P.nz + kPairTZ - 1) / kPairTZ;
+    G.work = int64_t(G.tiles_y) * G.tiles_z * P.nx;
+    const bool mom = P.unit_tau != 0;
+    return kind == kStoreF16   ? launch_pairs_single_f16(c, w, mom, b, G, st, device)
+           : kind == kStoreI16 ? launch_pairs_single_i16(c, w, mom, b, G, st, device)
+                               : launch_pairs_single_f32(c, w, mom, b, G, st, device);
+  }
+  if (kind == kStoreI16) return cudaErrorInvalidValue;
+  const bool mom = c == 2 && P.unit_tau && P.eq_form == 2;
+  return kind == kStoreF16 ? launch_fused_single_f16(c, w, mom, b, G, st, device)
+                           : launch_fused_single_f32(c, w, mom, b, G, st, device);
 }
 
 cudaError_t launch_fused(int kind, int c, const StepBuffers& b, const StepParams& P, cudaStream_t st,
@@ -101,7 +114,7 @@ cudaError_t launch_fused(int kind, int c, const StepBuffers& b, const StepParams
     cudaEventRecord(ev->ev[1], st);
   }
   cudaError_t e;
-  if (pairs_eligible(P, b)) {
+  if (pairs_eligible(kind, P, b)) {
     // two z-adjacent sites per thread (lb_pairs.cuh): 8 x 64 tiles
     FusedParams G = F;
     G.tiles_y = (P.ny + 7) / 8;

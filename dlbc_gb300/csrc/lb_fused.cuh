@@ -78,7 +78,8 @@ struct FusedParams {
   // in planes; nullptr: static equal ranges
   int* work_counter;
   int32_t run_len;
-  // the pair kernel's plane range [x_begin, x_end) (the whole lattice: 0, nx)
+  // plane range [x_begin, x_end) of the dynamically scheduled kernels (the
+  // whole lattice: 0, nx)
   int32_t x_begin, x_end;
 };
 
@@ -528,7 +529,7 @@ __global__ void __launch_bounds__(TY * kFusedTZ, MOM ? (8 / TY) * mom_ctas<WALLS
   // time and the ring sites one gathers are still in L2 when the other
   // reads them (8-12 % faster than tile-major order)
   __shared__ int s_item;
-  const int nchunks = (P.nx + P.run_len - 1) / P.run_len;
+  const int nchunks = (P.x_end - P.x_begin + P.run_len - 1) / P.run_len;
   const int units = P.tiles_y * P.tiles_z * nchunks;
   for (;;) {
     __syncthreads();  // every thread has read the previous item
@@ -538,8 +539,8 @@ __global__ void __launch_bounds__(TY * kFusedTZ, MOM ? (8 / TY) * mom_ctas<WALLS
     if (item >= units) break;
     const int ntl = P.tiles_y * P.tiles_z;
     const int ch = item / ntl, tile = item - ch * ntl;
-    const int64_t w0 = int64_t(tile) * P.nx + int64_t(ch) * P.run_len;
-    const int64_t w1 = min(w0 + P.run_len, int64_t(tile + 1) * P.nx);
+    const int64_t w0 = int64_t(tile) * P.nx + P.x_begin + int64_t(ch) * P.run_len;
+    const int64_t w1 = min(w0 + P.run_len, int64_t(tile) * P.nx + P.x_end);
     fused_body<T, C, WALLS, TY, MOM>(P, f, fout, nbmask, force_out, w0, w1, sh);
   }
 }

@@ -26,9 +26,10 @@ cudaError_t go_single(const StepBuffers& b, const FusedParams& F, cudaStream_t s
     // runs of 32 planes, halved while there would be fewer than two runs
     // per CTA (each run gathers two extra planes to warm up)
     const int64_t tiles = int64_t(G.tiles_y) * G.tiles_z;
+    const int span = G.x_end - G.x_begin;
     int rl = 32;
-    while (rl > 4 && tiles * ((G.nx + rl - 1) / rl) < 2 * grid) rl /= 2;
-    G.run_len = rl < G.nx ? rl : G.nx;
+    while (rl > 4 && tiles * ((span + rl - 1) / rl) < 2 * grid) rl /= 2;
+    G.run_len = rl < span ? rl : span;
   }
   if (grid > G.work) grid = G.work;
   kern<<<unsigned(grid), TY * kFusedTZ, smem, st>>>(static_cast<const T*>(b.f), static_cast<T*>(b.fout), b.nbmask,

@@ -77,8 +77,8 @@ namespace lbk {
 cudaError_t launch_fused(int kind, int c, const StepBuffers& b, const StepParams& P, cudaStream_t stream,
                          int64_t* launches, const StepEvents* ev, int device);
 // whether launch_fused runs the pair kernel (lb_pairs.cuh) for this lattice
-bool pairs_eligible(const StepParams& P, const StepBuffers& b);
-// the pair step over the planes [x0, x1) only (every tile), for the host
+bool pairs_eligible(int kind, const StepParams& P, const StepBuffers& b);
+// the fused step over the planes [x0, x1) only (every tile), for the host
 // transfers' wavefront; it reads the populations of planes x0 - 2 .. x1 + 1
 cudaError_t launch_fused_range(int kind, int c, const StepBuffers& b, const StepParams& P, int x0, int x1,
                                cudaStream_t stream, int64_t* launches, int device);

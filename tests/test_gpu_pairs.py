@@ -1,15 +1,18 @@
 """The pair kernel (two z-adjacent sites per thread, lb_pairs.cuh): the
-fused single-pass step of the FP32, FP16 and I16 forms for lattices with an
-even z extent and the BDist2 equilibrium.
+fused single-pass step of the I16 form, and of the FP32 and FP16 forms for
+lattices with an even z extent, the BDist2 equilibrium, every tau = 1 and
+no wall (elsewhere FP32 and FP16 run the one-site-per-thread kernel, which
+the same tests cover).
 
 * Against the two-kernel float step (LBGPU_TWO_KERNEL=1, a different
   kernel with the reference's per-site operation order): populations within
   the tolerances of the fused-versus-two-kernel test (2e-6 of the largest
   population in FP32, 2e-3 in FP16), forces within 3e-7 / 3e-4, over tile
   edges in y and z, partial tiles, tiny extents, walls with the wall force,
-  tau != 1 and one component.  I16, which runs on the pair kernel only,
-  against FP32 within the FP16 tolerances.
-* Translation invariance, bit for bit: a lattice shifted periodically by
+  tau != 1 and one component.  I16, which runs on the pair kernel only
+  (walls and tau != 1 included), against FP32 within the FP16 tolerances.
+* Translation invariance, bit for bit (every form, walls included): a
+  lattice shifted periodically by
   (3, 5, 2), by 66 sites along z or by (1, 8, 64) steps to the shifted
   result.  The shifted sites move to other lanes, warps, tiles and ring
   gathers, so this checks that a site's arithmetic does not depend on where

@@ -4,10 +4,9 @@ same bits, step after step, with the output array used as the next input.
 
 The FP64 form, the FP32 form and (with their storage scale pinned) the
 FP16 and I16 forms run as a wavefront over chunks of x-planes (copies in,
-kernels, copies out overlapping; the reduced forms on the pair kernel, for
-D3Q19 lattices with an even z extent and BDist2); lattices too small for
-it, profiled handles, other reduced-form lattices and unpinned FP16/I16 run
-the three calls in turn.  The launch counts tell the two apart: the
+kernels, copies out overlapping; the reduced forms' fused kernel over plane
+ranges); lattices too small for it, profiled handles and unpinned FP16/I16
+run the three calls in turn.  The launch counts tell the two apart: the
 wavefront launches the step kernels once per chunk, the fallback exactly as
 the sequence does.
 """
@@ -109,9 +108,11 @@ def test_step_host_reduced_forms(precision, pin):
              scale=SCALES[precision] if pin else None)
 
 
-def test_step_host_fp32_off_the_pair_kernel_runs_the_sequence():
-    p = spinodal((37, 10, 9))  # odd z extent: the one-site-per-thread kernel
-    _compare(p, lbgpu.FP32, 3, False)
+def test_step_host_fp32_one_site_kernel_wavefront():
+    """An odd z extent runs the one-site-per-thread fused kernel: its plane
+    ranges make the same wavefront."""
+    p = spinodal((37, 10, 9))
+    _compare(p, lbgpu.FP32, 3, True)
 
 
 @pytest.mark.parametrize("precision", [lbgpu.FP32, lbgpu.FP16])
