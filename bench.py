@@ -176,6 +176,64 @@ def time_form_device(p, precision, steps, warmup, device, torch, seed=11):
     return ms / steps, k2_ms / max(k2_n, 1), k1_ms / max(k1_n, 1), launches
 
 
+def storage_scale(fluids, precision, q=19):
+    """The FP16 / I16 offsets' rest density and scale that an upload of
+    these fields derives (the rules of lbgpu_upload), to pin them."""
+    import numpy as np
+    from dlbc_gb300 import lbgpu
+    w = np.array([1 / 3] + [1 / 18] * 6 + [1 / 36] * 12)
+    rho0, scale = [], []
+    for f in fluids:
+        a = f[2:-2, 2:-2, 2:-2]
+        r = float(a.sum(axis=-1).mean())
+        dev = float(np.abs(a / w - r).max())
+        rho0.append(r)
+        scale.append(max(abs(r), 4 * dev) / 1024 if precision == lbgpu.FP16 else 3 * max(abs(r), dev) / 32767)
+    return rho0, scale
+
+
+def e2e_form(p, fluids, hb, hm, precision, n_e2e, device, world, sites, barrier, dist):
+    """End to end through the C ABI: per step, one lbgpu_step_host call on
+    pinned host AoS arrays (inputs in, the same arrays out), and beside it
+    lbgpu_upload + lbgpu_step(1) + lbgpu_download one after another.  FP16
+    and I16 pin their storage scale first (the wavefront needs it)."""
+    from dlbc_gb300 import lbgpu, replicas
+    g = lbgpu.GPULattice(p, precision=precision, device=device)
+    if precision in (lbgpu.FP16, lbgpu.I16):
+        g.set_storage_scale(*storage_scale(fluids, precision))
+    g.upload(hb, hm)
+
+    def timed(one_step):
+        for _ in range(3):
+            one_step()
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(n_e2e):
+            one_step()
+        barrier()
+        dt = replicas.max_over_ranks(time.perf_counter() - t0, dist, device=f"cuda:{device}")
+        return world * sites * n_e2e / dt / 1e6
+
+    def three_calls():
+        g.upload(hb, hm)
+        g.step(1)
+        g.download(hb)
+
+    # fresh inputs each time: the arrays hold the fields of the last step
+    e2e_value = timed(lambda: g.step_host(hb, hm, hb))
+    e2e_seq = timed(three_calls)
+    g.close()
+    for h, f in zip(hb, fluids):
+        h.copy_(__import__("torch").from_numpy(f))
+    return {"value": round(e2e_value, 2), "unit": UNIT,
+            "h2d_bytes_per_step": sum(int(x.numel()) * 8 for x in hb) + int(hm.numel()) * 4,
+            "d2h_bytes_per_step": sum(int(x.numel()) * 8 for x in hb), "steps": n_e2e,
+            "call": "lbgpu_step_host(pinned AoS haloed fluids + mask in, the same arrays out): input copies, "
+                    "kernels and output copies overlap by chunks of 8 x-planes",
+            "three_calls_value": round(e2e_seq, 2),
+            "three_calls": "lbgpu_upload -> lbgpu_step(1) -> lbgpu_download, one after another"}
+
+
 SPINODAL_N = 512
 SPINODAL_WORKLOAD = (f"periodic spinodal {SPINODAL_N}^3 D3Q19 two-component Shan-Chen, rho 0.7 +- 0.02, "
                      f"tau 1, g 3.6, BDist2")
@@ -554,40 +612,11 @@ def main():
     # ---- end to end through the C ABI with pinned host buffers:
     # per step, upload the state (populations + mask), one timestep, download
     e2e = None
+    hb = hm = None
     if args.e2e_steps > 0:
-        g = lbgpu.GPULattice(p, precision=head, device=device)
         hb = [torch.from_numpy(f).pin_memory() for f in fluids]
         hm = torch.from_numpy(mask).pin_memory()
-        g.upload(hb, hm)
-        n_e2e = args.e2e_steps
-
-        def timed(one_step):
-            for _ in range(3):
-                one_step()
-            barrier()
-            t0 = time.perf_counter()
-            for _ in range(n_e2e):
-                one_step()
-            barrier()
-            dt = replicas.max_over_ranks(time.perf_counter() - t0, dist, device=f"cuda:{device}")
-            return world * sites * n_e2e / dt / 1e6
-
-        def three_calls():
-            g.upload(hb, hm)
-            g.step(1)
-            g.download(hb)
-
-        e2e_value = timed(lambda: g.step_host(hb, hm, hb))
-        e2e_seq = timed(three_calls)
-        e2e = {"value": round(e2e_value, 2), "unit": UNIT,
-               "h2d_bytes_per_step": sum(int(x.numel()) * 8 for x in hb) + int(hm.numel()) * 4,
-               "d2h_bytes_per_step": sum(int(x.numel()) * 8 for x in hb), "steps": n_e2e,
-               "call": "lbgpu_step_host(pinned AoS haloed fluids + mask in, the same arrays out): input copies, "
-                       "kernels and output copies overlap by chunks of 8 x-planes",
-               "three_calls_value": round(e2e_seq, 2),
-               "three_calls": "lbgpu_upload -> lbgpu_step(1) -> lbgpu_download, one after another"}
-        g.close()
-        del hb, hm
+        e2e = e2e_form(p, fluids, hb, hm, head, args.e2e_steps, device, world, sites, barrier, dist)
 
     # ---- the other forms of the same workload
     forms = {}
@@ -604,11 +633,15 @@ def main():
                                                 fp64_peak),
                            "step_roofline_frac": round(bytes_per_site(prec) * sites / (f_ms * 1e-3) / 1e9 / peak,
                                                        4)}
+            if hb is not None:
+                forms[name]["e2e"] = e2e_form(p, fluids, hb, hm, prec, args.e2e_steps, device, world, sites,
+                                              barrier, dist)
 
     spinodal = None if args.no_spinodal else run_spinodal(device, torch, peak, peak_kind, fp64_peak, dist=dist,
                                                             n=args.spinodal_n,
                                                             forms=args.spinodal_forms.split(",") if args.spinodal_forms
                                                             else None)
+    del hb, hm
     batched = None if args.no_batched else run_batched(device, torch, dist=dist)
     served = None if args.no_served else run_served(device, n_requests=args.served_requests,
                                                     n_sustained=args.served_requests // 2, dist=dist)
