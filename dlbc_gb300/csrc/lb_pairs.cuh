@@ -450,28 +450,6 @@ __device__ __forceinline__ void pair_body(const FusedParams& P, const T* __restr
         wr_nxt = walled;
       }
     };
-    // L2 prefetch of the row segments the gather of plane xg will read (one
-    // bulk prefetch per population and component, issued by one lane each;
-    // nothing waits on it): issued an iteration ahead, the gather's loads
-    // then find their lines in L2
-    auto prefetch_rows = [&](int xg) {
-      if (!row_on) return;
-      const uint32_t p3[3] = {uint32_t(wrap(xg - 1, P.nx)) * plane_sz, uint32_t(xg) * plane_sz,
-                              uint32_t(wrap(xg + 1, P.nx)) * plane_sz};
-      const uint64_t arr_end = reinterpret_cast<uint64_t>(f + size_t(C) * 19 * size_t(P.n));
-      for (int i = lane; i < 19 * C; i += 32) {
-        const int c = i >= 19 ? 1 : 0, q = i - 19 * c;
-        const int cx = Conn<19>::cx(q), cy = Conn<19>::cy(q);
-        const uint32_t elem = p3[1 - cx] + r3[1 - cy] - uint32_t(zl) + uint32_t(z0) + P.qn[q];
-        const uint64_t a = reinterpret_cast<uint64_t>(fc[c] + elem);
-        const uint64_t start = a & ~uint64_t(15);
-        uint64_t end = (a + uint64_t(tzv) * sizeof(T) + 15) & ~uint64_t(15);
-        if (end > arr_end) end = arr_end & ~uint64_t(15);
-        if (end > start)
-          asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(start), "r"(uint32_t(end - start))
-                       : "memory");
-      }
-    };
     // the ring warps' scalar sites of plane xg (z0 - 1 and z0 + tzv of each
     // row) into psi slot ps
     auto gather_zring = [&](int ps, int xg) {
@@ -506,7 +484,6 @@ __device__ __forceinline__ void pair_body(const FusedParams& P, const T* __restr
     // warm-up: psi of xs - 1; psi and moments of xs; the z-ring of xs + 1.
     // Plane xs - 1 + j lives in psi slot j % 4.
     __syncthreads();
-    prefetch_rows(xs);
     gather_rows(0, wrap(xs - 1, P.nx), -1);
     gather_zring(0, wrap(xs - 1, P.nx));
     gather_rows(1, xs, 0);
@@ -523,7 +500,6 @@ __device__ __forceinline__ void pair_body(const FusedParams& P, const T* __restr
       nb_cur = nb_nxt;
       wr_cur = wr_nxt;
       __syncthreads();  // psi slot sp (plane x - 3) and words buffer 1 - cur are free
-      if (k + 1 < run) prefetch_rows(wrap(x + 2, P.nx));
       gather_rows(sp, wrap(x + 1, P.nx), 1 - cur);
       __syncthreads();
       // the ring warps, idle in the collision: the z-ring of plane x + 2 into
