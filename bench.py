@@ -555,7 +555,7 @@ def main():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--served-requests", type=int, default=200,
-                    help="requests of the oversubscribed served stream (half as many at the sustainable rate)")
+                    help="requests of the oversubscribed served stream (0.3 x as many at the sustainable rate)")
     ap.add_argument("--no-spinodal", action="store_true", help="skip the 512^3 spinodal block")
     ap.add_argument("--spinodal-n", type=int, default=SPINODAL_N, help="edge of the spinodal lattice")
     ap.add_argument("--spinodal-forms", default=None, help="comma-separated forms of the spinodal block (default all)")
@@ -644,7 +644,7 @@ def main():
     del hb, hm
     batched = None if args.no_batched else run_batched(device, torch, dist=dist)
     served = None if args.no_served else run_served(device, n_requests=args.served_requests,
-                                                    n_sustained=args.served_requests // 2, dist=dist)
+                                                    n_sustained=max(10, (3 * args.served_requests) // 10), dist=dist)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
