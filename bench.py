@@ -290,17 +290,30 @@ def fp64_rate(device):
         return None
 
 
+def step_kernel(precision, walls, unit_tau=True, nz_even=True):
+    """The kernel that runs the D3Q19 BDist2 step (the library's dispatch
+    rule, lbk::pairs_eligible): k_collide for FP64; k_pairs for I16, and for
+    FP32/FP16 with every tau = 1, no solid site and an even nz; k_fused
+    otherwise."""
+    from dlbc_gb300 import lbgpu
+    if precision == lbgpu.FP64:
+        return "k_collide"
+    if precision == lbgpu.I16 or (unit_tau and not walls and nz_even):
+        return "k_pairs"
+    return "k_fused"
+
+
 def roofline(precision, sites, kernel_ms, peak, peak_kind, traffic=None, fp64_peak=None, walls=True,
              kernel=None):
-    """HBM roofline of the dominant kernel: k_collide (FP64 two-kernel step)
-    or k_fused (the single-pass FP32 / FP16 step).  k_collide is limited by
-    the FP64 pipe, not by HBM: its FP64 instruction rate against the FP64
-    rate measured on this GPU goes beside the HBM figures."""
+    """HBM roofline of the dominant kernel: k_collide (FP64 two-kernel step),
+    k_fused or k_pairs (the single-pass step).  k_collide is limited by the
+    FP64 pipe, not by HBM: its FP64 instruction rate against the FP64 rate
+    measured on this GPU goes beside the HBM figures."""
     alg = bytes_per_site(precision, walls) * sites
     achieved = alg / (kernel_ms * 1e-3) / 1e9
     from dlbc_gb300 import lbgpu
     if kernel is None:
-        kernel = "k_collide" if precision == lbgpu.FP64 else "k_fused"
+        kernel = step_kernel(precision, walls)
     out = {"bound": "hbm", "kernel": kernel, "achieved": round(achieved, 1), "peak": peak,
            "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
            "traffic": traffic["bytes"] if traffic else None,
@@ -328,7 +341,10 @@ def read_traffic(key):
         with open(path) as fh:
             d = json.load(fh)
         e = d["captures"][key]
-        return {"bytes": e["bytes"], "source": f"ncu one-pass capture at commit {e['commit']} ({e['command']})"}
+        src = f"ncu one-pass capture of {e['kernel']} at commit {e['commit']} ({e['command']})"
+        if e.get("scaled"):
+            src += "; " + e["scaled"]
+        return {"bytes": e["bytes"], "source": src}
     except Exception:
         return None
 
