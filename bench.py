@@ -31,11 +31,11 @@ WORKLOAD = "droplet-channel 256x128x128 D3Q19 two-component Shan-Chen, walls z=0
 LATTICE = (256, 128, 128)
 
 
-def workload_params(n=LATTICE, eq="BDist2"):
+def workload_params(n=LATTICE, eq="BDist2", tau=1.0):
     from dlbc_gb300 import params
     lines = [
         "[lattice]", f"gn = [{n[0]}, {n[1]}, {n[2]}]",
-        "[lb]", "components = 2", 'fieldNames = ["red", "blue"]', "tau = [1.0, 1.0]",
+        "[lb]", "components = 2", 'fieldNames = ["red", "blue"]', f"tau = [{tau!r}, {tau!r}]",
         f"eqdist.eqDistForm = {eq}",
         "force.enableShanChen = true", "force.gcc = [[0.0, 3.6], [3.6, 0.0]]",
         "force.psiForm = Exponential", "force.globalAcc = [1e-6, 0.0, 0.0]",
@@ -49,11 +49,11 @@ def workload_params(n=LATTICE, eq="BDist2"):
     return params.LBParams.from_dict(params.parse_lines(lines), "d3q19")
 
 
-def bytes_per_site(precision: int, walls: bool = True) -> int:
+def bytes_per_site(precision: int, walls: bool = True, q: int = 19) -> int:
     """Algorithmic bytes per site-update: every population read once and
-    written once (2 components x 19), plus the 1-byte mask when walls exist."""
+    written once (2 components x q), plus the 1-byte mask when walls exist."""
     s = {0: 8, 1: 4, 2: 2, 3: 2}[precision]
-    return 2 * 2 * 19 * s + (1 if walls else 0)
+    return 2 * 2 * q * s + (1 if walls else 0)
 
 
 def measured_peaks():
@@ -234,6 +234,8 @@ def e2e_form(p, fluids, hb, hm, precision, n_e2e, device, world, sites, barrier,
             "three_calls": "lbgpu_upload -> lbgpu_step(1) -> lbgpu_download, one after another"}
 
 
+GENERAL_TAU = 0.9
+D2Q9_N = 4096
 SPINODAL_N = 512
 SPINODAL_WORKLOAD = (f"periodic spinodal {SPINODAL_N}^3 D3Q19 two-component Shan-Chen, rho 0.7 +- 0.02, "
                      f"tau 1, g 3.6, BDist2")
@@ -265,6 +267,29 @@ def run_spinodal(device, torch, peak, peak_kind, fp64_peak, dist=None, n=SPINODA
     return out
 
 
+def run_d2q9(device, torch, peak, peak_kind, dist=None, n=D2Q9_N):
+    """The D2Q9 spinodal (n^2 periodic sites, the D3Q19 spinodal's physics:
+    rho 0.7 +- 0.02, tau = 1, g = 3.6, BDist2), initialised on the device, in
+    the FP64 two-kernel form and the fused FP32 / FP16 forms (k_fused2d)."""
+    from dlbc_gb300 import lbgpu, precision_study, replicas
+    p = precision_study.spinodal_params(n, 0.02, d=2)
+    sites = n * n
+    world = dist.get_world_size() if dist is not None else 1
+    out = {"workload": f"periodic spinodal {n}^2 D2Q9 two-component Shan-Chen, rho 0.7 +- 0.02, tau 1, g 3.6, "
+                       f"BDist2", "lattice": [n, n], "init": "device (lbgpu_init_fields, counter-based noise)",
+           "l2": f"inputs larger than L2 (FP16 populations, both buffers: {2 * 2 * 9 * 2 * sites / 1e9:.2f} GB)",
+           "forms": {}}
+    for name, prec, steps in (("fp64", lbgpu.FP64, 10), ("fp32", lbgpu.FP32, 40), ("fp16", lbgpu.FP16, 40)):
+        ms, k2, k1, launches = time_form_device(p, prec, steps, 3, device, torch)
+        ms = replicas.max_over_ranks(ms, dist, device=f"cuda:{device}")
+        out["forms"][name] = {
+            "value": round(world * sites / (ms * 1e-3) / 1e6, 1), "unit": UNIT, "ms_per_step": round(ms, 4),
+            "steps": steps, "warmup": 3, "gpu_launches": launches,
+            "roofline": roofline(prec, sites, k2, peak, peak_kind, None, None, walls=False, q=9),
+            "step_roofline_frac": round(bytes_per_site(prec, False, 9) * sites / (ms * 1e-3) / 1e9 / peak, 4)}
+    return out
+
+
 # FP64 operations per site of k_collide (D3Q19, two components, BDist2,
 # tau = 1, z walls): ncu counted 4.0 M DMUL + 3.9 M DADD warp instructions
 # (no DFMA: the reference's arithmetic without contraction) for the 524,288
@@ -290,36 +315,38 @@ def fp64_rate(device):
         return None
 
 
-def step_kernel(precision, walls, unit_tau=True, nz_even=True):
-    """The kernel that runs the D3Q19 BDist2 step (the library's dispatch
-    rule, lbk::pairs_eligible): k_collide for FP64; k_pairs for I16, and for
-    FP32/FP16 with every tau = 1, no solid site and an even nz; k_fused
-    otherwise."""
+def step_kernel(precision, walls, unit_tau=True, nz_even=True, q=19):
+    """The kernel that runs the BDist2 step (the library's dispatch rule,
+    lbk::pairs_eligible): k_collide for FP64; for D2Q9 k_fused2d; for D3Q19
+    k_pairs for I16, and for FP32/FP16 with every tau = 1, no solid site and
+    an even nz; k_fused otherwise."""
     from dlbc_gb300 import lbgpu
     if precision == lbgpu.FP64:
         return "k_collide"
+    if q == 9:
+        return "k_fused2d"
     if precision == lbgpu.I16 or (unit_tau and not walls and nz_even):
         return "k_pairs"
     return "k_fused"
 
 
 def roofline(precision, sites, kernel_ms, peak, peak_kind, traffic=None, fp64_peak=None, walls=True,
-             kernel=None):
+             kernel=None, q=19):
     """HBM roofline of the dominant kernel: k_collide (FP64 two-kernel step),
     k_fused or k_pairs (the single-pass step).  k_collide is limited by the
     FP64 pipe, not by HBM: its FP64 instruction rate against the FP64 rate
     measured on this GPU goes beside the HBM figures."""
-    alg = bytes_per_site(precision, walls) * sites
+    alg = bytes_per_site(precision, walls, q) * sites
     achieved = alg / (kernel_ms * 1e-3) / 1e9
     from dlbc_gb300 import lbgpu
     if kernel is None:
-        kernel = step_kernel(precision, walls)
+        kernel = step_kernel(precision, walls, q=q)
     out = {"bound": "hbm", "kernel": kernel, "achieved": round(achieved, 1), "peak": peak,
            "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
            "traffic": traffic["bytes"] if traffic else None,
            "traffic_source": traffic["source"] if traffic else None, "algorithmic_bytes": alg,
            "kernel_ms": round(kernel_ms, 5)}
-    if precision == lbgpu.FP64:
+    if precision == lbgpu.FP64 and q == 19:
         g = K_COLLIDE_FP64_OPS_PER_SITE * sites / (kernel_ms * 1e-3) / 1e9
         lim = {"pipe": "fp64", "ops_per_site": K_COLLIDE_FP64_OPS_PER_SITE, "achieved": round(g, 1),
                "unit": "G FP64 thread instructions/s"}
@@ -573,6 +600,8 @@ def main():
     ap.add_argument("--served-requests", type=int, default=200,
                     help="requests of the oversubscribed served stream (0.3 x as many at the sustainable rate)")
     ap.add_argument("--no-spinodal", action="store_true", help="skip the 512^3 spinodal block")
+    ap.add_argument("--no-general-tau", action="store_true", help="skip the tau != 1 block")
+    ap.add_argument("--no-d2q9", action="store_true", help="skip the D2Q9 block")
     ap.add_argument("--spinodal-n", type=int, default=SPINODAL_N, help="edge of the spinodal lattice")
     ap.add_argument("--spinodal-forms", default=None, help="comma-separated forms of the spinodal block (default all)")
     ap.add_argument("--form", default="fp64", choices=["fp64", "fp32", "fp16", "i16"],
@@ -653,6 +682,26 @@ def main():
                 forms[name]["e2e"] = e2e_form(p, fluids, hb, hm, prec, args.e2e_steps, device, world, sites,
                                               barrier, dist)
 
+    # ---- the general collision (tau != 1) of the bandwidth forms, beside
+    # the tau = 1 figures above
+    general_tau = None
+    if not args.no_general_tau:
+        p9 = workload_params(LATTICE, tau=GENERAL_TAU)
+        f9, m9 = init.init_fields(p9)
+        general_tau = {"workload": f"the same channel with tau = {GENERAL_TAU} for both components", "forms": {}}
+        for name in ("fp32", "fp16"):
+            prec = forms_all[name]
+            g_ms, g_k2, _, _ = time_form(p9, f9, m9, prec, args.steps, args.warmup, device, torch)
+            g_ms = replicas.max_over_ranks(g_ms, dist, device=f"cuda:{device}")
+            v = world * sites / (g_ms * 1e-3) / 1e6
+            e = {"value": round(v, 1), "ms_per_step": round(g_ms, 4),
+                 "roofline": roofline(prec, sites, g_k2, peak, peak_kind, None, None, kernel="k_fused")}
+            unit = forms.get(name, {}).get("value") if name != args.form else value
+            if unit:
+                e["vs_tau_1"] = round(v / unit, 4)
+            general_tau["forms"][name] = e
+
+    d2q9 = None if args.no_d2q9 else run_d2q9(device, torch, peak, peak_kind, dist=dist)
     spinodal = None if args.no_spinodal else run_spinodal(device, torch, peak, peak_kind, fp64_peak, dist=dist,
                                                             n=args.spinodal_n,
                                                             forms=args.spinodal_forms.split(",") if args.spinodal_forms
@@ -686,6 +735,8 @@ def main():
             "gpu_launches": launches,
             "clocks": clk.summary(),
             "forms": forms,
+            "general_tau": general_tau,
+            "d2q9": d2q9,
             "spinodal512": spinodal,
             "batched": batched,
             "served": served,

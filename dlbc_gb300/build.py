@@ -5,9 +5,10 @@ Translation units compiled in parallel with one ``-gencode``:
 * ``lb_step_f64.cu``, ``lb_api.cu`` and ``lb_init.cu`` with ``-fmad=false``
   (the FP64 form and the double-precision moments must round every product
   and sum as the reference does);
-* the fused FP32 / FP16-storage step (``lb_fused*.cu``, split by storage
-  type and batching) also with ``-fmad=false``: its fused multiply-adds are
-  explicit, so all its kernel variants give the same bits;
+* the fused FP32 / FP16 / I16-storage steps (``lb_fused*.cu``, split by
+  storage type, connectivity and batching) also with ``-fmad=false``: their
+  fused multiply-adds are explicit, so all variants of a kernel give the
+  same bits;
 * the two-kernel FP32 / FP16 step and the rest (``lb_step_lp.cu``,
   ``lb_batch.cu``, ``lb_noalloc.cu``) with contraction allowed.
 
@@ -42,6 +43,7 @@ UNITS = {
     "lb_fused_f32.cu": ["-fmad=false"],
     "lb_fused_f16.cu": ["-fmad=false"],
     "lb_fused_batch.cu": ["-fmad=false"],
+    "lb_fused2d.cu": ["-fmad=false"],
     "lb_batch.cu": [],
     "lb_noalloc.cu": [],
 }

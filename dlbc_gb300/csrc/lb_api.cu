@@ -420,7 +420,7 @@ int lb_handle_create(const lbgpu_config* cfg, bool lite, double* staging, size_t
   {
     const char* tk = getenv("LBGPU_TWO_KERNEL");
     // the fused kernel indexes a component's populations with 32-bit offsets
-    h->fused = cfg->precision != LBGPU_FP64 && cfg->q == 19 &&
+    h->fused = cfg->precision != LBGPU_FP64 && (cfg->q == 19 || (cfg->q == 9 && cfg->precision != LBGPU_I16)) &&
                (cfg->precision == LBGPU_I16 || !(tk && tk[0] == '1' && !lite)) && 19 * h->n < (int64_t(1) << 32);
   }
   if (cfg->precision == LBGPU_I16 && !h->fused) {
@@ -428,7 +428,7 @@ int lb_handle_create(const lbgpu_config* cfg, bool lite, double* staging, size_t
     delete h;
     return LBGPU_E_INVALID;
   }
-  if (lite && !h->fused) {
+  if (lite && (!h->fused || cfg->q != 19)) {
     *err = "batch members must be FP32/FP16 D3Q19 lattices below 2^32/19 sites";
     delete h;
     return LBGPU_E_INVALID;
@@ -526,7 +526,8 @@ int64_t lb_member_bytes(const lbgpu_config* cfg) {
 
 // Neighbour mask of every site: bit 0 the site's own solid flag, bit q the
 // solid flag of x + c_q (periodic), for the fused step's bounce-back, stencil
-// and wall-force tests.
+// and wall-force tests (D3Q19, or D2Q9 with nz = 1).
+template <int Q>
 __global__ void k_nbmask(const uint8_t* __restrict__ mask, uint32_t* __restrict__ nbm, Geo g) {
   const int64_t s = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (s >= g.n) return;
@@ -536,10 +537,10 @@ __global__ void k_nbmask(const uint8_t* __restrict__ mask, uint32_t* __restrict_
   const int y = int(r / g.nz), z = int(r - int64_t(y) * g.nz);
   uint32_t bits = mask[s] ? 1u : 0u;
 #pragma unroll
-  for (int q = 1; q < 19; ++q) {
-    const int xn = (x + lbk::Conn<19>::cx(q) + g.nx) % g.nx;
-    const int yn = (y + lbk::Conn<19>::cy(q) + g.ny) % g.ny;
-    const int zn = (z + lbk::Conn<19>::cz(q) + g.nz) % g.nz;
+  for (int q = 1; q < Q; ++q) {
+    const int xn = (x + lbk::Conn<Q>::cx(q) + g.nx) % g.nx;
+    const int yn = (y + lbk::Conn<Q>::cy(q) + g.ny) % g.ny;
+    const int zn = (z + lbk::Conn<Q>::cz(q) + g.nz) % g.nz;
     if (mask[(int64_t(xn) * g.ny + yn) * g.nz + zn]) bits |= 1u << q;
   }
   nbm[s] = bits;
@@ -591,7 +592,7 @@ int lb_sync_solids(lbgpu_handle* h, int cur, cudaStream_t st) {
 
 int lb_update_nbmask(lbgpu_handle* h) {
   h->solids_synced = false;  // new populations or a new mask
-  const bool want = h->mask && (h->fused || h->lite) && h->Q == 19;
+  const bool want = h->mask && (h->fused || h->lite) && (h->Q == 19 || h->Q == 9);
   const int tiles_y = (h->ny + 7) / 8, tiles_z = (h->nz + 31) / 32;
   const int64_t nflags = int64_t(h->nx) * tiles_y * tiles_z;
   const int segs = (h->nz + lbk::kPairTZ - 1) / lbk::kPairTZ;
@@ -623,10 +624,14 @@ int lb_update_nbmask(lbgpu_handle* h) {
     }
     h->device_bytes += 4 * h->n;
   }
-  k_nbmask<<<unsigned(ceil_div(h->n, 256)), 256, 0, h->stream>>>(h->mask, h->nbmask, geo_of(h));
+  if (h->Q == 9)
+    k_nbmask<9><<<unsigned(ceil_div(h->n, 256)), 256, 0, h->stream>>>(h->mask, h->nbmask, geo_of(h));
+  else
+    k_nbmask<19><<<unsigned(ceil_div(h->n, 256)), 256, 0, h->stream>>>(h->mask, h->nbmask, geo_of(h));
   h->launches++;
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return h->cuda_fail(e, "neighbour mask kernel");
+  if (h->Q == 9) return LBGPU_OK;  // the D2Q9 kernel reads the neighbour masks only
   if (!h->row_walls) {
     e = cudaMalloc(&h->row_walls, size_t(nrow));
     if (e != cudaSuccess) {
@@ -961,7 +966,7 @@ int lbgpu_step(lbgpu_handle* h, int32_t nsteps) {
       e = lbk::launch_step_f64(h->Q, h->C, b, P, h->stream, &h->launches, evp);
     else if (h->fused) {
       if (int rc = lb_sync_solids(h, h->cur, h->stream)) return rc;
-      e = lbk::launch_fused(storage_kind(h->cfg.precision), h->C, b, P, h->stream, &h->launches, evp,
+      e = lbk::launch_fused(storage_kind(h->cfg.precision), h->Q, h->C, b, P, h->stream, &h->launches, evp,
                             h->cfg.device);
     } else if (h->cfg.precision == LBGPU_FP32)
       e = lbk::launch_step_f32(h->Q, h->C, b, P, h->stream, &h->launches, evp);
@@ -1109,7 +1114,7 @@ int step_host_wave(lbgpu_handle* h, const double* const* in, double* const* out,
       // the fused forms: one pair-kernel launch per plane range (it reads
       // planes x0 - 2 .. x1 + 1, those the FP64 collide part needs)
       if (which != lbk::kPartCollide) return cudaSuccess;
-      return lbk::launch_fused_range(storage_kind(h->cfg.precision), h->C, b, P, x0, x1, h->stream, &h->launches,
+      return lbk::launch_fused_range(storage_kind(h->cfg.precision), h->Q, h->C, b, P, x0, x1, h->stream, &h->launches,
                                      h->cfg.device);
     }
     P.s_begin = int64_t(x0) * plane_sites;

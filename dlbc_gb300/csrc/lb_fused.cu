@@ -8,7 +8,7 @@
 
 namespace lbk {
 
-FusedParams make_fused_params(const StepParams& P, int ty) {
+FusedParams make_fused_params(const StepParams& P, int ty, int q) {
   FusedParams F{};
   F.nx = P.nx;
   F.ny = P.ny;
@@ -39,13 +39,14 @@ FusedParams make_fused_params(const StepParams& P, int ty) {
     F.inv_scale[c] = P.inv_scale[c];
   }
   for (int i = 0; i < 3; ++i) F.acc[i] = float(P.acc[i]);
-  for (int q = 0; q < 19; ++q) {
-    F.qn[q] = uint32_t(int64_t(q) * P.n);
+  for (int i = 0; i < 19; ++i) F.qn[i] = i < q ? uint32_t(int64_t(i) * P.n) : 0u;
+  for (int i = 0; i < q; ++i) {
     for (int c = 0; c < 2; ++c) {
-      // one value per weight class (q = 0, 1..6, 7..18)
-      const int k = Conn<19>::wclass(q);
-      F.wrho[c][k] = weight<19, float>(q) * P.rho0[c];
-      F.wscale[c][k] = weight<19, float>(q) * P.scale[c];
+      // one value per weight class (rest, axis, diagonal)
+      const int k = q == 9 ? Conn<9>::wclass(i) : Conn<19>::wclass(i);
+      const float w = q == 9 ? weight<9, float>(i) : weight<19, float>(i);
+      F.wrho[c][k] = w * P.rho0[c];
+      F.wscale[c][k] = w * P.scale[c];
       F.inv_wscale[c][k] = 1.0f / F.wscale[c][k];
       F.hoff[c][k] = -F.wrho[c][k] * F.inv_wscale[c][k];
     }
@@ -69,11 +70,11 @@ bool pairs_eligible(int kind, const StepParams& P, const StepBuffers& b) {
 // wavefront; the pair kernel or the one-site-per-thread kernel, whichever
 // launch_fused would run): reads the populations of planes x0 - 2 .. x1 + 1
 // (periodic)
-cudaError_t launch_fused_range(int kind, int c, const StepBuffers& b, const StepParams& P, int x0, int x1,
+cudaError_t launch_fused_range(int kind, int q, int c, const StepBuffers& b, const StepParams& P, int x0, int x1,
                                cudaStream_t st, int64_t* launches, int device) {
   if (x1 <= x0) return cudaSuccess;
   if (!b.work_counter) return cudaErrorInvalidValue;
-  FusedParams G = make_fused_params(P, 8);
+  FusedParams G = make_fused_params(P, 8, q);
   G.tile_walls = b.tile_walls;
   G.work_counter = b.work_counter;
   G.x_begin = x0;
@@ -82,6 +83,7 @@ cudaError_t launch_fused_range(int kind, int c, const StepBuffers& b, const Step
   const bool w = b.mask != nullptr;
   if (w && !b.nbmask) return cudaErrorInvalidValue;
   *launches += 1;
+  if (q == 9) return launch_fused2d(kind, c, w, c == 2 && P.unit_tau && P.eq_form == 2, b, G, st, device);
   if (pairs_eligible(kind, P, b)) {
     G.tiles_y = (P.ny + 7) / 8;
     G.tiles_z = (P.nz + kPairTZ - 1) / kPairTZ;
@@ -97,9 +99,9 @@ cudaError_t launch_fused_range(int kind, int c, const StepBuffers& b, const Step
                            : launch_fused_single_f32(c, w, mom, b, G, st, device);
 }
 
-cudaError_t launch_fused(int kind, int c, const StepBuffers& b, const StepParams& P, cudaStream_t st,
+cudaError_t launch_fused(int kind, int q, int c, const StepBuffers& b, const StepParams& P, cudaStream_t st,
                          int64_t* launches, const StepEvents* ev, int device) {
-  FusedParams F = make_fused_params(P, 8);
+  FusedParams F = make_fused_params(P, 8, q);
   F.tile_walls = b.tile_walls;
   if (b.work_counter) {
     // dynamic runs (length chosen at launch)
@@ -114,7 +116,9 @@ cudaError_t launch_fused(int kind, int c, const StepBuffers& b, const StepParams
     cudaEventRecord(ev->ev[1], st);
   }
   cudaError_t e;
-  if (pairs_eligible(kind, P, b)) {
+  if (q == 9) {
+    e = launch_fused2d(kind, c, w, c == 2 && P.unit_tau && P.eq_form == 2, b, F, st, device);
+  } else if (pairs_eligible(kind, P, b)) {
     // two z-adjacent sites per thread (lb_pairs.cuh): 8 x 64 tiles
     FusedParams G = F;
     G.tiles_y = (P.ny + 7) / 8;

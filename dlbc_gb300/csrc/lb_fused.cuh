@@ -83,10 +83,12 @@ struct FusedParams {
   int32_t x_begin, x_end;
 };
 
-template <typename T>
+// Storage of connectivity Q (D3Q19 or D2Q9): the half form's constants
+// depend on q only through its weight class.
+template <typename T, int Q = 19>
 struct FStore;
-template <>
-struct FStore<float> {
+template <int Q>
+struct FStore<float, Q> {
   __device__ static __forceinline__ float load(const float* p, int, int, const FusedParams&) { return __ldg(p); }
   // population q or, bounced back, population b (q, b compile-time constants)
   __device__ static __forceinline__ float load2(const float* p, int, int, int, bool, const FusedParams&) {
@@ -94,18 +96,18 @@ struct FStore<float> {
   }
   __device__ static __forceinline__ void store(float* p, float v, int, int, const FusedParams&) { *p = v; }
 };
-template <>
-struct FStore<__half> {
+template <int Q>
+struct FStore<__half, Q> {
   __device__ static __forceinline__ float load(const __half* p, int c, int q, const FusedParams& P) {
-    return fmaf(P.wscale[c][Conn<19>::wclass(q)], __half2float(__ldg(p)), P.wrho[c][Conn<19>::wclass(q)]);
+    return fmaf(P.wscale[c][Conn<Q>::wclass(q)], __half2float(__ldg(p)), P.wrho[c][Conn<Q>::wclass(q)]);
   }
   // opposite populations have equal weights (w_b = w_q), so either decodes
   // with q's constants
   __device__ static __forceinline__ float load2(const __half* p, int c, int q, int, bool, const FusedParams& P) {
-    return fmaf(P.wscale[c][Conn<19>::wclass(q)], __half2float(__ldg(p)), P.wrho[c][Conn<19>::wclass(q)]);
+    return fmaf(P.wscale[c][Conn<Q>::wclass(q)], __half2float(__ldg(p)), P.wrho[c][Conn<Q>::wclass(q)]);
   }
   __device__ static __forceinline__ void store(__half* p, float v, int c, int q, const FusedParams& P) {
-    *p = __float2half_rn(fmaf(v, P.inv_wscale[c][Conn<19>::wclass(q)], P.hoff[c][Conn<19>::wclass(q)]));
+    *p = __float2half_rn(fmaf(v, P.inv_wscale[c][Conn<Q>::wclass(q)], P.hoff[c][Conn<Q>::wclass(q)]));
   }
 };
 

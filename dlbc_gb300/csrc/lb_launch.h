@@ -71,16 +71,17 @@ cudaError_t launch_phase_f16(int phase, int q, int c, const StepBuffers& b, cons
 
 namespace lbk {
 
-// Fused single-pass D3Q19 step (lb_fused.cuh) for the float-arithmetic
-// forms; `kind` is the storage (kStoreF32 / kStoreF16 / kStoreI16; I16 runs
-// on the pair kernel only).
-cudaError_t launch_fused(int kind, int c, const StepBuffers& b, const StepParams& P, cudaStream_t stream,
+// Fused single-pass step for the float-arithmetic forms: D3Q19
+// (lb_fused.cuh, lb_pairs.cuh; q = 19) or D2Q9 (lb_fused2d.cuh; q = 9);
+// `kind` is the storage (kStoreF32 / kStoreF16 / kStoreI16; I16 runs on the
+// D3Q19 pair kernel only).
+cudaError_t launch_fused(int kind, int q, int c, const StepBuffers& b, const StepParams& P, cudaStream_t stream,
                          int64_t* launches, const StepEvents* ev, int device);
 // whether launch_fused runs the pair kernel (lb_pairs.cuh) for this lattice
 bool pairs_eligible(int kind, const StepParams& P, const StepBuffers& b);
 // the fused step over the planes [x0, x1) only (every tile), for the host
 // transfers' wavefront; it reads the populations of planes x0 - 2 .. x1 + 1
-cudaError_t launch_fused_range(int kind, int c, const StepBuffers& b, const StepParams& P, int x0, int x1,
+cudaError_t launch_fused_range(int kind, int q, int c, const StepBuffers& b, const StepParams& P, int x0, int x1,
                                cudaStream_t stream, int64_t* launches, int device);
 
 }  // namespace lbk
@@ -91,8 +92,9 @@ struct FusedParams;
 struct FusedSim;
 struct PairSim;
 
-// float parameters of the fused kernel for tiles of height ty (4 or 8)
-FusedParams make_fused_params(const StepParams& P, int ty);
+// float parameters of the fused kernel for tiles of height ty (4 or 8) and
+// connectivity q (19, or 9 for the D2Q9 kernel)
+FusedParams make_fused_params(const StepParams& P, int ty, int q = 19);
 
 // One timestep of every simulation in `sims` (device array, two-component,
 // D3Q19) in one persistent launch.  ctas_per_sm <= 0: as many as fit.

@@ -420,9 +420,6 @@ __device__ __forceinline__ void pair_body(const FusedParams& P, const T* __restr
           }
           if (!MOM && keep >= 0 && !ring_warp) sh.pops[keep][c][q][warp][lane] = word;
           v[q] = IO::val(word);
-#ifdef LB_PAIRS_SPLIT_LOADS
-          if (q == 9) __syncwarp();
-#endif
         }
         m[c] = pair_moments<OFF>(v, s36[c], P.rho0[c]);
         ps2[c] = make_float2(pair_psi(m[c].rho.x, P.psi_form), pair_psi(m[c].rho.y, P.psi_form));

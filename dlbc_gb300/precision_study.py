@@ -24,17 +24,18 @@ import numpy as np
 from . import lbgpu, params
 
 
-def spinodal_params(n: int, perturb: float) -> params.LBParams:
+def spinodal_params(n: int, perturb: float, d: int = 3) -> params.LBParams:
+    """The spinodal lattice: n^3 D3Q19, or n^2 D2Q9 with d = 2."""
     lines = [
-        "[lattice]", f"gn = [{n}, {n}, {n}]",
+        "[lattice]", f"gn = [{', '.join([str(n)] * d)}]",
         "[lb]", "components = 2", 'fieldNames = ["red", "blue"]', "tau = [1.0, 1.0]",
         "eqdist.eqDistForm = BDist2", "force.enableShanChen = true",
         "force.gcc = [[0.0, 3.6], [3.6, 0.0]]", "force.psiForm = Exponential",
-        "force.globalAcc = [0.0, 0.0, 0.0]",
+        f"force.globalAcc = [{', '.join(['0.0'] * d)}]",
         "init.fluidInit = [EqDistPerturb, EqDistPerturb]", "init.fluidDensities = [[0.7], [0.7]]",
         f"init.fluidPerturb = [{perturb}, {perturb}]",
     ]
-    return params.LBParams.from_dict(params.parse_lines(lines), "d3q19")
+    return params.LBParams.from_dict(params.parse_lines(lines), "d3q19" if d == 3 else "d2q9")
 
 
 def run_form(p, precision, steps, checkpoints, seed, device=0, rho0=(0.0, 0.0)):

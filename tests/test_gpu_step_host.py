@@ -108,6 +108,14 @@ def test_step_host_reduced_forms(precision, pin):
              scale=SCALES[precision] if pin else None)
 
 
+@pytest.mark.parametrize("precision", [lbgpu.FP32, lbgpu.FP16])
+def test_step_host_d2q9_fused_wavefront(precision):
+    """The D2Q9 fused kernel over row ranges (the wavefront) computes the bits
+    of its whole-lattice launch: walls, the wall force and a partial tile."""
+    p = droplet_channel((48, 300), radius=8.0, acc=1e-3, gwc=(0.3, -0.2), d=2)
+    _compare(p, precision, 3, True, record_force=True, scale=SCALES.get(precision))
+
+
 def test_step_host_fp32_one_site_kernel_wavefront():
     """An odd z extent runs the one-site-per-thread fused kernel: its plane
     ranges make the same wavefront."""

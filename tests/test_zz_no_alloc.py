@@ -7,7 +7,7 @@ It must give the same populations as the regular entry points
 in FP64, the tolerance every FP64 parity test here uses; in FP32 within the
 tolerance the fused-versus-two-kernel FP32 test uses (2e-6 of the largest
 population), because lbgpu_step runs the fused single-pass kernel for FP32
-D3Q19 and this entry point the two-kernel float step.  The caller owns the
+D3Q19 and D2Q9 and this entry point the two-kernel float step.  The caller owns the
 population buffers (torch CUDA tensors here); the scratch is the library's
 static device array, shared by all calls.  (Its size check, which needs no
 GPU, is in test_cabi.py.)
