@@ -267,7 +267,7 @@ def run_spinodal(device, torch, peak, peak_kind, fp64_peak, dist=None, n=SPINODA
     return out
 
 
-def run_d2q9(device, torch, peak, peak_kind, dist=None, n=D2Q9_N):
+def run_d2q9(device, torch, peak, peak_kind, dist=None, n=D2Q9_N, forms=None):
     """The D2Q9 spinodal (n^2 periodic sites, the D3Q19 spinodal's physics:
     rho 0.7 +- 0.02, tau = 1, g = 3.6, BDist2), initialised on the device, in
     the FP64 two-kernel form and the fused FP32 / FP16 forms (k_fused2d)."""
@@ -280,12 +280,15 @@ def run_d2q9(device, torch, peak, peak_kind, dist=None, n=D2Q9_N):
            "l2": f"inputs larger than L2 (FP16 populations, both buffers: {2 * 2 * 9 * 2 * sites / 1e9:.2f} GB)",
            "forms": {}}
     for name, prec, steps in (("fp64", lbgpu.FP64, 10), ("fp32", lbgpu.FP32, 40), ("fp16", lbgpu.FP16, 40)):
+        if forms and name not in forms:
+            continue
         ms, k2, k1, launches = time_form_device(p, prec, steps, 3, device, torch)
         ms = replicas.max_over_ranks(ms, dist, device=f"cuda:{device}")
         out["forms"][name] = {
             "value": round(world * sites / (ms * 1e-3) / 1e6, 1), "unit": UNIT, "ms_per_step": round(ms, 4),
             "steps": steps, "warmup": 3, "gpu_launches": launches,
-            "roofline": roofline(prec, sites, k2, peak, peak_kind, None, None, walls=False, q=9),
+            "roofline": roofline(prec, sites, k2, peak, peak_kind, read_traffic(f"d2q9_{n}/{name}"), None,
+                                 walls=False, q=9),
             "step_roofline_frac": round(bytes_per_site(prec, False, 9) * sites / (ms * 1e-3) / 1e9 / peak, 4)}
     return out
 
@@ -602,6 +605,8 @@ def main():
     ap.add_argument("--no-spinodal", action="store_true", help="skip the 512^3 spinodal block")
     ap.add_argument("--no-general-tau", action="store_true", help="skip the tau != 1 block")
     ap.add_argument("--no-d2q9", action="store_true", help="skip the D2Q9 block")
+    ap.add_argument("--d2q9-n", type=int, default=D2Q9_N, help="edge of the D2Q9 lattice")
+    ap.add_argument("--d2q9-forms", default=None, help="comma-separated forms of the D2Q9 block (default all)")
     ap.add_argument("--spinodal-n", type=int, default=SPINODAL_N, help="edge of the spinodal lattice")
     ap.add_argument("--spinodal-forms", default=None, help="comma-separated forms of the spinodal block (default all)")
     ap.add_argument("--form", default="fp64", choices=["fp64", "fp32", "fp16", "i16"],
@@ -701,7 +706,8 @@ def main():
                 e["vs_tau_1"] = round(v / unit, 4)
             general_tau["forms"][name] = e
 
-    d2q9 = None if args.no_d2q9 else run_d2q9(device, torch, peak, peak_kind, dist=dist)
+    d2q9 = None if args.no_d2q9 else run_d2q9(device, torch, peak, peak_kind, dist=dist, n=args.d2q9_n,
+                                              forms=args.d2q9_forms.split(",") if args.d2q9_forms else None)
     spinodal = None if args.no_spinodal else run_spinodal(device, torch, peak, peak_kind, fp64_peak, dist=dist,
                                                             n=args.spinodal_n,
                                                             forms=args.spinodal_forms.split(",") if args.spinodal_forms
