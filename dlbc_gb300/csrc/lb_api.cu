@@ -526,7 +526,7 @@ int64_t lb_member_bytes(const lbgpu_config* cfg) {
 
 // Neighbour mask of every site: bit 0 the site's own solid flag, bit q the
 // solid flag of x + c_q (periodic), for the fused step's bounce-back, stencil
-// and wall-force tests (D3Q19, or D2Q9 with nz = 1).
+// and wall-force tests (any connectivity; nz = 1 in 2D, ny = nz = 1 in 1D).
 template <int Q>
 __global__ void k_nbmask(const uint8_t* __restrict__ mask, uint32_t* __restrict__ nbm, Geo g) {
   const int64_t s = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -592,7 +592,9 @@ int lb_sync_solids(lbgpu_handle* h, int cur, cudaStream_t st) {
 
 int lb_update_nbmask(lbgpu_handle* h) {
   h->solids_synced = false;  // new populations or a new mask
-  const bool want = h->mask && (h->fused || h->lite) && (h->Q == 19 || h->Q == 9);
+  // every walled lattice: the two-kernel step reads them too (one 32-bit
+  // load per site instead of one mask byte per neighbour)
+  const bool want = h->mask != nullptr;
   const int tiles_y = (h->ny + 7) / 8, tiles_z = (h->nz + 31) / 32;
   const int64_t nflags = int64_t(h->nx) * tiles_y * tiles_z;
   const int segs = (h->nz + lbk::kPairTZ - 1) / lbk::kPairTZ;
@@ -624,14 +626,20 @@ int lb_update_nbmask(lbgpu_handle* h) {
     }
     h->device_bytes += 4 * h->n;
   }
-  if (h->Q == 9)
-    k_nbmask<9><<<unsigned(ceil_div(h->n, 256)), 256, 0, h->stream>>>(h->mask, h->nbmask, geo_of(h));
+  const unsigned nb_blocks = unsigned(ceil_div(h->n, 256));
+  if (h->Q == 19)
+    k_nbmask<19><<<nb_blocks, 256, 0, h->stream>>>(h->mask, h->nbmask, geo_of(h));
+  else if (h->Q == 9)
+    k_nbmask<9><<<nb_blocks, 256, 0, h->stream>>>(h->mask, h->nbmask, geo_of(h));
+  else if (h->Q == 5)
+    k_nbmask<5><<<nb_blocks, 256, 0, h->stream>>>(h->mask, h->nbmask, geo_of(h));
   else
-    k_nbmask<19><<<unsigned(ceil_div(h->n, 256)), 256, 0, h->stream>>>(h->mask, h->nbmask, geo_of(h));
+    k_nbmask<3><<<nb_blocks, 256, 0, h->stream>>>(h->mask, h->nbmask, geo_of(h));
   h->launches++;
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return h->cuda_fail(e, "neighbour mask kernel");
-  if (h->Q == 9) return LBGPU_OK;  // the D2Q9 kernel reads the neighbour masks only
+  // the row and tile wall flags: the D3Q19 fused kernels only
+  if (h->Q != 19 || !(h->fused || h->lite)) return LBGPU_OK;
   if (!h->row_walls) {
     e = cudaMalloc(&h->row_walls, size_t(nrow));
     if (e != cudaSuccess) {

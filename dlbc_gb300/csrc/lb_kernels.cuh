@@ -126,16 +126,35 @@ __device__ __forceinline__ R force_sub(R F, R prefactor, int c) {
   return F;
 }
 
+// Solid tests around site s: from the 8-bit mask, one load per neighbour,
+// or (NBM) from the site's 32-bit neighbour mask (bit 0: the site is solid;
+// bit q: the site x + c_q is solid, periodic images included), one load per
+// site.  The two give the same answers.
+template <bool NBM>
+struct Solids {
+  const uint8_t* mask;
+  uint32_t bits;
+  __device__ __forceinline__ Solids(const uint8_t* m, const uint32_t* nbm, int64_t s)
+      : mask(m), bits(NBM ? __ldg(nbm + s) : 0u) {}
+  // the site itself
+  __device__ __forceinline__ bool self(int64_t s) const { return NBM ? (bits & 1u) != 0 : mask[s] != 0; }
+  // the site x + c_q, whose index is nb
+  __device__ __forceinline__ bool at(int q, int64_t nb) const {
+    return NBM ? ((bits >> q) & 1u) != 0 : __ldg(mask + nb) != 0;
+  }
+};
+
 // Pull-streamed populations of one component at a fluid site.
-template <typename T, typename R, int Q, bool WALLS>
-__device__ __forceinline__ void gather(const T* __restrict__ f, const uint8_t* __restrict__ mask, const Site& S,
-                                       int64_t s, int c, const StepParams& P, R* pop) {
+template <typename T, typename R, int Q, bool WALLS, bool NBM>
+__device__ __forceinline__ void gather(const T* __restrict__ f, const Solids<NBM>& W, const Site& S, int64_t s, int c,
+                                       const StepParams& P, R* pop) {
   const T* fc = f + int64_t(c) * Q * P.n;
   pop[0] = Store<T, R, Q>::load(fc + s, c, 0, P);
 #pragma unroll
   for (int q = 1; q < Q; ++q) {
     const int64_t nb = nb_index<Q>(S, q, -1, P);
-    if (WALLS && __ldg(mask + nb)) {
+    // the source x - c_q is x + c_b
+    if (WALLS && W.at(Conn<Q>::bounce(q), nb)) {
       const int b = Conn<Q>::bounce(q);
       pop[q] = Store<T, R, Q>::load(fc + int64_t(b) * P.n + s, c, b, P);
     } else {
@@ -154,20 +173,23 @@ __device__ __forceinline__ void load_local(const T* __restrict__ f, int64_t s, i
 // ---------------------------------------------------------------------------
 // kernel 1: densities and psi after streaming, at every site
 // ---------------------------------------------------------------------------
-template <typename T, typename R, int Q, int C, bool WALLS, bool STREAM = true>
+// (NBM: solid tests from the neighbour masks nbmask, else from mask)
+template <typename T, typename R, int Q, int C, bool WALLS, bool STREAM = true, bool NBM = false>
 __global__ void __launch_bounds__(128) k_density_psi(const T* __restrict__ f, const uint8_t* __restrict__ mask,
-                                                     R* __restrict__ rho, R* __restrict__ psi, StepParams P) {
+                                                     const uint32_t* __restrict__ nbmask, R* __restrict__ rho,
+                                                     R* __restrict__ psi, StepParams P) {
   const int64_t s = P.s_begin + int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (s >= (P.s_end ? P.s_end : P.n)) return;
   const Site S = make_site(s, P);
-  const bool solid = WALLS && mask[s];
+  const Solids<WALLS && NBM> W(mask, nbmask, s);
+  const bool solid = WALLS && W.self(s);
 #pragma unroll
   for (int c = 0; c < C; ++c) {
     R pop[Q];
     if (solid || !STREAM)
       load_local<T, R, Q>(f, s, c, P, pop);
     else
-      gather<T, R, Q, WALLS>(f, mask, S, s, c, P, pop);
+      gather<T, R, Q, WALLS>(f, W, S, s, c, P, pop);
     const R den = density<Q, R>(pop);
     rho[int64_t(c) * P.n + s] = den;
     // psi of a solid site is never read (force.d:273 uses the site's own psi)
@@ -180,15 +202,17 @@ __global__ void __launch_bounds__(128) k_density_psi(const T* __restrict__ f, co
 // ---------------------------------------------------------------------------
 // (at most 168 registers, three 128-thread CTAs per SM: the FP64 form is
 // latency bound at two)
-template <typename T, typename R, int Q, int C, bool WALLS, bool STREAM = true>
+template <typename T, typename R, int Q, int C, bool WALLS, bool STREAM = true, bool NBM = false>
 __global__ void __launch_bounds__(128, 3) k_collide(const T* __restrict__ f, T* __restrict__ fout,
-                                                 const uint8_t* __restrict__ mask, const R* __restrict__ rho,
+                                                 const uint8_t* __restrict__ mask,
+                                                 const uint32_t* __restrict__ nbmask, const R* __restrict__ rho,
                                                  const R* __restrict__ psi, double* __restrict__ force_out,
                                                  StepParams P) {
   constexpr int D = Conn<Q>::D;
   const int64_t s = P.s_begin + int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (s >= (P.s_end ? P.s_end : P.n)) return;
-  const bool solid = WALLS && mask[s];
+  const Solids<WALLS && NBM> W(mask, nbmask, s);
+  const bool solid = WALLS && W.self(s);
 
   R den[C];
 #pragma unroll
@@ -236,7 +260,7 @@ __global__ void __launch_bounds__(128, 3) k_collide(const T* __restrict__ f, T* 
 #pragma unroll
         for (int q = 1; q < Q; ++q) {
           const int64_t nb = nb_index<Q>(S, q, +1, P);
-          const R psiden2 = (WALLS && __ldg(mask + nb)) ? ps[f2] : __ldg(p2 + nb);
+          const R psiden2 = (WALLS && W.at(q, nb)) ? ps[f2] : __ldg(p2 + nb);
           const R prefactor = (Conn<Q>::wclass(q) == 1 ? wpsi1 : wpsi2) * psiden2 * cc;
 #pragma unroll
           for (int vd = 0; vd < D; ++vd) F[f1][vd] = force_sub(F[f1][vd], prefactor, cvel<Q>(q, vd));
@@ -249,7 +273,7 @@ __global__ void __launch_bounds__(128, 3) k_collide(const T* __restrict__ f, T* 
 #pragma unroll
           for (int q = 1; q < Q; ++q) {
             const int64_t nb = nb_index<Q>(S, q, +1, P);
-            if (__ldg(mask + nb)) {
+            if (W.at(q, nb)) {
               const R prefactor = (Conn<Q>::wclass(q) == 1 ? wpsi1 : wpsi2) * __ldg(r1 + nb) * wc;
 #pragma unroll
               for (int vd = 0; vd < D; ++vd) F[f1][vd] = force_sub(F[f1][vd], prefactor, cvel<Q>(q, vd));
@@ -282,7 +306,7 @@ __global__ void __launch_bounds__(128, 3) k_collide(const T* __restrict__ f, T* 
 #pragma unroll
   for (int c = 0; c < C; ++c) {
     if (STREAM)
-      gather<T, R, Q, WALLS>(f, mask, S, s, c, P, pop[c]);
+      gather<T, R, Q, WALLS>(f, W, S, s, c, P, pop[c]);
     else
       load_local<T, R, Q>(f, s, c, P, pop[c]);
   }

@@ -7,17 +7,18 @@ namespace lbk {
 
 constexpr int kStepThreads = 128;
 
-template <typename T, typename R, int Q, int C, bool W>
+// (NBM: the solid tests read the neighbour masks b.nbmask)
+template <typename T, typename R, int Q, int C, bool W, bool NBM = false>
 cudaError_t launch_step_t(const StepBuffers& b, const StepParams& P, cudaStream_t st, int64_t* launches,
                           const StepEvents* ev) {
   const unsigned blocks = unsigned((P.n + kStepThreads - 1) / kStepThreads);
   if (ev) cudaEventRecord(ev->ev[0], st);
-  k_density_psi<T, R, Q, C, W><<<blocks, kStepThreads, 0, st>>>(static_cast<const T*>(b.f), b.mask,
-                                                                 static_cast<R*>(b.rho), static_cast<R*>(b.psi), P);
+  k_density_psi<T, R, Q, C, W, true, NBM><<<blocks, kStepThreads, 0, st>>>(
+      static_cast<const T*>(b.f), b.mask, b.nbmask, static_cast<R*>(b.rho), static_cast<R*>(b.psi), P);
   if (ev) cudaEventRecord(ev->ev[1], st);
-  k_collide<T, R, Q, C, W><<<blocks, kStepThreads, 0, st>>>(static_cast<const T*>(b.f), static_cast<T*>(b.fout),
-                                                             b.mask, static_cast<const R*>(b.rho),
-                                                             static_cast<const R*>(b.psi), b.force, P);
+  k_collide<T, R, Q, C, W, true, NBM><<<blocks, kStepThreads, 0, st>>>(
+      static_cast<const T*>(b.f), static_cast<T*>(b.fout), b.mask, b.nbmask, static_cast<const R*>(b.rho),
+      static_cast<const R*>(b.psi), b.force, P);
   if (ev) cudaEventRecord(ev->ev[2], st);
   *launches += 2;
   return cudaGetLastError();
@@ -27,10 +28,12 @@ template <typename T, typename R>
 cudaError_t dispatch_step(int q, int c, const StepBuffers& b, const StepParams& P, cudaStream_t st,
                           int64_t* launches, const StepEvents* ev) {
   const bool w = b.mask != nullptr;
-#define LB_CASE(QQ, CC)                                                     \
-  if (q == QQ && c == CC)                                                   \
-    return w ? launch_step_t<T, R, QQ, CC, true>(b, P, st, launches, ev)        \
-             : launch_step_t<T, R, QQ, CC, false>(b, P, st, launches, ev);
+  const bool nbm = w && b.nbmask != nullptr;
+#define LB_CASE(QQ, CC)                                                               \
+  if (q == QQ && c == CC)                                                             \
+    return nbm ? launch_step_t<T, R, QQ, CC, true, true>(b, P, st, launches, ev)      \
+           : w ? launch_step_t<T, R, QQ, CC, true>(b, P, st, launches, ev)            \
+               : launch_step_t<T, R, QQ, CC, false>(b, P, st, launches, ev);
   LB_CASE(19, 2)
   LB_CASE(19, 1)
   LB_CASE(9, 2)
@@ -46,18 +49,18 @@ cudaError_t dispatch_step(int q, int c, const StepBuffers& b, const StepParams& 
 // One kernel of the timestep over the sites [P.s_begin, P.s_end) (whole
 // x-planes): part kPartDensityPsi queues k_density_psi, kPartCollide
 // k_collide.  The per-site arithmetic is that of launch_step_t.
-template <typename T, typename R, int Q, int C, bool W>
+template <typename T, typename R, int Q, int C, bool W, bool NBM = false>
 cudaError_t launch_part_t(int part, const StepBuffers& b, const StepParams& P, cudaStream_t st, int64_t* launches) {
   const int64_t count = P.s_end - P.s_begin;
   if (P.s_end <= 0 || count <= 0 || P.s_begin < 0 || P.s_end > P.n) return cudaErrorInvalidValue;
   const unsigned blocks = unsigned((count + kStepThreads - 1) / kStepThreads);
   if (part == kPartDensityPsi)
-    k_density_psi<T, R, Q, C, W><<<blocks, kStepThreads, 0, st>>>(static_cast<const T*>(b.f), b.mask,
-                                                                   static_cast<R*>(b.rho), static_cast<R*>(b.psi), P);
+    k_density_psi<T, R, Q, C, W, true, NBM><<<blocks, kStepThreads, 0, st>>>(
+        static_cast<const T*>(b.f), b.mask, b.nbmask, static_cast<R*>(b.rho), static_cast<R*>(b.psi), P);
   else if (part == kPartCollide)
-    k_collide<T, R, Q, C, W><<<blocks, kStepThreads, 0, st>>>(static_cast<const T*>(b.f), static_cast<T*>(b.fout),
-                                                               b.mask, static_cast<const R*>(b.rho),
-                                                               static_cast<const R*>(b.psi), b.force, P);
+    k_collide<T, R, Q, C, W, true, NBM><<<blocks, kStepThreads, 0, st>>>(
+        static_cast<const T*>(b.f), static_cast<T*>(b.fout), b.mask, b.nbmask, static_cast<const R*>(b.rho),
+        static_cast<const R*>(b.psi), b.force, P);
   else
     return cudaErrorInvalidValue;
   *launches += 1;
@@ -68,10 +71,12 @@ template <typename T, typename R>
 cudaError_t dispatch_part(int part, int q, int c, const StepBuffers& b, const StepParams& P, cudaStream_t st,
                           int64_t* launches) {
   const bool w = b.mask != nullptr;
-#define LB_CASE(QQ, CC)                                                 \
-  if (q == QQ && c == CC)                                               \
-    return w ? launch_part_t<T, R, QQ, CC, true>(part, b, P, st, launches) \
-             : launch_part_t<T, R, QQ, CC, false>(part, b, P, st, launches);
+  const bool nbm = w && b.nbmask != nullptr;
+#define LB_CASE(QQ, CC)                                                           \
+  if (q == QQ && c == CC)                                                         \
+    return nbm ? launch_part_t<T, R, QQ, CC, true, true>(part, b, P, st, launches) \
+           : w ? launch_part_t<T, R, QQ, CC, true>(part, b, P, st, launches)       \
+               : launch_part_t<T, R, QQ, CC, false>(part, b, P, st, launches);
   LB_CASE(19, 2)
   LB_CASE(19, 1)
   LB_CASE(9, 2)
@@ -96,9 +101,9 @@ cudaError_t launch_phase_t(int phase, const StepBuffers& b, const StepParams& P,
     *launches += 1;
   } else {
     k_density_psi<T, R, Q, C, W, false><<<blocks, kStepThreads, 0, st>>>(
-        static_cast<const T*>(b.f), b.mask, static_cast<R*>(b.rho), static_cast<R*>(b.psi), P);
+        static_cast<const T*>(b.f), b.mask, nullptr, static_cast<R*>(b.rho), static_cast<R*>(b.psi), P);
     k_collide<T, R, Q, C, W, false><<<blocks, kStepThreads, 0, st>>>(
-        static_cast<const T*>(b.f), static_cast<T*>(b.fout), b.mask, static_cast<const R*>(b.rho),
+        static_cast<const T*>(b.f), static_cast<T*>(b.fout), b.mask, nullptr, static_cast<const R*>(b.rho),
         static_cast<const R*>(b.psi), b.force, P);
     *launches += 2;
   }
