@@ -27,6 +27,8 @@ FusedParams make_fused_params(const StepParams& P, int ty, int q) {
   F.run_len = P.nx;
   F.x_begin = 0;
   F.x_end = P.nx;
+  F.x_split = P.nx;
+  F.tail_len = 1;
   for (int c = 0; c < 2; ++c) {
     F.tau[c] = float(P.tau[c]);
     F.inv_tau[c] = float(1.0 / P.tau[c]);

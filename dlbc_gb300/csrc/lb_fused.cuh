@@ -81,7 +81,56 @@ struct FusedParams {
   // plane range [x_begin, x_end) of the dynamically scheduled kernels (the
   // whole lattice: 0, nx)
   int32_t x_begin, x_end;
+  // the single-lattice schedule: planes [x_begin, x_split) of every tile in
+  // runs of run_len, then [x_split, x_end) in runs of tail_len
+  int32_t x_split, tail_len;
 };
+
+// The dynamic schedule of the single-lattice kernels (k_fused, k_pairs,
+// k_fused2d): work item i of a counter is a run of planes [x0, x1) of one of
+// ntl tiles.  The first items cover planes [x_begin, x_split) of every tile
+// in runs of run_len, x-chunk-major (neighbouring tiles march over the same
+// planes at the same time and share their ring sites through L2); the last
+// cover [x_split, x_end) in the shorter runs of tail_len.  The CTAs take
+// those last, so the step ends at nearly the same time on every CTA instead
+// of waiting for the few that drew a last long run.
+__host__ __device__ __forceinline__ int sched_units(const FusedParams& P, int ntl) {
+  const int bulk = (P.x_split - P.x_begin) / P.run_len;
+  const int tail = (P.x_end - P.x_split + P.tail_len - 1) / P.tail_len;
+  return ntl * (bulk + tail);
+}
+__device__ __forceinline__ void sched_run(const FusedParams& P, int ntl, int item, int& tile, int& x0, int& x1) {
+  const int ub = ntl * ((P.x_split - P.x_begin) / P.run_len);
+  if (item < ub) {
+    const int ch = item / ntl;
+    tile = item - ch * ntl;
+    x0 = P.x_begin + ch * P.run_len;
+    x1 = x0 + P.run_len;
+  } else {
+    const int j = item - ub;
+    const int ch = j / ntl;
+    tile = j - ch * ntl;
+    x0 = P.x_split + ch * P.tail_len;
+    x1 = min(x0 + P.tail_len, P.x_end);
+  }
+}
+// Run lengths for `tiles` tiles and `grid` resident CTAs: runs of 32 planes
+// (halved while there would be fewer runs than CTAs; every run gathers two
+// extra planes to warm up), and about two runs per CTA of a quarter of that
+// length at the end of every tile.
+inline void plan_runs(FusedParams& G, int64_t tiles, int64_t grid) {
+  const int span = G.x_end - G.x_begin;
+  int rl = 32;
+  while (rl > 4 && tiles * ((span + rl - 1) / rl) < grid) rl /= 2;
+  if (rl > span) rl = span;
+  const int tl = rl >= 8 ? rl / 4 : rl;
+  int tail = int((2 * grid * tl + tiles - 1) / tiles);
+  tail = ((tail + tl - 1) / tl) * tl;
+  if (tail > span / 2) tail = span / 2;
+  G.run_len = rl;
+  G.tail_len = tl;
+  G.x_split = G.x_begin + ((span - tail) / rl) * rl;
+}
 
 // Storage of connectivity Q (D3Q19 or D2Q9): the half form's constants
 // depend on q only through its weight class.
@@ -525,25 +574,22 @@ __global__ void __launch_bounds__(TY * kFusedTZ, MOM ? (8 / TY) * mom_ctas<WALLS
     fused_body<T, C, WALLS, TY, MOM>(P, f, fout, nbmask, force_out, w0, w1, sh);
     return;
   }
-  // dynamic: runs of run_len planes of one tile taken from a counter, so
-  // that CTAs on cheap (wall-free) tiles take more runs; in x-chunk-major
-  // order, so that neighbouring tiles march over the same planes at the same
-  // time and the ring sites one gathers are still in L2 when the other
-  // reads them (8-12 % faster than tile-major order)
+  // dynamic: runs of planes of one tile taken from a counter (sched_run),
+  // so that CTAs on cheap (wall-free) tiles take more runs; x-chunk-major
+  // (8-12 % faster than tile-major order)
   __shared__ int s_item;
-  const int nchunks = (P.x_end - P.x_begin + P.run_len - 1) / P.run_len;
-  const int units = P.tiles_y * P.tiles_z * nchunks;
+  const int ntl = P.tiles_y * P.tiles_z;
+  const int units = sched_units(P, ntl);
   for (;;) {
     __syncthreads();  // every thread has read the previous item
     if (threadIdx.x == 0) s_item = atomicAdd(P.work_counter, 1);
     __syncthreads();
     const int item = s_item;
     if (item >= units) break;
-    const int ntl = P.tiles_y * P.tiles_z;
-    const int ch = item / ntl, tile = item - ch * ntl;
-    const int64_t w0 = int64_t(tile) * P.nx + P.x_begin + int64_t(ch) * P.run_len;
-    const int64_t w1 = min(w0 + P.run_len, int64_t(tile) * P.nx + P.x_end);
-    fused_body<T, C, WALLS, TY, MOM>(P, f, fout, nbmask, force_out, w0, w1, sh);
+    int tile, x0, x1;
+    sched_run(P, ntl, item, tile, x0, x1);
+    const int64_t w0 = int64_t(tile) * P.nx + x0;
+    fused_body<T, C, WALLS, TY, MOM>(P, f, fout, nbmask, force_out, w0, w0 + (x1 - x0), sh);
   }
 }
 

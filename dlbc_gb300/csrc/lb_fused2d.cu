@@ -23,13 +23,8 @@ cudaError_t go2d(const StepBuffers& b, const FusedParams& F, cudaStream_t st, in
   FusedParams G = F;
   G.tiles_y = 1;
   G.tiles_z = (G.ny + kF2W - 1) / kF2W;
-  // runs of 32 rows, halved while there would be fewer than two runs per CTA
-  // (each run gathers two extra rows to warm up)
-  const int span = G.x_end - G.x_begin;
-  int rl = 32;
-  while (rl > 4 && int64_t(G.tiles_z) * ((span + rl - 1) / rl) < 2 * grid) rl /= 2;
-  G.run_len = rl < span ? rl : span;
-  const int64_t units = int64_t(G.tiles_z) * ((span + G.run_len - 1) / G.run_len);
+  plan_runs(G, G.tiles_z, grid);
+  const int64_t units = sched_units(G, G.tiles_z);
   if (grid > units) grid = units;
   kern<<<unsigned(grid), kF2W, smem, st>>>(static_cast<const T*>(b.f), static_cast<T*>(b.fout), b.nbmask, b.force,
                                             G);

@@ -17,10 +17,10 @@
 // wall force, as in the D3Q19 kernel; solid sites are not written (both
 // population buffers hold them).
 //
-// Scheduling: runs of run_len consecutive rows of one tile taken from an
-// atomic counter in x-chunk-major order (neighbouring tiles march together),
-// or, without a counter, run items strided over the CTAs.  Every run starts
-// with two warm-up rows.
+// Scheduling: runs of consecutive rows of one tile taken from an atomic
+// counter (sched_run: x-chunk-major, shorter runs last), or, without a
+// counter, run items strided over the CTAs.  Every run starts with two
+// warm-up rows.
 //
 // Per-site arithmetic restates the reference (addShanChenForcePsi
 // force.d:238-309, distributeForce force.d:179-197,
@@ -304,7 +304,7 @@ __device__ __forceinline__ void fused2d_run(const FusedParams& P, const T* __res
 }
 
 // P.tiles_z y-segments of kF2W sites per row (P.tiles_y = 1); rows
-// [P.x_begin, P.x_end) in runs of P.run_len
+// [P.x_begin, P.x_end) in the runs of sched_run
 template <typename T, int C, bool WALLS, bool MOM>
 __global__ void __launch_bounds__(kF2W, MOM ? 4 : 3)
     k_fused2d(const T* __restrict__ f, T* __restrict__ fout, const uint32_t* __restrict__ nbmask,
@@ -313,8 +313,7 @@ __global__ void __launch_bounds__(kF2W, MOM ? 4 : 3)
   Fused2Shared<MOM ? 2 : 9>& sh = *reinterpret_cast<Fused2Shared<MOM ? 2 : 9>*>(smem_raw);
   __shared__ int s_item;
   const int tiles = P.tiles_z;
-  const int nchunks = (P.x_end - P.x_begin + P.run_len - 1) / P.run_len;
-  const int units = tiles * nchunks;
+  const int units = sched_units(P, tiles);
   int next = blockIdx.x;
   for (;;) {
     __syncthreads();  // every thread has read the previous item
@@ -323,9 +322,8 @@ __global__ void __launch_bounds__(kF2W, MOM ? 4 : 3)
     const int item = s_item;
     next += gridDim.x;
     if (item >= units) break;
-    const int ch = item / tiles, tile = item - ch * tiles;
-    const int xa = P.x_begin + ch * P.run_len;
-    const int xb = min(xa + P.run_len, P.x_end);
+    int tile, xa, xb;
+    sched_run(P, tiles, item, tile, xa, xb);
     fused2d_run<T, C, WALLS, MOM>(P, f, fout, nbmask, force_out, tile, xa, xb, sh);
   }
 }

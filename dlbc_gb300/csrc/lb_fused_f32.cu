@@ -22,13 +22,10 @@ cudaError_t go_single(const StepBuffers& b, const FusedParams& F, cudaStream_t s
   int64_t grid = int64_t(per_sm) * sm_count(device);
   FusedParams G = F;
   if (G.work_counter) {
-    // runs of 32 planes, halved while there would be fewer than two runs
-    // per CTA (each run gathers two extra planes to warm up)
     const int64_t tiles = int64_t(G.tiles_y) * G.tiles_z;
-    const int span = G.x_end - G.x_begin;
-    int rl = 32;
-    while (rl > 4 && tiles * ((span + rl - 1) / rl) < 2 * grid) rl /= 2;
-    G.run_len = rl < span ? rl : span;
+    plan_runs(G, tiles, grid);
+    const int64_t units = sched_units(G, int(tiles));
+    if (grid > units) grid = units;
   }
   if (grid > G.work) grid = G.work;
   kern<<<unsigned(grid), TY * kFusedTZ, smem, st>>>(static_cast<const T*>(b.f), static_cast<T*>(b.fout), b.nbmask,

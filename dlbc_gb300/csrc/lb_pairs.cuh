@@ -737,19 +737,18 @@ __global__ void __launch_bounds__(kPairThreads, (MOM || sizeof(T) == 2) ? LB_PAI
   extern __shared__ __align__(16) unsigned char smem_raw[];
   auto& sh = *reinterpret_cast<PairShared<C, WALLS, MOM, T>*>(smem_raw);
   __shared__ int s_item;
-  const int nchunks = (P.x_end - P.x_begin + P.run_len - 1) / P.run_len;
   const int ntl = P.tiles_y * P.tiles_z;
-  const int units = ntl * nchunks;
+  const int units = sched_units(P, ntl);
   for (;;) {
     __syncthreads();  // every thread has read the previous item
     if (threadIdx.x == 0) s_item = atomicAdd(P.work_counter, 1);
     __syncthreads();
     const int item = s_item;
     if (item >= units) break;
-    const int ch = item / ntl, tile = item - ch * ntl;
-    const int64_t w0 = int64_t(tile) * P.nx + P.x_begin + int64_t(ch) * P.run_len;
-    const int64_t w1 = min(w0 + P.run_len, int64_t(tile) * P.nx + P.x_end);
-    pair_body<T, C, WALLS, MOM>(P, f, fout, nbmask, row_walls, force_out, w0, w1, sh);
+    int tile, x0, x1;
+    sched_run(P, ntl, item, tile, x0, x1);
+    const int64_t w0 = int64_t(tile) * P.nx + x0;
+    pair_body<T, C, WALLS, MOM>(P, f, fout, nbmask, row_walls, force_out, w0, w0 + (x1 - x0), sh);
   }
 }
 
@@ -842,14 +841,9 @@ cudaError_t go_pairs(const StepBuffers& b, const FusedParams& F, cudaStream_t st
   if (e != cudaSuccess) return e;
   int64_t grid = int64_t(per_sm) * sm_count(device);
   FusedParams G = F;
-  // runs of 32 planes, halved while there would be fewer than 1.5 runs per
-  // CTA (each run gathers two extra planes to warm up)
   const int64_t tiles = int64_t(G.tiles_y) * G.tiles_z;
-  const int span = G.x_end - G.x_begin;
-  int rl = 32;
-  while (rl > 4 && 2 * tiles * ((span + rl - 1) / rl) < 3 * grid) rl /= 2;
-  G.run_len = rl < span ? rl : span;
-  const int64_t units = tiles * ((span + G.run_len - 1) / G.run_len);
+  plan_runs(G, tiles, grid);
+  const int64_t units = sched_units(G, int(tiles));
   if (grid > units) grid = units;
   kern<<<unsigned(grid), kPairThreads, smem, st>>>(static_cast<const T*>(b.f), static_cast<T*>(b.fout), b.nbmask,
                                                    b.row_walls, b.force, G);
