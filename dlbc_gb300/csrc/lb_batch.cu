@@ -117,7 +117,7 @@ std::string signature(const lbgpu_batch* b) {
 // lone lattice, lbk::pairs_eligible)
 bool pair_member(const lbgpu_handle* h) {
   if (!(h->nz % 2 == 0 && h->P.eq_form == 2)) return false;
-  return h->cfg.precision == LBGPU_I16 || (h->P.unit_tau != 0 && h->mask == nullptr);
+  return h->mask == nullptr && (h->cfg.precision == LBGPU_I16 || h->P.unit_tau != 0);
 }
 
 template <typename D>
@@ -257,7 +257,10 @@ cudaError_t launch_one(lbgpu_batch* b, int parity) {
   }
   if (!b->table_n) return cudaSuccess;
   b->launches++;
-  return lbk::launch_fused_batch(b->precision == LBGPU_FP16, b->shape.ty, b->walls, b->d_table, b->table_n,
+  const int kind = b->precision == LBGPU_FP16  ? lbk::kStoreF16
+                   : b->precision == LBGPU_I16 ? lbk::kStoreI16
+                                               : lbk::kStoreF32;
+  return lbk::launch_fused_batch(kind, b->shape.ty, b->walls, b->d_table, b->table_n,
                                  b->total_work, parity, b->shape.ctas_per_sm, b->stream, b->device,
                                  b->total_units,
                                  (!kStatic && b->total_units < (int64_t(1) << 31)) ? b->d_counters : nullptr);

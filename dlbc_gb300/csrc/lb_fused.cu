@@ -62,10 +62,10 @@ bool pairs_eligible(int kind, const StepParams& P, const StepBuffers& b) {
   // the BDist2 equilibrium and schedules through the work counter
   if (!(P.nz % 2 == 0 && P.eq_form == 2 && b.work_counter != nullptr && (b.mask == nullptr || b.row_walls != nullptr)))
     return false;
-  // I16 runs on the pair kernel only; FP32 and FP16 where it is the faster
-  // kernel: every tau = 1 and no solid site (measured on GB300: walls and
-  // the relaxation's shared-memory populations favour one site per thread)
-  return kind == kStoreI16 || (P.unit_tau != 0 && b.mask == nullptr);
+  // where it is the faster kernel (measured on GB300): no solid site, and
+  // every tau = 1 or the I16 storage (walls, and for FP32/FP16 the
+  // relaxation's shared-memory populations, favour one site per thread)
+  return b.mask == nullptr && (kind == kStoreI16 || P.unit_tau != 0);
 }
 
 // the fused step over planes [x0, x1) of every tile (the host transfers
@@ -95,10 +95,10 @@ cudaError_t launch_fused_range(int kind, int q, int c, const StepBuffers& b, con
            : kind == kStoreI16 ? launch_pairs_single_i16(c, w, mom, b, G, st, device)
                                : launch_pairs_single_f32(c, w, mom, b, G, st, device);
   }
-  if (kind == kStoreI16) return cudaErrorInvalidValue;
   const bool mom = c == 2 && P.unit_tau && P.eq_form == 2;
-  return kind == kStoreF16 ? launch_fused_single_f16(c, w, mom, b, G, st, device)
-                           : launch_fused_single_f32(c, w, mom, b, G, st, device);
+  return kind == kStoreF16   ? launch_fused_single_f16(c, w, mom, b, G, st, device)
+         : kind == kStoreI16 ? launch_fused_single_i16(c, w, mom, b, G, st, device)
+                             : launch_fused_single_f32(c, w, mom, b, G, st, device);
 }
 
 cudaError_t launch_fused(int kind, int q, int c, const StepBuffers& b, const StepParams& P, cudaStream_t st,
@@ -130,12 +130,11 @@ cudaError_t launch_fused(int kind, int q, int c, const StepBuffers& b, const Ste
     e = kind == kStoreF16   ? launch_pairs_single_f16(c, w, mom, b, G, st, device)
         : kind == kStoreI16 ? launch_pairs_single_i16(c, w, mom, b, G, st, device)
                             : launch_pairs_single_f32(c, w, mom, b, G, st, device);
-  } else if (kind == kStoreI16) {
-    e = cudaErrorInvalidValue;  // the I16 form runs on the pair kernel only
   } else {
     const bool mom = c == 2 && P.unit_tau && P.eq_form == 2;
-    e = kind == kStoreF16 ? launch_fused_single_f16(c, w, mom, b, F, st, device)
-                          : launch_fused_single_f32(c, w, mom, b, F, st, device);
+    e = kind == kStoreF16   ? launch_fused_single_f16(c, w, mom, b, F, st, device)
+        : kind == kStoreI16 ? launch_fused_single_i16(c, w, mom, b, F, st, device)
+                            : launch_fused_single_f32(c, w, mom, b, F, st, device);
   }
   if (ev) cudaEventRecord(ev->ev[2], st);
   *launches += 1;

@@ -159,6 +159,22 @@ struct FStore<__half, Q> {
     *p = __float2half_rn(fmaf(v, P.inv_wscale[c][Conn<Q>::wclass(q)], P.hoff[c][Conn<Q>::wclass(q)]));
   }
 };
+// 16-bit fixed-point offsets (LBGPU_I16): the half form's constants, the
+// offset rounded to the nearest integer (ties to even) and saturated to
+// +-32767, as the pair kernel stores it
+template <int Q>
+struct FStore<int16_t, Q> {
+  __device__ static __forceinline__ float load(const int16_t* p, int c, int q, const FusedParams& P) {
+    return fmaf(P.wscale[c][Conn<Q>::wclass(q)], float(__ldg(p)), P.wrho[c][Conn<Q>::wclass(q)]);
+  }
+  __device__ static __forceinline__ float load2(const int16_t* p, int c, int q, int, bool, const FusedParams& P) {
+    return load(p, c, q, P);
+  }
+  __device__ static __forceinline__ void store(int16_t* p, float v, int c, int q, const FusedParams& P) {
+    const int h = __float2int_rn(fmaf(v, P.inv_wscale[c][Conn<Q>::wclass(q)], P.hoff[c][Conn<Q>::wclass(q)]));
+    *p = int16_t(h < -32767 ? -32767 : (h > 32767 ? 32767 : h));
+  }
+};
 
 // NP = 19: the tile's populations; NP = 3: its momentum per component (the
 // populations-free collision), which leaves room for more CTAs per SM

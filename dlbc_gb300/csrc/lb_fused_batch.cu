@@ -56,14 +56,20 @@ cudaError_t launch_pairs_batch(int kind, bool walls, const PairSim* sims, int ns
 #undef LB_PBATCH
 }
 
-cudaError_t launch_fused_batch(bool half_storage, int ty, bool walls, const FusedSim* sims, int nsims,
+cudaError_t launch_fused_batch(int kind, int ty, bool walls, const FusedSim* sims, int nsims,
                                int64_t total_work, int parity, int ctas_per_sm, cudaStream_t st, int device,
                                int64_t total_units, int* counters) {
 #define LB_BATCH(T, W, TYV) \
   go_batch<T, W, TYV>(sims, nsims, total_work, parity, ctas_per_sm, st, device, total_units, counters)
-  if (half_storage) {
+  if (kind == kStoreF16) {
     if (ty == 4) return walls ? LB_BATCH(__half, true, 4) : LB_BATCH(__half, false, 4);
     return walls ? LB_BATCH(__half, true, 8) : LB_BATCH(__half, false, 8);
+  }
+  if (kind == kStoreI16) {
+    // I16 members here have solid sites (the rest run the pair batch)
+    if (!walls) return cudaErrorInvalidValue;
+    if (ty == 4) return LB_BATCH(int16_t, true, 4);
+    return LB_BATCH(int16_t, true, 8);
   }
   if (ty == 4) return walls ? LB_BATCH(float, true, 4) : LB_BATCH(float, false, 4);
   return walls ? LB_BATCH(float, true, 8) : LB_BATCH(float, false, 8);

@@ -44,6 +44,17 @@ cudaError_t launch_fused_single_f16(int c, bool w, bool mom, const StepBuffers& 
   return w ? go_single<__half, 1, true, 8>(b, F, st, device) : go_single<__half, 1, false, 8>(b, F, st, device);
 }
 
+// I16 lattices with solid sites (the pair kernel's walled rows are slower)
+cudaError_t launch_fused_single_i16(int c, bool w, bool mom, const StepBuffers& b, const FusedParams& F,
+                                   cudaStream_t st, int device) {
+  if (mom)
+    return w ? go_single<int16_t, 2, true, 8, true>(b, F, st, device)
+             : go_single<int16_t, 2, false, 8, true>(b, F, st, device);
+  if (c == 2)
+    return w ? go_single<int16_t, 2, true, 8>(b, F, st, device) : go_single<int16_t, 2, false, 8>(b, F, st, device);
+  return w ? go_single<int16_t, 1, true, 8>(b, F, st, device) : go_single<int16_t, 1, false, 8>(b, F, st, device);
+}
+
 cudaError_t launch_pairs_single_f16(int c, bool w, bool mom, const StepBuffers& b, const FusedParams& F,
                                     cudaStream_t st, int device) {
   return launch_pairs<__half>(c, w, mom, b, F, st, device);

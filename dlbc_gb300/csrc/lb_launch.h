@@ -100,7 +100,7 @@ FusedParams make_fused_params(const StepParams& P, int ty, int q = 19);
 // D3Q19) in one persistent launch.  ctas_per_sm <= 0: as many as fit.
 // counters (two ints, zero before the first launch): dynamic scheduling of
 // total_units runs; nullptr: static equal ranges of total_work plane-tiles.
-cudaError_t launch_fused_batch(bool half_storage, int ty, bool walls, const FusedSim* sims, int nsims,
+cudaError_t launch_fused_batch(int kind, int ty, bool walls, const FusedSim* sims, int nsims,
                                int64_t total_work, int parity, int ctas_per_sm, cudaStream_t stream, int device,
                                int64_t total_units, int* counters);
 // The pair-kernel batch (lb_pairs.cuh): members with an even z extent and the
