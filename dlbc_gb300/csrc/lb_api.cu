@@ -519,9 +519,8 @@ int lb_handle_create(const lbgpu_config* cfg, bool lite, double* staging, size_t
 int64_t lb_member_bytes(const lbgpu_config* cfg) {
   int64_t n = 1;
   for (int i = 0; i < cfg->d; ++i) n *= cfg->gn[i];
-  // populations (two buffers), mask byte, 32-bit neighbour mask and the
-  // pair step's row wall flags (at most one byte per two sites)
-  return 2 * int64_t(cfg->components) * cfg->q * n * int64_t(storage_size(cfg->precision)) + 5 * n + n / 2 + 1;
+  // populations (two buffers), mask byte and 32-bit neighbour mask
+  return 2 * int64_t(cfg->components) * cfg->q * n * int64_t(storage_size(cfg->precision)) + 5 * n + 1;
 }
 
 // Neighbour mask of every site: bit 0 the site's own solid flag, bit q the
@@ -569,19 +568,6 @@ __global__ void k_tile_walls(const uint32_t* __restrict__ nbm, uint8_t* __restri
   out[i] = any != 0;
 }
 
-// Wall flag of every (x, y, 64-site z segment) for the pair step: 1 if a
-// site of the segment has a nonzero neighbour mask.
-__global__ void k_row_walls(const uint32_t* __restrict__ nbm, uint8_t* __restrict__ out, Geo g, int segs) {
-  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (i >= int64_t(g.nx) * g.ny * segs) return;
-  const int64_t row = i / segs;
-  const int z0 = int(i - row * segs) * lbk::kPairTZ;
-  const int z1 = min(z0 + lbk::kPairTZ, g.nz);
-  uint32_t any = 0;
-  for (int z = z0; z < z1; ++z) any |= nbm[row * g.nz + z];
-  out[i] = any != 0;
-}
-
 int lb_sync_solids(lbgpu_handle* h, int cur, cudaStream_t st) {
   if (!h->mask || !h->fused || h->solids_synced) return LBGPU_OK;
   cudaError_t e = cudaMemcpyAsync(h->f[1 - cur], h->f[cur], h->fbytes, cudaMemcpyDeviceToDevice, st);
@@ -597,14 +583,7 @@ int lb_update_nbmask(lbgpu_handle* h) {
   const bool want = h->mask != nullptr;
   const int tiles_y = (h->ny + 7) / 8, tiles_z = (h->nz + 31) / 32;
   const int64_t nflags = int64_t(h->nx) * tiles_y * tiles_z;
-  const int segs = (h->nz + lbk::kPairTZ - 1) / lbk::kPairTZ;
-  const int64_t nrow = int64_t(h->nx) * h->ny * segs;
   if (!want) {
-    if (h->row_walls) {
-      cudaFree(h->row_walls);
-      h->device_bytes -= nrow;
-      h->row_walls = nullptr;
-    }
     if (h->nbmask) {
       cudaFree(h->nbmask);
       h->device_bytes -= 4 * h->n;
@@ -638,22 +617,9 @@ int lb_update_nbmask(lbgpu_handle* h) {
   h->launches++;
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return h->cuda_fail(e, "neighbour mask kernel");
-  // the row and tile wall flags: the D3Q19 fused kernels only
-  if (h->Q != 19 || !(h->fused || h->lite)) return LBGPU_OK;
-  if (!h->row_walls) {
-    e = cudaMalloc(&h->row_walls, size_t(nrow));
-    if (e != cudaSuccess) {
-      cudaGetLastError();
-      h->row_walls = nullptr;
-      return h->fail(LBGPU_E_NOMEM, "row wall flags allocation failed");
-    }
-    h->device_bytes += nrow;
-  }
-  k_row_walls<<<unsigned(ceil_div(nrow, 128)), 128, 0, h->stream>>>(h->nbmask, h->row_walls, geo_of(h), segs);
-  h->launches++;
-  e = cudaGetLastError();
-  if (e != cudaSuccess) return h->cuda_fail(e, "row wall flags kernel");
-  if (h->lite) return LBGPU_OK;  // batch members use other tile shapes
+  // the tile wall flags: the D3Q19 one-site fused kernel of a lone lattice
+  // (batch members use other tile shapes)
+  if (h->Q != 19 || !h->fused || h->lite) return LBGPU_OK;
   if (!h->tile_walls) {
     e = cudaMalloc(&h->tile_walls, size_t(nflags));
     if (e != cudaSuccess) {
@@ -709,7 +675,6 @@ void lbgpu_destroy(lbgpu_handle* h) {
   if (h->mask) cudaFree(h->mask);
   if (h->nbmask) cudaFree(h->nbmask);
   if (h->tile_walls) cudaFree(h->tile_walls);
-  if (h->row_walls) cudaFree(h->row_walls);
   if (h->work_counter) cudaFree(h->work_counter);
   if (h->force) cudaFree(h->force);
   for (auto& e : h->ev_pending)
@@ -943,7 +908,6 @@ int lbgpu_step(lbgpu_handle* h, int32_t nsteps) {
     b.mask = h->mask;
     b.nbmask = h->nbmask;
     b.tile_walls = h->tile_walls;
-    b.row_walls = h->row_walls;
     b.work_counter = h->work_counter;
     b.rho = h->rho;
     b.psi = h->psi;
@@ -1093,7 +1057,6 @@ int step_host_wave(lbgpu_handle* h, const double* const* in, double* const* out,
   b.mask = h->mask;
   b.nbmask = h->nbmask;
   b.tile_walls = h->tile_walls;
-  b.row_walls = h->row_walls;
   b.work_counter = h->work_counter;
   b.rho = h->rho;
   b.psi = h->psi;

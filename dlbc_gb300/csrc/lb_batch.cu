@@ -73,7 +73,6 @@ struct lbgpu_batch {
   int ptable_n = 0;
   int64_t ptotal_units = 0;
   int* d_pcounters = nullptr;
-  bool pwalls = false;
   bool dirty = true;
   int64_t steps_since_build = 0;
   std::vector<int> table_ids;
@@ -153,7 +152,6 @@ int build_table(lbgpu_batch* b, const Shape& sh) {
   b->total_units = 0;
   b->ptotal_units = 0;
   b->walls = false;
-  b->pwalls = false;
   for (size_t id = 0; id < b->sims.size(); ++id) {
     lbgpu_handle* h = b->sims[id];
     if (!h) continue;
@@ -167,14 +165,11 @@ int build_table(lbgpu_batch* b, const Shape& sh) {
       ps.P.run_len = h->nx < sh.prun ? h->nx : sh.prun;
       ps.f[0] = h->f[0];
       ps.f[1] = h->f[1];
-      ps.nbmask = h->nbmask;
-      ps.row_walls = h->row_walls;
       ps.force_out = nullptr;
       ps.phase = h->cur;
       ps.nchunks = (h->nx + ps.P.run_len - 1) / ps.P.run_len;
       ps.unit_begin = b->ptotal_units;
       b->ptotal_units += int64_t(ps.P.tiles_y) * ps.P.tiles_z * ps.nchunks;
-      b->pwalls = b->pwalls || h->mask != nullptr;
       ptab.push_back(ps);
     } else {
       lbk::FusedSim fs;
@@ -251,7 +246,7 @@ cudaError_t launch_one(lbgpu_batch* b, int parity) {
     const int kind = b->precision == LBGPU_FP16  ? lbk::kStoreF16
                      : b->precision == LBGPU_I16 ? lbk::kStoreI16
                                                  : lbk::kStoreF32;
-    cudaError_t e = lbk::launch_pairs_batch(kind, b->pwalls, b->d_ptable, b->ptable_n, parity, b->shape.pctas,
+    cudaError_t e = lbk::launch_pairs_batch(kind, b->d_ptable, b->ptable_n, parity, b->shape.pctas,
                                             b->stream, b->device, b->ptotal_units, b->d_pcounters);
     if (e != cudaSuccess) return e;
   }

@@ -60,8 +60,7 @@ FusedParams make_fused_params(const StepParams& P, int ty, int q) {
 bool pairs_eligible(int kind, const StepParams& P, const StepBuffers& b) {
   // aligned two-site words need an even z extent; the pair kernel computes
   // the BDist2 equilibrium and schedules through the work counter
-  if (!(P.nz % 2 == 0 && P.eq_form == 2 && b.work_counter != nullptr && (b.mask == nullptr || b.row_walls != nullptr)))
-    return false;
+  if (!(P.nz % 2 == 0 && P.eq_form == 2 && b.work_counter != nullptr)) return false;
   // where it is the faster kernel (measured on GB300): no solid site, and
   // every tau = 1 or the I16 storage (walls, and for FP32/FP16 the
   // relaxation's shared-memory populations, favour one site per thread)
@@ -91,9 +90,9 @@ cudaError_t launch_fused_range(int kind, int q, int c, const StepBuffers& b, con
     G.tiles_z = (P.nz + kPairTZ - 1) / kPairTZ;
     G.work = int64_t(G.tiles_y) * G.tiles_z * P.nx;
     const bool mom = P.unit_tau != 0;
-    return kind == kStoreF16   ? launch_pairs_single_f16(c, w, mom, b, G, st, device)
-           : kind == kStoreI16 ? launch_pairs_single_i16(c, w, mom, b, G, st, device)
-                               : launch_pairs_single_f32(c, w, mom, b, G, st, device);
+    return kind == kStoreF16   ? launch_pairs_single_f16(c, mom, b, G, st, device)
+           : kind == kStoreI16 ? launch_pairs_single_i16(c, mom, b, G, st, device)
+                               : launch_pairs_single_f32(c, mom, b, G, st, device);
   }
   const bool mom = c == 2 && P.unit_tau && P.eq_form == 2;
   return kind == kStoreF16   ? launch_fused_single_f16(c, w, mom, b, G, st, device)
@@ -127,9 +126,9 @@ cudaError_t launch_fused(int kind, int q, int c, const StepBuffers& b, const Ste
     G.tiles_z = (P.nz + kPairTZ - 1) / kPairTZ;
     G.work = int64_t(G.tiles_y) * G.tiles_z * P.nx;
     const bool mom = P.unit_tau != 0;
-    e = kind == kStoreF16   ? launch_pairs_single_f16(c, w, mom, b, G, st, device)
-        : kind == kStoreI16 ? launch_pairs_single_i16(c, w, mom, b, G, st, device)
-                            : launch_pairs_single_f32(c, w, mom, b, G, st, device);
+    e = kind == kStoreF16   ? launch_pairs_single_f16(c, mom, b, G, st, device)
+        : kind == kStoreI16 ? launch_pairs_single_i16(c, mom, b, G, st, device)
+                            : launch_pairs_single_f32(c, mom, b, G, st, device);
   } else {
     const bool mom = c == 2 && P.unit_tau && P.eq_form == 2;
     e = kind == kStoreF16   ? launch_fused_single_f16(c, w, mom, b, F, st, device)

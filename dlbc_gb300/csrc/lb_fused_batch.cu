@@ -28,12 +28,12 @@ cudaError_t go_batch(const FusedSim* sims, int nsims, int64_t total, int parity,
   return cudaGetLastError();
 }
 
-template <typename T, bool W>
+template <typename T>
 cudaError_t go_pairs_batch(const PairSim* sims, int nsims, int parity, int ctas_per_sm, cudaStream_t st, int device,
                            int64_t total_units, int* counters) {
   static KernelInfo info;
-  auto kern = k_pairs_batch<T, W>;
-  const int smem = int(sizeof(PairShared<2, W, false, T>));
+  auto kern = k_pairs_batch<T>;
+  const int smem = int(sizeof(PairShared<2, false, T>));
   int per_sm = 0;
   cudaError_t e = kernel_setup(kern, smem, kPairThreads, device, info, &per_sm);
   if (e != cudaSuccess) return e;
@@ -47,12 +47,12 @@ cudaError_t go_pairs_batch(const PairSim* sims, int nsims, int parity, int ctas_
 
 }  // namespace
 
-cudaError_t launch_pairs_batch(int kind, bool walls, const PairSim* sims, int nsims, int parity, int ctas_per_sm,
+cudaError_t launch_pairs_batch(int kind, const PairSim* sims, int nsims, int parity, int ctas_per_sm,
                                cudaStream_t st, int device, int64_t total_units, int* counters) {
-#define LB_PBATCH(T, W) go_pairs_batch<T, W>(sims, nsims, parity, ctas_per_sm, st, device, total_units, counters)
-  if (kind == kStoreF16) return walls ? LB_PBATCH(__half, true) : LB_PBATCH(__half, false);
-  if (kind == kStoreI16) return walls ? LB_PBATCH(int16_t, true) : LB_PBATCH(int16_t, false);
-  return walls ? LB_PBATCH(float, true) : LB_PBATCH(float, false);
+#define LB_PBATCH(T) go_pairs_batch<T>(sims, nsims, parity, ctas_per_sm, st, device, total_units, counters)
+  if (kind == kStoreF16) return LB_PBATCH(__half);
+  if (kind == kStoreI16) return LB_PBATCH(int16_t);
+  return LB_PBATCH(float);
 #undef LB_PBATCH
 }
 

@@ -55,14 +55,14 @@ cudaError_t launch_fused_single_i16(int c, bool w, bool mom, const StepBuffers& 
   return w ? go_single<int16_t, 1, true, 8>(b, F, st, device) : go_single<int16_t, 1, false, 8>(b, F, st, device);
 }
 
-cudaError_t launch_pairs_single_f16(int c, bool w, bool mom, const StepBuffers& b, const FusedParams& F,
-                                    cudaStream_t st, int device) {
-  return launch_pairs<__half>(c, w, mom, b, F, st, device);
+cudaError_t launch_pairs_single_f16(int c, bool mom, const StepBuffers& b, const FusedParams& F, cudaStream_t st,
+                                    int device) {
+  return launch_pairs<__half>(c, mom, b, F, st, device);
 }
 
-cudaError_t launch_pairs_single_i16(int c, bool w, bool mom, const StepBuffers& b, const FusedParams& F,
-                                    cudaStream_t st, int device) {
-  return launch_pairs<int16_t>(c, w, mom, b, F, st, device);
+cudaError_t launch_pairs_single_i16(int c, bool mom, const StepBuffers& b, const FusedParams& F, cudaStream_t st,
+                                    int device) {
+  return launch_pairs<int16_t>(c, mom, b, F, st, device);
 }
 
 }  // namespace lbk

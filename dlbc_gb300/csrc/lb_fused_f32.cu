@@ -43,9 +43,9 @@ cudaError_t launch_fused_single_f32(int c, bool w, bool mom, const StepBuffers& 
   return w ? go_single<float, 1, true, 8>(b, F, st, device) : go_single<float, 1, false, 8>(b, F, st, device);
 }
 
-cudaError_t launch_pairs_single_f32(int c, bool w, bool mom, const StepBuffers& b, const FusedParams& F,
-                                    cudaStream_t st, int device) {
-  return launch_pairs<float>(c, w, mom, b, F, st, device);
+cudaError_t launch_pairs_single_f32(int c, bool mom, const StepBuffers& b, const FusedParams& F, cudaStream_t st,
+                                    int device) {
+  return launch_pairs<float>(c, mom, b, F, st, device);
 }
 
 }  // namespace lbk

@@ -49,14 +49,15 @@ cudaError_t launch_fused_single_f16(int c, bool walls, bool mom, const StepBuffe
                                     cudaStream_t st, int device);
 cudaError_t launch_fused_single_i16(int c, bool walls, bool mom, const StepBuffers& b, const FusedParams& F,
                                     cudaStream_t st, int device);
-// The single-lattice pair step (lb_pairs.cuh): F holds the 8 x 64 pair
-// tiling; mom: every tau = 1 (the gathered populations are not kept).
-cudaError_t launch_pairs_single_f32(int c, bool walls, bool mom, const StepBuffers& b, const FusedParams& F,
-                                    cudaStream_t st, int device);
-cudaError_t launch_pairs_single_f16(int c, bool walls, bool mom, const StepBuffers& b, const FusedParams& F,
-                                    cudaStream_t st, int device);
-cudaError_t launch_pairs_single_i16(int c, bool walls, bool mom, const StepBuffers& b, const FusedParams& F,
-                                    cudaStream_t st, int device);
+// The single-lattice pair step (lb_pairs.cuh), lattices without solid
+// sites: F holds the 8 x 64 pair tiling; mom: every tau = 1 (the gathered
+// populations are not kept).
+cudaError_t launch_pairs_single_f32(int c, bool mom, const StepBuffers& b, const FusedParams& F, cudaStream_t st,
+                                    int device);
+cudaError_t launch_pairs_single_f16(int c, bool mom, const StepBuffers& b, const FusedParams& F, cudaStream_t st,
+                                    int device);
+cudaError_t launch_pairs_single_i16(int c, bool mom, const StepBuffers& b, const FusedParams& F, cudaStream_t st,
+                                    int device);
 // The single-lattice D2Q9 step (lb_fused2d.cuh), F from make_fused_params
 // with q = 9; kind kStoreF32 or kStoreF16.
 cudaError_t launch_fused2d(int kind, int c, bool walls, bool mom, const StepBuffers& b, const FusedParams& F,

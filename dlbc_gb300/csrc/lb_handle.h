@@ -30,7 +30,6 @@ struct lbgpu_handle {
   uint8_t* mask = nullptr;
   uint32_t* nbmask = nullptr;       // neighbour masks for the fused step (walls only)
   uint8_t* tile_walls = nullptr;    // per (x, 8x32 tile) wall flags for the fused step
-  uint8_t* row_walls = nullptr;     // per (x, y, 64-site z segment) wall flags for the pair step
   int* work_counter = nullptr;      // the fused step's dynamic scheduling counter
   void* rho = nullptr;
   void* psi = nullptr;

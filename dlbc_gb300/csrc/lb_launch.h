@@ -29,7 +29,6 @@ struct StepBuffers {
   const uint8_t* mask;  // nullptr: no walls
   const uint32_t* nbmask = nullptr;  // neighbour masks (fused step; set iff mask is)
   const uint8_t* tile_walls = nullptr;  // per (x, 8x32 tile) wall flags (fused step)
-  const uint8_t* row_walls = nullptr;   // per (x, y, 64-site z segment) wall flags (pair step)
   int* work_counter = nullptr;          // dynamic scheduling counter (fused step)
   void* rho;            // C*N (double for FP64, float otherwise)
   void* psi;            // C*N
@@ -103,9 +102,9 @@ FusedParams make_fused_params(const StepParams& P, int ty, int q = 19);
 cudaError_t launch_fused_batch(int kind, int ty, bool walls, const FusedSim* sims, int nsims,
                                int64_t total_work, int parity, int ctas_per_sm, cudaStream_t stream, int device,
                                int64_t total_units, int* counters);
-// The pair-kernel batch (lb_pairs.cuh): members with an even z extent and the
-// BDist2 equilibrium; counters as above (required).
-cudaError_t launch_pairs_batch(int kind, bool walls, const PairSim* sims, int nsims, int parity, int ctas_per_sm,
+// The pair-kernel batch (lb_pairs.cuh): members with an even z extent, the
+// BDist2 equilibrium and no solid site; counters as above (required).
+cudaError_t launch_pairs_batch(int kind, const PairSim* sims, int nsims, int parity, int ctas_per_sm,
                                cudaStream_t stream, int device, int64_t total_units, int* counters);
 
 }  // namespace lbk

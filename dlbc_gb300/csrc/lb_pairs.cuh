@@ -39,17 +39,11 @@
 // equilibrium goes straight to h space, h_eq = (rho / scale) g_q(u) -
 // rho0 / scale (the weight cancels).
 //
-// Walls: per (x, y, 64-site row segment) a flag says whether any site of
-// the segment has a solid neighbour or is solid; only flagged rows read the
-// 32-bit neighbour masks (bit 0: solid; bit q: x + c_q solid) and fix up
-// bounce-back (a fluid site whose upstream x - c_q is solid takes its own
-// population of the opposite direction), the stencil's wall substitution
-// (a solid neighbour contributes the site's own psi, force.d:273) and the
-// wall force (gwc, force.d:285-303).  Solid sites are neither collided nor
-// written.
-//
-// Requirements: nz even (aligned words), BDist2 equilibrium; the launcher
-// falls back to the one-site-per-thread kernel (lb_fused.cuh) otherwise.
+// Requirements: nz even (aligned words), the BDist2 equilibrium and no solid
+// site; the launcher runs the one-site-per-thread kernel (lb_fused.cuh)
+// otherwise.  (Walled rows with per-site bounce-back addresses were slower
+// here than the one-site kernel's wall code: a word covers two sites whose
+// sources differ next to a wall.)
 //
 // The arithmetic restates the reference (advectFieldsKernel
 // advection.d:61-89, psi force.d:320-333, addShanChenForcePsi
@@ -112,10 +106,6 @@ struct PairIO<float> {
   static constexpr int kLeftEdge = 0;
   __device__ static __forceinline__ W ld(const float* p) { return __ldg(reinterpret_cast<const float2*>(p)); }
   __device__ static __forceinline__ float ld1(const float* p) { return __ldg(p); }
-  // one site's stored value, and a word from two of them
-  using R = float;
-  __device__ static __forceinline__ R ldraw(const float* p) { return __ldg(p); }
-  __device__ static __forceinline__ W pack(R lo, R hi) { return make_float2(lo, hi); }
   // (f(z-1), f(z)) from the pair (f(z), f(z+1)): the lane below's upper site,
   // or at the warp's left edge one load at edge_p (the site z0 - 1)
   __device__ static __forceinline__ W up(W w, bool lane0, const float* edge_p) {
@@ -133,11 +123,6 @@ struct PairIO<float> {
   __device__ static __forceinline__ float2 val(W w) { return w; }
   __device__ static __forceinline__ W enc(float2 v) { return v; }
   __device__ static __forceinline__ void st(float* p, W w) { *reinterpret_cast<float2*>(p) = w; }
-  __device__ static __forceinline__ void st1(float* p, float v) { *p = v; }
-  // per-site select: a where take, else b
-  __device__ static __forceinline__ W sel(W b, W a, bool take0, bool take1) {
-    return make_float2(take0 ? a.x : b.x, take1 ? a.y : b.y);
-  }
 };
 
 // The 16-bit storages share their word handling: site z in the low half,
@@ -150,9 +135,6 @@ struct PairIO16 {
   static constexpr bool kOffsets = true;
   static constexpr int kLeftEdge = -1;
   __device__ static __forceinline__ W ld(const T* p) { return __ldg(reinterpret_cast<const unsigned int*>(p)); }
-  using R = unsigned short;
-  __device__ static __forceinline__ R ldraw(const T* p) { return __ldg(reinterpret_cast<const unsigned short*>(p)); }
-  __device__ static __forceinline__ W pack(R lo, R hi) { return uint32_t(lo) | (uint32_t(hi) << 16); }
   __device__ static __forceinline__ W up(W w, bool lane0, const T* edge_p) {
     W prev = __shfl_up_sync(0xffffffffu, w, 1);
     if (lane0) prev = __ldg(reinterpret_cast<const unsigned int*>(edge_p));
@@ -164,10 +146,6 @@ struct PairIO16 {
     return __byte_perm(w, next, 0x5432);  // (w.hi, next.lo)
   }
   __device__ static __forceinline__ void st(T* p, W w) { *reinterpret_cast<unsigned int*>(p) = w; }
-  __device__ static __forceinline__ W sel(W b, W a, bool take0, bool take1) {
-    const uint32_t m = (take0 ? 0x0000ffffu : 0u) | (take1 ? 0xffff0000u : 0u);
-    return (a & m) | (b & ~m);
-  }
 };
 
 template <>
@@ -182,7 +160,6 @@ struct PairIO<__half> : PairIO16<__half> {
     const __half2 h = __float22half2_rn(v);
     return *reinterpret_cast<const W*>(&h);
   }
-  __device__ static __forceinline__ void st1(__half* p, float v) { *p = __float2half_rn(v); }
 };
 
 // 16-bit fixed point (the I16 form): h rounded to nearest, saturated to
@@ -203,7 +180,6 @@ struct PairIO<int16_t> : PairIO16<int16_t> {
     return make_float2(float(int16_t(w & 0xffffu)), float(int16_t(w >> 16)));
   }
   __device__ static __forceinline__ W enc(float2 v) { return pack_s16x2(v.x, v.y); }
-  __device__ static __forceinline__ void st1(int16_t* p, float v) { *p = int16_t(pack_s16x2(v, 0.f) & 0xffffu); }
 };
 
 // ---------------------------------------------------------------------------
@@ -249,12 +225,11 @@ __device__ __forceinline__ float pair_psi(float rho, int psi_form) { return psi_
 // ---------------------------------------------------------------------------
 // Shared memory and equilibrium constants
 // ---------------------------------------------------------------------------
-template <int C, bool WALLS, bool MOM, typename T>
+template <int C, bool MOM, typename T>
 struct PairShared {
   // four plane slots: the ring warps gather the z-ring of plane x + 2 while
   // the row warps collide plane x with the slots of x - 1, x, x + 1
   float psi[4][C][kPairTY + 2][kPairRZ];
-  float rho[WALLS ? 4 : 1][C][kPairTY + 2][WALLS ? kPairRZ : 1];  // the wall force reads solid neighbours' density
   // tau != 1: the row warps' gathered words of the next plane, [buffer][c][q][row][lane]
   typename PairIO<T>::W pops[MOM ? 1 : 2][C][MOM ? 1 : 19][MOM ? 1 : kPairTY][32];
   // tau = 1: the row warps' density and momentum of the next plane,
@@ -296,11 +271,10 @@ __device__ __forceinline__ PairEq pair_eq_constants(float2 rho, float2 cst, floa
 
 // Process plane-tiles [w0, w1) of one lattice (tile-major: w = tile*nx + x).
 // Every thread of the CTA calls this with the same range.
-template <typename T, int C, bool WALLS, bool MOM>
+template <typename T, int C, bool MOM>
 __device__ __forceinline__ void pair_body(const FusedParams& P, const T* __restrict__ f, T* __restrict__ fout,
-                                          const uint32_t* __restrict__ nbmask, const uint8_t* __restrict__ row_walls,
                                           double* __restrict__ force_out, int64_t w0, int64_t w1,
-                                          PairShared<C, WALLS, MOM, T>& sh) {
+                                          PairShared<C, MOM, T>& sh) {
   using IO = PairIO<T>;
   using W = typename IO::W;
   constexpr bool OFF = IO::kOffsets;
@@ -314,8 +288,6 @@ __device__ __forceinline__ void pair_body(const FusedParams& P, const T* __restr
     fo[c] = fout + size_t(c) * 19 * size_t(P.n);
   }
   const bool unit = MOM || P.unit_tau != 0;
-  // wall force: solid sites' own densities are needed
-  const bool need_solid = WALLS && (P.gwc[0] != 0.f || (C > 1 && P.gwc[1] != 0.f));
   float s36[C];
 #pragma unroll
   for (int c = 0; c < C; ++c) s36[c] = P.scale[c] * (1.0f / 36.0f);
@@ -327,7 +299,6 @@ __device__ __forceinline__ void pair_body(const FusedParams& P, const T* __restr
     const int run = int(min(w1 - w, int64_t(P.nx - xs)));
     const int y0 = (tile / P.tiles_z) * kPairTY, z0 = (tile % P.tiles_z) * kPairTZ;
     const int tyv = min(kPairTY, P.ny - y0), tzv = min(kPairTZ, P.nz - z0);
-    const int ztile = tile % P.tiles_z;
     // this warp's gathered row: r (shared row index) and y; ring warps take
     // rows 0 and tyv + 1
     const bool ring_warp = warp >= kPairTY;
@@ -343,10 +314,6 @@ __device__ __forceinline__ void pair_body(const FusedParams& P, const T* __restr
     const int zleft = z0 > 0 ? z0 - 1 : P.nz - 1;
     const int zright = z0 + tzv < P.nz ? z0 + tzv : 0;
     const int dl = zleft + IO::kLeftEdge - zl, dr = zright - zl;
-    // walled rows' per-site loads: source z - c_z of the sites zl and zl + 1
-    // relative to zl, indexed by 1 - c_z (periodic)
-    const uint32_t zd0[3] = {uint32_t(zl > 0 ? -1 : P.nz - 1), 0u, 1u};
-    const uint32_t zd1[3] = {0u, 1u, uint32_t(zl + 2 < P.nz ? 2 : 2 - P.nz)};
     const uint32_t r3[3] = {uint32_t(wrap(y - 1, P.ny)) * uint32_t(P.nz) + uint32_t(zl),
                             uint32_t(y) * uint32_t(P.nz) + uint32_t(zl),
                             uint32_t(wrap(y + 1, P.ny)) * uint32_t(P.nz) + uint32_t(zl)};
@@ -364,11 +331,9 @@ __device__ __forceinline__ void pair_body(const FusedParams& P, const T* __restr
     zrs[1] = zr;
     zrs[2] = zr + 1 < P.nz ? zr + 1 : 0;
 
-    // moments, psi and neighbour masks of the plane the row warp collides
-    // next (cur) and of the plane it gathers (nxt)
+    // moments of the plane the row warp collides next (cur) and of the plane
+    // it gathers (nxt)
     PairMom<float2> m_cur[C], m_nxt[C];
-    uint2 nb_cur = make_uint2(0u, 0u), nb_nxt = make_uint2(0u, 0u);
-    bool wr_cur = false, wr_nxt = false;
 
     // gather the warp's row of plane xg into psi slot ps (and, for the row
     // warps, the moments/words for its collision: keep >= 0 selects the
@@ -377,16 +342,6 @@ __device__ __forceinline__ void pair_body(const FusedParams& P, const T* __restr
       const uint32_t p3[3] = {uint32_t(wrap(xg - 1, P.nx)) * plane_sz, uint32_t(xg) * plane_sz,
                               uint32_t(wrap(xg + 1, P.nx)) * plane_sz};
       if (!row_on) return;
-      const uint32_t own = p3[1] + r3[1];
-      bool walled = false;
-      uint2 nb = make_uint2(0u, 0u);
-      // (a batch runs its wall-free members in the walled kernel too: no
-      // flags, no masks)
-      if (WALLS && row_walls) {
-        walled = __ldg(row_walls + (size_t(xg) * P.ny + size_t(y)) * P.tiles_z + ztile) != 0;
-        if (walled && active) nb = __ldg(reinterpret_cast<const uint2*>(nbmask + own));
-      }
-      const bool solid0 = nb.x & 1u, solid1 = nb.y & 1u;
       PairMom<float2> m[C];
       float2 ps2[C];
 #pragma unroll
@@ -396,37 +351,15 @@ __device__ __forceinline__ void pair_body(const FusedParams& P, const T* __restr
         for (int q = 0; q < 19; ++q) {
           const int cx = Conn<19>::cx(q), cy = Conn<19>::cy(q), cz = Conn<19>::cz(q);
           const uint32_t off = p3[1 - cx] + r3[1 - cy] + P.qn[q];
-          W word;
-          if (WALLS && walled) {
-            // rows next to a wall: one load per site, its address chosen
-            // per site without branches (bounce-back: x - c_q = x + c_b
-            // solid and the site fluid, the site's own population b; a solid
-            // site its own population, whose density the wall force reads)
-            uint32_t o0 = off + zd0[1 - cz], o1 = off + zd1[1 - cz];
-            if (q > 0) {
-              const int b = Conn<19>::bounce(q);
-              if (((nb.x >> b) & 1u) && !solid0) o0 = own + P.qn[b];
-              if (((nb.y >> b) & 1u) && !solid1) o1 = own + 1u + P.qn[b];
-            }
-            if (need_solid) {
-              if (solid0) o0 = own + P.qn[q];
-              if (solid1) o1 = own + 1u + P.qn[q];
-            }
-            word = IO::pack(IO::ldraw(fc[c] + o0), IO::ldraw(fc[c] + o1));
-          } else {
-            word = IO::ld(fc[c] + off);
-            if (cz == 1) word = IO::up(word, lane0, fc[c] + (off + uint32_t(dl)));
-            if (cz == -1) word = IO::down(word, lastl, fc[c] + (off + uint32_t(dr)));
-          }
+          W word = IO::ld(fc[c] + off);
+          if (cz == 1) word = IO::up(word, lane0, fc[c] + (off + uint32_t(dl)));
+          if (cz == -1) word = IO::down(word, lastl, fc[c] + (off + uint32_t(dr)));
           if (!MOM && keep >= 0 && !ring_warp) sh.pops[keep][c][q][warp][lane] = word;
           v[q] = IO::val(word);
         }
         m[c] = pair_moments<OFF>(v, s36[c], P.rho0[c]);
         ps2[c] = make_float2(pair_psi(m[c].rho.x, P.psi_form), pair_psi(m[c].rho.y, P.psi_form));
-        if (active) {
-          *reinterpret_cast<float2*>(&sh.psi[ps][c][r][2 + 2 * lane]) = ps2[c];
-          if (WALLS) *reinterpret_cast<float2*>(&sh.rho[ps][c][r][2 + 2 * lane]) = m[c].rho;
-        }
+        if (active) *reinterpret_cast<float2*>(&sh.psi[ps][c][r][2 + 2 * lane]) = ps2[c];
         // one component's loads in flight at a time: the next component's
         // loads are not hoisted above this point, which bounds the live
         // registers (two components' 38 words would spill)
@@ -443,8 +376,6 @@ __device__ __forceinline__ void pair_body(const FusedParams& P, const T* __restr
             m_nxt[c] = m[c];
           }
         }
-        nb_nxt = nb;
-        wr_nxt = walled;
       }
     };
     // the ring warps' scalar sites of plane xg (z0 - 1 and z0 + tzv of each
@@ -453,28 +384,17 @@ __device__ __forceinline__ void pair_body(const FusedParams& P, const T* __restr
       if (!has_zring) return;
       const uint32_t p3[3] = {uint32_t(wrap(xg - 1, P.nx)) * plane_sz, uint32_t(xg) * plane_sz,
                               uint32_t(wrap(xg + 1, P.nx)) * plane_sz};
-      const uint32_t own = p3[1] + uint32_t(yr) * uint32_t(P.nz) + uint32_t(zr);
-      uint32_t nbs = 0u;
-      if (WALLS && nbmask) nbs = __ldg(nbmask + own);
-      const bool solid = nbs & 1u;
 #pragma unroll
       for (int c = 0; c < C; ++c) {
         float v[19];
 #pragma unroll
         for (int q = 0; q < 19; ++q) {
           const int cx = Conn<19>::cx(q), cy = Conn<19>::cy(q), cz = Conn<19>::cz(q);
-          const int b = Conn<19>::bounce(q);
-          uint32_t off = p3[1 - cx] + uint32_t(yrs[1 - cy]) * uint32_t(P.nz) + uint32_t(zrs[1 - cz]) + P.qn[q];
-          if (WALLS) {
-            const bool bb = q > 0 && ((nbs >> b) & 1u) && !solid;
-            if (bb) off = own + P.qn[b];
-            if (solid && need_solid) off = own + P.qn[q];
-          }
+          const uint32_t off = p3[1 - cx] + uint32_t(yrs[1 - cy]) * uint32_t(P.nz) + uint32_t(zrs[1 - cz]) + P.qn[q];
           v[q] = IO::ld1(fc[c] + off);
         }
         const PairMom<float> m = pair_moments<OFF>(v, s36[c], P.rho0[c]);
         sh.psi[ps][c][lane][zr_i] = pair_psi(m.rho, P.psi_form);
-        if (WALLS) sh.rho[ps][c][lane][zr_i] = m.rho;
       }
     };
 
@@ -494,8 +414,6 @@ __device__ __forceinline__ void pair_body(const FusedParams& P, const T* __restr
 #pragma unroll
         for (int c = 0; c < C; ++c) m_cur[c] = m_nxt[c];
       }
-      nb_cur = nb_nxt;
-      wr_cur = wr_nxt;
       __syncthreads();  // psi slot sp (plane x - 3) and words buffer 1 - cur are free
       gather_rows(sp, wrap(x + 1, P.nx), 1 - cur);
       __syncthreads();
@@ -517,10 +435,6 @@ __device__ __forceinline__ void pair_body(const FusedParams& P, const T* __restr
           }
         }
         const int slot[3] = {sm, s0, sp};  // by c_x + 1
-        const bool walled = WALLS && wr_cur;
-        uint32_t any = 0u;
-        if (walled) any = __reduce_or_sync(__activemask(), nb_cur.x | nb_cur.y);
-        const bool solid0 = WALLS && (nb_cur.x & 1u), solid1 = WALLS && (nb_cur.y & 1u);
         // psi of this lane's own sites (written by its own gather of plane x)
         auto psi_own = [&](int c) { return *reinterpret_cast<const float2*>(&sh.psi[s0][c][r][zi]); };
         // --- Shan-Chen: S_c = sum_q w_q psi_c(x + c_q) c_q
@@ -537,9 +451,7 @@ __device__ __forceinline__ void pair_body(const FusedParams& P, const T* __restr
             };
             auto Lv = [&](int dx, int dy) { return sh.psi[slot[dx + 1]][c][r + dy][zi - 1]; };
             auto Rv = [&](int dx, int dy) { return sh.psi[slot[dx + 1]][c][r + dy][zi + 2]; };
-            const float2 own_psi = walled ? psi_own(c) : make_float2(0.f, 0.f);
-            // psi_c(x + c_q) at both sites, a solid neighbour replaced by the
-            // site's own psi (per lane, without branches)
+            // psi_c(x + c_q) at both sites
             auto nbv = [&](int q) -> float2 {
               const int cx = Conn<19>::cx(q), cy = Conn<19>::cy(q), cz = Conn<19>::cz(q);
               float2 v;
@@ -551,10 +463,6 @@ __device__ __forceinline__ void pair_body(const FusedParams& P, const T* __restr
               } else {
                 const float2 m = M(cx, cy);
                 v = make_float2(Lv(cx, cy), m.x);
-              }
-              if (walled) {
-                v.x = ((nb_cur.x >> q) & 1u) ? own_psi.x : v.x;
-                v.y = ((nb_cur.y >> q) & 1u) ? own_psi.y : v.y;
               }
               return v;
             };
@@ -585,31 +493,6 @@ __device__ __forceinline__ void pair_body(const FusedParams& P, const T* __restr
             const float2 mp = make_float2(-own_psi.x, -own_psi.y);
 #pragma unroll
             for (int vd = 0; vd < 3; ++vd) F[f1][vd] = vmul(mp, g[vd]);
-            if (walled && P.gwc[f1] != 0.f && any != 0u) {
-              // wall force: -psi_c(x) gwc_c sum_q w_q rho_c(x + c_q) c_q over solid x + c_q
-              float2 a[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
-              float2 d[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
-#pragma unroll
-              for (int q = 1; q < 19; ++q) {
-                if (!((any >> q) & 1u)) continue;
-                const int cx = Conn<19>::cx(q), cy = Conn<19>::cy(q), cz = Conn<19>::cz(q);
-                const float* row = sh.rho[slot[cx + 1]][f1][r + cy];
-                float2 v = make_float2(((nb_cur.x >> q) & 1u) ? row[zi + cz] : 0.f,
-                                       ((nb_cur.y >> q) & 1u) ? row[zi + 1 + cz] : 0.f);
-                float2* acc = Conn<19>::wclass(q) == 1 ? a : d;
-                if (cx > 0) acc[0] = vadd(acc[0], v);
-                if (cx < 0) acc[0] = vsub(acc[0], v);
-                if (cy > 0) acc[1] = vadd(acc[1], v);
-                if (cy < 0) acc[1] = vsub(acc[1], v);
-                if (cz > 0) acc[2] = vadd(acc[2], v);
-                if (cz < 0) acc[2] = vsub(acc[2], v);
-              }
-              const float2 wc = vmul(own_psi, splat<float2>(P.gwc[f1]));
-#pragma unroll
-              for (int vd = 0; vd < 3; ++vd)
-                F[f1][vd] = vsub(F[f1][vd],
-                                 vmul(wc, vmul(splat<float2>(1.0f / 36.0f), vfma(splat<float2>(2.f), a[vd], d[vd]))));
-            }
           }
         }
         float2 tot = m_cur[0].rho;
@@ -617,19 +500,13 @@ __device__ __forceinline__ void pair_body(const FusedParams& P, const T* __restr
 #pragma unroll
         for (int c = 0; c < C; ++c) {
           // distributeForce with no distributed force: only its NaN cases
-          // matter; solid sites carry no force
+          // matter
           const bool bad0 = tot.x == 0.f || isnan(tot.x) || isinf(m_cur[c].rho.x) || isnan(m_cur[c].rho.x);
           const bool bad1 = tot.y == 0.f || isnan(tot.y) || isinf(m_cur[c].rho.y) || isnan(m_cur[c].rho.y);
 #pragma unroll
           for (int vd = 0; vd < 3; ++vd) {
-            if (bad0)
-              F[c][vd].x = NAN;
-            else if (solid0)
-              F[c][vd].x = 0.f;
-            if (bad1)
-              F[c][vd].y = NAN;
-            else if (solid1)
-              F[c][vd].y = 0.f;
+            if (bad0) F[c][vd].x = NAN;
+            if (bad1) F[c][vd].y = NAN;
           }
         }
         if (P.record_force) {
@@ -659,8 +536,7 @@ __device__ __forceinline__ void pair_body(const FusedParams& P, const T* __restr
           }
         }
         // --- collision: equilibrium (and relaxation) of every population,
-        // one word store per population; solid sites are not written
-        const bool store_pair = !(solid0 || solid1);
+        // one word store per population
 #pragma unroll
         for (int c = 0; c < C; ++c) {
           const float2 rd = make_float2(__frcp_rn(m_cur[c].rho.x), __frcp_rn(m_cur[c].rho.y));
@@ -679,15 +555,7 @@ __device__ __forceinline__ void pair_body(const FusedParams& P, const T* __restr
           const float2 omo = splat<float2>(P.one_minus_omega[c]);
           auto put = [&](int q, float2 val) {
             if (!unit) val = vfma(IO::val(sh.pops[cur][c][q][warp][lane]), omo, val);
-            const W word = IO::enc(val);
-            T* p = fo[c] + (P.qn[q] + own);
-            if (store_pair) {
-              IO::st(p, word);
-            } else {
-              const float2 v2 = IO::val(word);
-              if (!solid0) IO::st1(p, v2.x);
-              if (!solid1) IO::st1(p + 1, v2.y);
-            }
+            IO::st(fo[c] + (P.qn[q] + own), IO::enc(val));
           };
           auto pair = [&](float2 cu, int axis, int ip, int im) {
             const float2 cu2 = vmul(cu, cu);
@@ -730,12 +598,11 @@ __device__ __forceinline__ void pair_body(const FusedParams& P, const T* __restr
 // one tile from the counter, x-chunk-major (neighbouring tiles march over
 // the same planes together and share their ring rows through L2), over the
 // planes [x_begin, x_end) of every tile.
-template <typename T, int C, bool WALLS, bool MOM>
+template <typename T, int C, bool MOM>
 __global__ void __launch_bounds__(kPairThreads, (MOM || sizeof(T) == 2) ? LB_PAIRS_MINB : 1)
-    k_pairs(const T* __restrict__ f, T* __restrict__ fout, const uint32_t* __restrict__ nbmask,
-            const uint8_t* __restrict__ row_walls, double* __restrict__ force_out, FusedParams P) {
+    k_pairs(const T* __restrict__ f, T* __restrict__ fout, double* __restrict__ force_out, FusedParams P) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  auto& sh = *reinterpret_cast<PairShared<C, WALLS, MOM, T>*>(smem_raw);
+  auto& sh = *reinterpret_cast<PairShared<C, MOM, T>*>(smem_raw);
   __shared__ int s_item;
   const int ntl = P.tiles_y * P.tiles_z;
   const int units = sched_units(P, ntl);
@@ -748,7 +615,7 @@ __global__ void __launch_bounds__(kPairThreads, (MOM || sizeof(T) == 2) ? LB_PAI
     int tile, x0, x1;
     sched_run(P, ntl, item, tile, x0, x1);
     const int64_t w0 = int64_t(tile) * P.nx + x0;
-    pair_body<T, C, WALLS, MOM>(P, f, fout, nbmask, row_walls, force_out, w0, w0 + (x1 - x0), sh);
+    pair_body<T, C, MOM>(P, f, fout, force_out, w0, w0 + (x1 - x0), sh);
   }
 }
 
@@ -757,8 +624,6 @@ __global__ void __launch_bounds__(kPairThreads, (MOM || sizeof(T) == 2) ? LB_PAI
 struct PairSim {
   FusedParams P;           // pair tiling (8 x 64), run_len set
   const void* f[2];
-  const uint32_t* nbmask;  // neighbour masks; nullptr: no solid site
-  const uint8_t* row_walls;
   double* force_out;       // nullptr unless recording
   int64_t unit_begin;      // first run of this simulation in the batch
   int32_t phase;
@@ -771,7 +636,7 @@ struct PairSim {
 // counter for the next launch.  Each member runs pair_body with its own
 // parameters (staged in shared memory), so it computes exactly what its
 // lone lattice computes.
-template <typename T, bool WALLS>
+template <typename T>
 __global__ void __launch_bounds__(kPairThreads, 2)
     k_pairs_batch(const PairSim* __restrict__ sims, int nsims, int parity, int64_t total_units,
                   int* __restrict__ counters) {
@@ -821,21 +686,21 @@ __global__ void __launch_bounds__(kPairThreads, 2)
     const long long r0 = s_w[0], r1 = s_w[1];
     __syncthreads();
     if (Ps.unit_tau)
-      pair_body<T, 2, WALLS, true>(Ps, fin, fout, sims[i].nbmask, sims[i].row_walls, sims[i].force_out, r0, r1,
-                                   *reinterpret_cast<PairShared<2, WALLS, true, T>*>(smem_raw));
+      pair_body<T, 2, true>(Ps, fin, fout, sims[i].force_out, r0, r1,
+                            *reinterpret_cast<PairShared<2, true, T>*>(smem_raw));
     else
-      pair_body<T, 2, WALLS, false>(Ps, fin, fout, sims[i].nbmask, sims[i].row_walls, sims[i].force_out, r0, r1,
-                                    *reinterpret_cast<PairShared<2, WALLS, false, T>*>(smem_raw));
+      pair_body<T, 2, false>(Ps, fin, fout, sims[i].force_out, r0, r1,
+                             *reinterpret_cast<PairShared<2, false, T>*>(smem_raw));
   }
 }
 
 // Host side: one persistent launch of k_pairs (F holds the pair tiling, the
 // plane range and the zeroed work counter).
-template <typename T, int C, bool W, bool MOM>
+template <typename T, int C, bool MOM>
 cudaError_t go_pairs(const StepBuffers& b, const FusedParams& F, cudaStream_t st, int device) {
   static KernelInfo info;
-  auto kern = k_pairs<T, C, W, MOM>;
-  const int smem = int(sizeof(PairShared<C, W, MOM, T>));
+  auto kern = k_pairs<T, C, MOM>;
+  const int smem = int(sizeof(PairShared<C, MOM, T>));
   int per_sm = 0;
   cudaError_t e = kernel_setup(kern, smem, kPairThreads, device, info, &per_sm);
   if (e != cudaSuccess) return e;
@@ -845,20 +710,15 @@ cudaError_t go_pairs(const StepBuffers& b, const FusedParams& F, cudaStream_t st
   plan_runs(G, tiles, grid);
   const int64_t units = sched_units(G, int(tiles));
   if (grid > units) grid = units;
-  kern<<<unsigned(grid), kPairThreads, smem, st>>>(static_cast<const T*>(b.f), static_cast<T*>(b.fout), b.nbmask,
-                                                   b.row_walls, b.force, G);
+  kern<<<unsigned(grid), kPairThreads, smem, st>>>(static_cast<const T*>(b.f), static_cast<T*>(b.fout), b.force, G);
   return cudaGetLastError();
 }
 
 template <typename T>
-cudaError_t launch_pairs(int c, bool w, bool mom, const StepBuffers& b, const FusedParams& F, cudaStream_t st,
-                         int device) {
-  if (c == 2) {
-    if (mom) return w ? go_pairs<T, 2, true, true>(b, F, st, device) : go_pairs<T, 2, false, true>(b, F, st, device);
-    return w ? go_pairs<T, 2, true, false>(b, F, st, device) : go_pairs<T, 2, false, false>(b, F, st, device);
-  }
-  if (mom) return w ? go_pairs<T, 1, true, true>(b, F, st, device) : go_pairs<T, 1, false, true>(b, F, st, device);
-  return w ? go_pairs<T, 1, true, false>(b, F, st, device) : go_pairs<T, 1, false, false>(b, F, st, device);
+cudaError_t launch_pairs(int c, bool mom, const StepBuffers& b, const FusedParams& F, cudaStream_t st, int device) {
+  if (b.mask) return cudaErrorInvalidValue;  // solid sites: the one-site kernel
+  if (c == 2) return mom ? go_pairs<T, 2, true>(b, F, st, device) : go_pairs<T, 2, false>(b, F, st, device);
+  return mom ? go_pairs<T, 1, true>(b, F, st, device) : go_pairs<T, 1, false>(b, F, st, device);
 }
 
 }  // namespace lbk

@@ -1,16 +1,16 @@
 """The pair kernel (two z-adjacent sites per thread, lb_pairs.cuh): the
-fused single-pass step of the I16 form, and of the FP32 and FP16 forms for
-lattices with an even z extent, the BDist2 equilibrium, every tau = 1 and
-no wall (elsewhere FP32 and FP16 run the one-site-per-thread kernel, which
-the same tests cover).
+fused single-pass step of lattices without solid sites, with an even z
+extent and the BDist2 equilibrium, in the I16 form and, with every tau = 1,
+the FP32 and FP16 forms.  Elsewhere the one-site-per-thread kernel
+(lb_fused.cuh) runs, which the same tests cover (the walled cases).
 
 * Against the two-kernel float step (LBGPU_TWO_KERNEL=1, a different
   kernel with the reference's per-site operation order): populations within
   the tolerances of the fused-versus-two-kernel test (2e-6 of the largest
   population in FP32, 2e-3 in FP16), forces within 3e-7 / 3e-4, over tile
   edges in y and z, partial tiles, tiny extents, walls with the wall force,
-  tau != 1 and one component.  I16, which runs on the pair kernel only
-  (walls and tau != 1 included), against FP32 within the FP16 tolerances.
+  tau != 1 and one component.  I16 (both kernels, tau != 1 included)
+  against FP32 within the FP16 tolerances.
 * Translation invariance, bit for bit (every form, walls included): a
   lattice shifted periodically by
   (3, 5, 2), by 66 sites along z or by (1, 8, 64) steps to the shifted
@@ -141,10 +141,10 @@ def test_pairs_translation_invariant_bitwise(precision, shift):
 @pytest.mark.parametrize("precision", [lbgpu.FP32, lbgpu.FP16, lbgpu.I16])
 @pytest.mark.parametrize("shift", [(3, 5, 0), (1, 8, 0)])
 def test_pairs_walled_channel_translation_invariant_bitwise(precision, shift):
-    """The same with z walls (shifted along x and y only): rows next to a
-    wall take their populations one site at a time (bounce-back chosen per
-    site), the wall force reads the solid sites' densities, and still every
-    site computes the same bits wherever it sits."""
+    """The same with z walls (shifted along x and y only; the one-site
+    kernel, whose tiles next to a wall run the wall code): bounce-back, the
+    wall force reading the solid sites' densities, and still every site
+    computes the same bits wherever it sits."""
     p = droplet_channel((12, 20, 70), radius=4.0, acc=1e-3, gwc=(0.2, -0.1))
     fl, m = init.init_fields(p)
     a, fa = _run(p, 15, precision, fields=(fl, m), rho0=(0.5, 0.5))
