@@ -17,6 +17,11 @@ struct StepEvents {
 
 // z sites per tile row of the pair step (lb_pairs.cuh): 32 lanes x 2
 constexpr int kPairTZ = 64;
+// rows (y) of a pair-kernel tile
+#ifndef LB_PAIR_TY
+#define LB_PAIR_TY 8
+#endif
+constexpr int kPairTY = LB_PAIR_TY;
 
 // storage of the float-arithmetic forms
 constexpr int kStoreF32 = 0;  // float populations

@@ -63,7 +63,6 @@
 
 namespace lbk {
 
-constexpr int kPairTY = 8;                  // interior rows per tile
 // (kPairTZ = 64 sites per tile row, 32 lanes x 2: lb_launch.h)
 constexpr int kPairRZ = kPairTZ + 4;        // shared row: [1] left ring, [2, 2 + tzv) tile, [2 + tzv] right ring
 constexpr int kPairWarps = kPairTY + 2;     // row warps + the two ring warps
