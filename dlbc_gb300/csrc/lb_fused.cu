@@ -84,7 +84,10 @@ cudaError_t launch_fused_range(int kind, int q, int c, const StepBuffers& b, con
   const bool w = b.mask != nullptr;
   if (w && !b.nbmask) return cudaErrorInvalidValue;
   *launches += 1;
-  if (q == 9) return launch_fused2d(kind, c, w, c == 2 && P.unit_tau && P.eq_form == 2, b, G, st, device);
+  if (q == 9)
+    return pairs2d_eligible(kind, c, P, b) ? launch_pairs2d(kind, b, G, st, device)
+                                           : launch_fused2d(kind, c, w, c == 2 && P.unit_tau && P.eq_form == 2, b, G,
+                                                            st, device);
   if (pairs_eligible(kind, P, b)) {
     G.tiles_y = (P.ny + kPairTY - 1) / kPairTY;
     G.tiles_z = (P.nz + kPairTZ - 1) / kPairTZ;
@@ -118,7 +121,9 @@ cudaError_t launch_fused(int kind, int q, int c, const StepBuffers& b, const Ste
   }
   cudaError_t e;
   if (q == 9) {
-    e = launch_fused2d(kind, c, w, c == 2 && P.unit_tau && P.eq_form == 2, b, F, st, device);
+    e = pairs2d_eligible(kind, c, P, b)
+            ? launch_pairs2d(kind, b, F, st, device)
+            : launch_fused2d(kind, c, w, c == 2 && P.unit_tau && P.eq_form == 2, b, F, st, device);
   } else if (pairs_eligible(kind, P, b)) {
     // two z-adjacent sites per thread (lb_pairs.cuh): 8 x 64 tiles
     FusedParams G = F;

@@ -62,5 +62,9 @@ cudaError_t launch_pairs_single_i16(int c, bool mom, const StepBuffers& b, const
 // with q = 9; kind kStoreF32 or kStoreF16.
 cudaError_t launch_fused2d(int kind, int c, bool walls, bool mom, const StepBuffers& b, const FusedParams& F,
                            cudaStream_t st, int device);
+// The D2Q9 pair step (lb_pairs2d.cuh) and the lattices it runs: FP32/FP16,
+// two components, every tau = 1, BDist2, even ny, no solid site.
+bool pairs2d_eligible(int kind, int c, const StepParams& P, const StepBuffers& b);
+cudaError_t launch_pairs2d(int kind, const StepBuffers& b, const FusedParams& F, cudaStream_t st, int device);
 
 }  // namespace lbk

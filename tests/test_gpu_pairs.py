@@ -117,9 +117,12 @@ def test_i16_close_to_fp32(case):
 
 
 def _shifted(fields, mask, shift):
-    fl = [np.roll(f[2:-2, 2:-2, 2:-2], shift, axis=(0, 1, 2)) for f in fields]
-    m = np.roll(mask[2:-2, 2:-2, 2:-2], shift, axis=(0, 1, 2))
-    pad = lambda a: np.pad(a, [(2, 2)] * 3 + [(0, 0)] * (a.ndim - 3), mode="wrap")  # noqa: E731
+    d = len(shift)
+    sl = (slice(2, -2),) * d
+    axes = tuple(range(d))
+    fl = [np.roll(f[sl], shift, axis=axes) for f in fields]
+    m = np.roll(mask[sl], shift, axis=axes)
+    pad = lambda a: np.pad(a, [(2, 2)] * d + [(0, 0)] * (a.ndim - d), mode="wrap")  # noqa: E731
     return [pad(f) for f in fl], pad(m)
 
 
@@ -174,3 +177,43 @@ def test_pairs_conserve_mass_over_phase_separation(precision):
     assert np.all(np.abs(mass1 - mass0) <= drift * np.abs(mass0)), (mass0, mass1)
     total = np.asarray(mom1, dtype=np.float64).reshape(p.components, 3).sum(axis=0)
     assert np.abs(total).max() <= 1e-3 * float(np.sum(mass1)), mom1
+
+
+# The D2Q9 pair kernel (lb_pairs2d.cuh, the FP16 form; FP32 runs the
+# one-site D2Q9 kernel on the same lattices): every tau = 1, BDist2, an even
+# ny, no solid site; tiles of 256 y, the second partial, and tiny extents.
+CASES_2D = {
+    "d2q9-two-tiles": lambda: spinodal((12, 300), perturb=0.03, d=2),
+    "d2q9-ny2": lambda: spinodal((6, 2), perturb=0.03, d=2),
+    "d2q9-ny258": lambda: spinodal((5, 258), perturb=0.03, d=2),
+}
+
+
+@pytest.mark.parametrize("precision", [lbgpu.FP32, lbgpu.FP16])
+@pytest.mark.parametrize("case", list(CASES_2D))
+def test_pairs2d_match_two_kernel_step(case, precision):
+    p = CASES_2D[case]()
+    a, fa = _run(p, 20, precision)
+    b, fb = _run(p, 20, precision, two_kernel=True)
+    tol = 2e-6 if precision == lbgpu.FP32 else 2e-3
+    ftol = 3e-7 if precision == lbgpu.FP32 else 3e-4
+    for c in range(p.components):
+        scale = np.abs(b[c]).max()
+        assert np.all(np.isfinite(a[c]))
+        assert np.abs(a[c] - b[c]).max() <= tol * scale, (c, np.abs(a[c] - b[c]).max() / scale)
+        assert np.nanmax(np.abs(fa[c] - fb[c])) <= ftol, (c, np.nanmax(np.abs(fa[c] - fb[c])))
+
+
+@pytest.mark.parametrize("precision", [lbgpu.FP32, lbgpu.FP16])
+@pytest.mark.parametrize("shift", [(3, 5), (0, 66), (1, 256)])
+def test_pairs2d_translation_invariant_bitwise(precision, shift):
+    """Shifted sites move to other lanes, warps (the shuffles' edge loads),
+    tiles and ring gathers, and still compute the same bits."""
+    p = spinodal((12, 300), perturb=0.05, d=2)
+    fl, m = init.init_fields(p)
+    a, fa = _run(p, 15, precision, fields=(fl, m), rho0=(0.7, 0.7))
+    fs, ms = _shifted(fl, m, shift)
+    b, fb = _run(p, 15, precision, fields=(fs, ms), rho0=(0.7, 0.7))
+    for c in range(2):
+        assert np.array_equal(np.roll(a[c], shift, axis=(0, 1)), b[c]), c
+        assert np.array_equal(np.roll(fa[c], shift, axis=(0, 1)), fb[c], equal_nan=True), c

@@ -109,10 +109,15 @@ def test_step_host_reduced_forms(precision, pin):
 
 
 @pytest.mark.parametrize("precision", [lbgpu.FP32, lbgpu.FP16])
-def test_step_host_d2q9_fused_wavefront(precision):
-    """The D2Q9 fused kernel over row ranges (the wavefront) computes the bits
-    of its whole-lattice launch: walls, the wall force and a partial tile."""
-    p = droplet_channel((48, 300), radius=8.0, acc=1e-3, gwc=(0.3, -0.2), d=2)
+@pytest.mark.parametrize("case", ["walls", "periodic"])
+def test_step_host_d2q9_fused_wavefront(precision, case):
+    """The D2Q9 fused kernels over row ranges (the wavefront) compute the
+    bits of their whole-lattice launch: the one-site kernel with walls, the
+    wall force and a partial tile; the pair kernel on a periodic lattice."""
+    if case == "walls":
+        p = droplet_channel((48, 300), radius=8.0, acc=1e-3, gwc=(0.3, -0.2), d=2)
+    else:
+        p = spinodal((48, 300), perturb=0.03, d=2)
     _compare(p, precision, 3, True, record_force=True, scale=SCALES.get(precision))
 
 
