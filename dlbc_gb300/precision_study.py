@@ -1,12 +1,14 @@
 """Precision study: FP32, FP16-offset and 16-bit fixed-point (I16) storage
-against FP64 on a large spinodal decomposition.
+against FP64 on a large spinodal decomposition, or on the droplet channel.
 
-Two-component D3Q19 Shan-Chen, periodic, rho = 0.7 +- `perturb` per site and
-component (device-side counter-based noise, the same initial state for every
-form up to the storage rounding), tau = 1, g = 3.6, psi = 1 - exp(-rho),
-BDist2.  Every form runs the same number of steps from the same initial
-fields; the FP64 form is the reference for the errors (it is bit-identical to
-the CPU restatement of the reference, checked at small sizes by the tests).
+Spinodal: two-component D3Q19 Shan-Chen, periodic, rho = 0.7 +- `perturb`
+per site and component (device-side counter-based noise, the same initial
+state for every form up to the storage rounding), tau = 1, g = 3.6,
+psi = 1 - exp(-rho), BDist2.  Channel (--workload channel): the benchmark's
+256x128x128 droplet channel, a flow that stays near its initial densities.
+Every form runs the same number of steps from the same initial fields; the
+FP64 form is the reference for the errors (it is bit-identical to the CPU
+restatement of the reference, checked at small sizes by the tests).
 
 Reported per form: time and MLUPS, relative L2 error of each component's
 density and velocity against FP64 at checkpoints, the fraction of sites
@@ -38,6 +40,27 @@ def spinodal_params(n: int, perturb: float, d: int = 3) -> params.LBParams:
     return params.LBParams.from_dict(params.parse_lines(lines), "d3q19" if d == 3 else "d2q9")
 
 
+def channel_params(n=(256, 128, 128)) -> params.LBParams:
+    """The droplet channel: a red sphere of radius 24 (1.0 / 0.05) in a blue
+    bath (0.05 / 1.0), bounce-back walls on z = 0 and z = nz - 1, body force
+    1e-6 along x, tau = 1, g = 3.6, BDist2: a flow that stays near its
+    initial densities, unlike the spinodal."""
+    lines = [
+        "[lattice]", f"gn = [{n[0]}, {n[1]}, {n[2]}]",
+        "[lb]", "components = 2", 'fieldNames = ["red", "blue"]', "tau = [1.0, 1.0]",
+        "eqdist.eqDistForm = BDist2", "force.enableShanChen = true",
+        "force.gcc = [[0.0, 3.6], [3.6, 0.0]]", "force.psiForm = Exponential",
+        "force.globalAcc = [1e-6, 0.0, 0.0]",
+        "init.fluidInit = [EqDistSphere, EqDistSphere]",
+        "init.fluidDensities = [[1.0, 0.05], [0.05, 1.0]]",
+        "init.initRadius = 24.0", "init.interfaceThickness = 0.0",
+        "mask.maskInit = Walls",
+        "mask.dimensionHasWall = [[false, false], [false, false], [true, true]]",
+        "mask.wallThickness = 1",
+    ]
+    return params.LBParams.from_dict(params.parse_lines(lines), "d3q19")
+
+
 def run_form(p, precision, steps, checkpoints, seed, device=0, rho0=(0.0, 0.0)):
     g = lbgpu.GPULattice(p, precision=precision, device=device, rho0=rho0)
     g.init_device(seed)
@@ -67,6 +90,8 @@ def rel_l2(a, b):
 
 def main():
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--workload", choices=["spinodal", "channel"], default="spinodal",
+                    help="the n^3 spinodal, or the 256x128x128 droplet channel (--n ignored)")
     ap.add_argument("--n", type=int, default=512)
     ap.add_argument("--steps", type=int, default=5000)
     ap.add_argument("--perturb", type=float, default=0.02)
@@ -77,11 +102,17 @@ def main():
                          "(a tiny value such as 1e-12 stores plain scaled f_q / w_q)")
     args = ap.parse_args()
     cps = sorted({int(c) for c in args.checkpoints.split(",") if int(c) <= args.steps} | {args.steps})
-    p = spinodal_params(args.n, args.perturb)
-    sites = args.n ** 3
+    if args.workload == "channel":
+        p = channel_params()
+        sites = 256 * 128 * 128
+        what = (f"256x128x128 droplet channel (walls z = 0 / 127, body force 1e-6, radius 24), "
+                f"{args.steps} steps, BDist2, g 3.6")
+    else:
+        p = spinodal_params(args.n, args.perturb)
+        sites = args.n ** 3
+        what = f"{args.n}^3 periodic spinodal decomposition, rho 0.7 +- {args.perturb}, {args.steps} steps, BDist2, g 3.6"
     ref, t64 = run_form(p, lbgpu.FP64, args.steps, cps, args.seed)
-    report = {"workload": f"{args.n}^3 periodic spinodal decomposition, rho 0.7 +- {args.perturb}, "
-                          f"{args.steps} steps, BDist2, g 3.6",
+    report = {"workload": what,
               "fp64": {"time_s": round(t64, 2), "mlups": round(sites * args.steps / t64 / 1e6, 1),
                        "mass_drift": {cp: ref[cp][2] for cp in cps}}}
     forms = [("fp32", lbgpu.FP32, (0.0, 0.0)), ("fp16", lbgpu.FP16, (0.0, 0.0)), ("i16", lbgpu.I16, (0.0, 0.0))]
