@@ -98,9 +98,12 @@ template <>
 __device__ __forceinline__ double from_storage<__half>(__half v, int q, int c, const StepParams& P, int Q) {
   return double(wq(Q, q) * fmaf(P.scale[c], __half2float(v), P.rho0[c]));
 }
+// I16 in double: the sums of a lattice whose integer offsets are conserved
+// (the I16 collision conserves every site's mass exactly) then are too, to
+// double rounding
 template <>
 __device__ __forceinline__ double from_storage<int16_t>(int16_t v, int q, int c, const StepParams& P, int Q) {
-  return double(wq(Q, q) * fmaf(P.scale[c], float(v), P.rho0[c]));
+  return lbk::weight_of(Q, q) * (double(P.rho0[c]) + double(P.scale[c]) * double(v));
 }
 
 struct Geo {

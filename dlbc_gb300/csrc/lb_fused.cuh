@@ -171,7 +171,11 @@ struct FStore<int16_t, Q> {
     return load(p, c, q, P);
   }
   __device__ static __forceinline__ void store(int16_t* p, float v, int c, int q, const FusedParams& P) {
-    const int h = __float2int_rn(fmaf(v, P.inv_wscale[c][Conn<Q>::wclass(q)], P.hoff[c][Conn<Q>::wclass(q)]));
+    store_h(p, fmaf(v, P.inv_wscale[c][Conn<Q>::wclass(q)], P.hoff[c][Conn<Q>::wclass(q)]));
+  }
+  // an offset in units of the scale, rounded and saturated
+  __device__ static __forceinline__ void store_h(int16_t* p, float hf) {
+    const int h = __float2int_rn(hf);
     *p = int16_t(h < -32767 ? -32767 : (h > 32767 ? 32767 : h));
   }
 };
@@ -274,10 +278,12 @@ __device__ __forceinline__ YZ make_yz(int y, int z, const FusedParams& P) {
 
 // Pull-gather one site; planes[0..2] are the offsets of planes xg-1, xg,
 // xg+1 of the gathered plane xg; nbm is the site's neighbour mask.
+// For the I16 form mass[c] accumulates the gathered mass in units of s/36,
+// 12 h_0 + 2 sum_axis h + sum_diag h, exactly (an integer held in float).
 template <typename T, bool WALLS, int C>
 __device__ __forceinline__ void fused_gather(const T* const (&fc)[2], const FusedParams& P,
                                              const uint32_t (&planes)[3], const YZ& yz, uint32_t nbm,
-                                             float (&pop)[C][19]) {
+                                             float (&pop)[C][19], float (&mass)[C]) {
   const uint32_t s = planes[1] + uint32_t(yz.off[1][1]);
   const bool solid = WALLS && (nbm & 1u);
   // branch-free (warps straddling a wall must not run two code paths):
@@ -292,8 +298,24 @@ __device__ __forceinline__ void fused_gather(const T* const (&fc)[2], const Fuse
     if (WALLS && q > 0) bb = ((nbm >> b) & 1u) && !solid;  // x - c_q = x + c_b is solid
     const uint32_t off = (bb ? P.qn[b] : P.qn[q]) + ((WALLS && (solid || bb)) ? s : nb);
 #pragma unroll
-    for (int c = 0; c < C; ++c) pop[c][q] = FStore<T>::load2(fc[c] + off, c, q, b, bb, P);
+    for (int c = 0; c < C; ++c) {
+      if constexpr (std::is_same<T, int16_t>::value) {
+        const float h = float(__ldg(fc[c] + off));
+        const int k = Conn<19>::wclass(q);
+        pop[c][q] = fmaf(P.wscale[c][k], h, P.wrho[c][k]);  // FStore<int16_t>::load2
+        mass[c] = fmaf(k == 0 ? 12.f : (k == 1 ? 2.f : 1.f), h, mass[c]);
+      } else {
+        pop[c][q] = FStore<T>::load2(fc[c] + off, c, q, b, bb, P);
+      }
+    }
   }
+}
+
+// Shared-memory slots per component and site of the tile's kept state: the
+// momenta (MOM) or the populations, and for the I16 form the gathered mass
+template <typename T, bool MOM>
+constexpr int fused_np() {
+  return (MOM ? 3 : 19) + (std::is_same<T, int16_t>::value ? 1 : 0);
 }
 
 // Process plane-tiles [w0, w1) of one lattice (tile-major: w = tile*nx + x).
@@ -307,8 +329,11 @@ __device__ __forceinline__ void fused_gather(const T* const (&fc)[2], const Fuse
 template <typename T, int C, bool WALLS, int TY, bool MOM = false>
 __device__ __forceinline__ void fused_body(const FusedParams& P, const T* __restrict__ f, T* __restrict__ fout,
                                            const uint32_t* __restrict__ nbmask, double* __restrict__ force_out,
-                                           int64_t w0, int64_t w1, FusedShared<TY, MOM ? 3 : 19>& sh) {
+                                           int64_t w0, int64_t w1, FusedShared<TY, fused_np<T, MOM>()>& sh) {
   constexpr int kFusedTY = TY;
+  // the I16 form conserves every site's mass exactly (see the collision)
+  constexpr bool EXACT = std::is_same<T, int16_t>::value;
+  constexpr int NP = fused_np<T, MOM>();
   const int t = threadIdx.x;
   const int ty = t / kFusedTZ, tz = t % kFusedTZ;
   const uint32_t plane_sz = uint32_t(P.ny) * uint32_t(P.nz);
@@ -378,17 +403,20 @@ __device__ __forceinline__ void fused_body(const FusedParams& P, const T* __rest
       if (active) {
         const uint32_t nbm = pw ? nbm_in : 0u;
         nbm_next = nbm;
-        float pop[C][19];
+        float pop[C][19], mass[C];
+#pragma unroll
+        for (int c = 0; c < C; ++c) mass[c] = 0.f;
         if (pw)
-          fused_gather<T, WALLS, C>(fc, P, planes, yz_in, nbm, pop);
+          fused_gather<T, WALLS, C>(fc, P, planes, yz_in, nbm, pop, mass);
         else
-          fused_gather<T, false, C>(fc, P, planes, yz_in, 0u, pop);
+          fused_gather<T, false, C>(fc, P, planes, yz_in, 0u, pop, mass);
 #pragma unroll
         for (int c = 0; c < C; ++c) {
           const float den = density<19, float>(pop[c]);
           sh.rho[ps][c][ty + 1][tz + 1] = den;
           sh.psi[ps][c][ty + 1][tz + 1] = P.psi_form ? 1.0f - __expf(-den) : den;
           if (keep >= 0) {
+            if (EXACT) sh.pops[keep][c][NP - 1][t] = mass[c];
             if (MOM) {
 #pragma unroll
               for (int vd = 0; vd < 3; ++vd) sh.pops[keep][c][vd][t] = moment<19, float>(pop[c], vd);
@@ -401,11 +429,13 @@ __device__ __forceinline__ void fused_body(const FusedParams& P, const T* __rest
       }
       if (has_ring) {
         const uint32_t nbm = pw ? nbm_ring : 0u;
-        float pop[C][19];
+        float pop[C][19], mass[C];  // (the ring sites' mass is not needed)
+#pragma unroll
+        for (int c = 0; c < C; ++c) mass[c] = 0.f;
         if (pw)
-          fused_gather<T, WALLS, C>(fc, P, planes, yz_ring, nbm, pop);
+          fused_gather<T, WALLS, C>(fc, P, planes, yz_ring, nbm, pop, mass);
         else
-          fused_gather<T, false, C>(fc, P, planes, yz_ring, 0u, pop);
+          fused_gather<T, false, C>(fc, P, planes, yz_ring, 0u, pop, mass);
 #pragma unroll
         for (int c = 0; c < C; ++c) {
           const float den = density<19, float>(pop[c]);
@@ -558,6 +588,32 @@ __device__ __forceinline__ void fused_body(const FusedParams& P, const T* __rest
           else
             eq_poly<19, float>(pop, dv, den[c], P.eq_form == 1, eq);
           const float omega = P.omega[c], omo = P.one_minus_omega[c];
+          if constexpr (EXACT) {
+            // Exact mass conservation (the pair kernel's rule): the new
+            // values rounded to integers and saturated, their mass 12 h_0 +
+            // 2 sum_axis h + sum_diag h made equal to the gathered one, the
+            // difference to h_0 in multiples of 12 and one unit each to the
+            // first diagonal populations
+            float m_out = 0.f;
+#pragma unroll
+            for (int q = 0; q < 19; ++q) {
+              const float v = (MOM || unit) ? eq[q] : relax(pop[q], omo, omega, eq[q]);
+              const int k = Conn<19>::wclass(q);
+              eq[q] = fminf(fmaxf(rintf(fmaf(v, P.inv_wscale[c][k], P.hoff[c][k])), -32767.f), 32767.f);
+              m_out = fmaf(k == 0 ? 12.f : (k == 1 ? 2.f : 1.f), eq[q], m_out);
+            }
+            const int d = __float2int_rz(sh.pops[cur][c][NP - 1][t] - m_out);
+            const int d0 = d / 12, r = d - 12 * d0;
+            eq[0] += float(d0);
+#pragma unroll
+            for (int k = 0; k < 12; ++k)
+              if (k < abs(r)) eq[7 + k] += r > 0 ? 1.f : -1.f;
+            if (!solid) {
+#pragma unroll
+              for (int q = 0; q < 19; ++q) FStore<int16_t>::store_h(fo[c] + (P.qn[q] + s), eq[q]);
+            }
+            continue;
+          }
           if (!solid) {
 #pragma unroll
             for (int q = 0; q < 19; ++q) {
@@ -583,7 +639,7 @@ __global__ void __launch_bounds__(TY * kFusedTZ, MOM ? (8 / TY) * mom_ctas<WALLS
     k_fused(const T* __restrict__ f, T* __restrict__ fout, const uint32_t* __restrict__ nbmask,
             double* __restrict__ force_out, FusedParams P) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  FusedShared<TY, MOM ? 3 : 19>& sh = *reinterpret_cast<FusedShared<TY, MOM ? 3 : 19>*>(smem_raw);
+  FusedShared<TY, fused_np<T, MOM>()>& sh = *reinterpret_cast<FusedShared<TY, fused_np<T, MOM>()>*>(smem_raw);
   if (!P.work_counter) {
     const int64_t w0 = P.work * blockIdx.x / gridDim.x;
     const int64_t w1 = P.work * (blockIdx.x + 1) / gridDim.x;
@@ -632,7 +688,7 @@ __global__ void __launch_bounds__(TY * kFusedTZ, 8 / TY * 2 > 4 ? 4 : 8 / TY * 2
     k_fused_batch(const FusedSim* __restrict__ sims, int nsims, int64_t total_work, int parity,
                   int64_t total_units, int* __restrict__ counters) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  FusedShared<TY>& sh = *reinterpret_cast<FusedShared<TY>*>(smem_raw);
+  FusedShared<TY, fused_np<T, false>()>& sh = *reinterpret_cast<FusedShared<TY, fused_np<T, false>()>*>(smem_raw);
   __shared__ FusedParams Ps;
   __shared__ int s_idx;
   __shared__ long long s_w[2];
@@ -692,7 +748,7 @@ __global__ void __launch_bounds__(TY * kFusedTZ, 8 / TY * 2 > 4 ? 4 : 8 / TY * 2
     // bits as the general body, with fewer instructions)
     if (C == 2 && Ps.unit_tau && Ps.eq_form == 2)
       fused_body<T, C, WALLS, TY, true>(Ps, fin, fout, sims[i].nbmask, sims[i].force_out, r0 - wb, r1 - wb,
-                                               *reinterpret_cast<FusedShared<TY, 3>*>(smem_raw));
+                                               *reinterpret_cast<FusedShared<TY, fused_np<T, true>()>*>(smem_raw));
     else
       fused_body<T, C, WALLS, TY>(Ps, fin, fout, sims[i].nbmask, sims[i].force_out, r0 - wb, r1 - wb, sh);
     w = r1;

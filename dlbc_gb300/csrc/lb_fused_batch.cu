@@ -16,7 +16,7 @@ cudaError_t go_batch(const FusedSim* sims, int nsims, int64_t total, int parity,
                      int device, int64_t total_units, int* counters) {
   static KernelInfo info;
   auto kern = k_fused_batch<T, 2, W, TY>;
-  const int smem = int(sizeof(FusedShared<TY>));
+  const int smem = int(sizeof(FusedShared<TY, fused_np<T, false>()>));
   int per_sm = 0;
   cudaError_t e = kernel_setup(kern, smem, TY * kFusedTZ, device, info, &per_sm);
   if (e != cudaSuccess) return e;

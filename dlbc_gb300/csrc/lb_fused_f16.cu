@@ -16,7 +16,7 @@ template <typename T, int C, bool W, int TY, bool MOM = false>
 cudaError_t go_single(const StepBuffers& b, const FusedParams& F, cudaStream_t st, int device) {
   static KernelInfo info;
   auto kern = k_fused<T, C, W, TY, MOM>;
-  const int smem = int(sizeof(FusedShared<TY, MOM ? 3 : 19>));
+  const int smem = int(sizeof(FusedShared<TY, fused_np<T, MOM>()>));
   int per_sm = 0;
   cudaError_t e = kernel_setup(kern, smem, TY * kFusedTZ, device, info, &per_sm);
   if (e != cudaSuccess) return e;

@@ -189,6 +189,9 @@ struct PairIO<int16_t> : PairIO16<int16_t> {
 template <typename V>
 struct PairMom {
   V rho, j[3];
+  // offsets: the mass in units of s/36, 12 h_0 + 2 sum_axis h + sum_diag h
+  // (an integer for the I16 form, held exactly in float)
+  V mass;
 };
 
 template <bool OFFSETS, typename V>
@@ -206,12 +209,14 @@ __device__ __forceinline__ PairMom<V> pair_moments(const V (&v)[19], float s36, 
   if (OFFSETS) {
     // f_q = w_q (rho0 + s h_q), w = 12/36, 2/36, 1/36
     const V two = splat<V>(2.f);
-    m.rho = vfma(splat<V>(s36), vfma(splat<V>(12.f), v[0], vfma(two, A, D)), splat<V>(rho0));
+    m.mass = vfma(splat<V>(12.f), v[0], vfma(two, A, D));
+    m.rho = vfma(splat<V>(s36), m.mass, splat<V>(rho0));
     m.j[0] = vmul(splat<V>(s36), vfma(two, Ax, Dx));
     m.j[1] = vmul(splat<V>(s36), vfma(two, Ay, Dy));
     m.j[2] = vmul(splat<V>(s36), vfma(two, Az, Dz));
   } else {
     m.rho = vadd(vadd(v[0], A), D);
+    m.mass = m.rho;
     m.j[0] = vadd(Ax, Dx);
     m.j[1] = vadd(Ay, Dy);
     m.j[2] = vadd(Az, Dz);
@@ -277,6 +282,8 @@ __device__ __forceinline__ void pair_body(const FusedParams& P, const T* __restr
   using IO = PairIO<T>;
   using W = typename IO::W;
   constexpr bool OFF = IO::kOffsets;
+  // the I16 form conserves every site's mass exactly (see the collision)
+  constexpr bool EXACT = std::is_same<T, int16_t>::value;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t plane_sz = uint32_t(P.ny) * uint32_t(P.nz);
   const T* fc[C];
@@ -368,7 +375,9 @@ __device__ __forceinline__ void pair_body(const FusedParams& P, const T* __restr
 #pragma unroll
         for (int c = 0; c < C; ++c) {
           if (MOM) {
-            sh.mom[keep][c][0][warp][lane] = m[c].rho;
+            // (I16: the exact mass, from which the collision recomputes rho
+            // with the same operation)
+            sh.mom[keep][c][0][warp][lane] = EXACT ? m[c].mass : m[c].rho;
 #pragma unroll
             for (int vd = 0; vd < 3; ++vd) sh.mom[keep][c][1 + vd][warp][lane] = m[c].j[vd];
           } else {
@@ -428,7 +437,12 @@ __device__ __forceinline__ void pair_body(const FusedParams& P, const T* __restr
         if (MOM) {
 #pragma unroll
           for (int c = 0; c < C; ++c) {
-            m_cur[c].rho = sh.mom[cur][c][0][warp][lane];
+            if (EXACT) {
+              m_cur[c].mass = sh.mom[cur][c][0][warp][lane];
+              m_cur[c].rho = vfma(splat<float2>(s36[c]), m_cur[c].mass, splat<float2>(P.rho0[c]));
+            } else {
+              m_cur[c].rho = sh.mom[cur][c][0][warp][lane];
+            }
 #pragma unroll
             for (int vd = 0; vd < 3; ++vd) m_cur[c].j[vd] = sh.mom[cur][c][1 + vd][warp][lane];
           }
@@ -552,32 +566,70 @@ __device__ __forceinline__ void pair_body(const FusedParams& P, const T* __restr
           const float2 scale = splat<float2>(unit ? 1.f : P.omega[c]);
           const PairEq e = pair_eq_constants<OFF>(m_cur[c].rho, cst, P.rho0[c] * P.inv_scale[c], P.inv_scale[c], scale);
           const float2 omo = splat<float2>(P.one_minus_omega[c]);
-          auto put = [&](int q, float2 val) {
-            if (!unit) val = vfma(IO::val(sh.pops[cur][c][q][warp][lane]), omo, val);
-            IO::st(fo[c] + (P.qn[q] + own), IO::enc(val));
+          // the new value of every population (equilibrium, relaxed for
+          // tau != 1), handed to sink(q, value) pair by pair
+          auto emit_all = [&](auto&& sink) {
+            auto val = [&](int q, float2 v) {
+              if (!unit) v = vfma(IO::val(sh.pops[cur][c][q][warp][lane]), omo, v);
+              sink(q, v);
+            };
+            auto pair = [&](float2 cu, int axis, int ip, int im) {
+              const float2 cu2 = vmul(cu, cu);
+              const float2 even = vfma(e.kh, cu2, e.k1);
+              const float2 odd = vmul(vfma(e.k6, cu2, e.kc), cu);
+              float2 vp = vadd(even, odd), vm = vsub(even, odd);
+              if (!OFF && axis) {
+                vp = vmul(splat<float2>(2.f), vp);
+                vm = vmul(splat<float2>(2.f), vm);
+              }
+              val(ip, vp);
+              val(im, vm);
+            };
+            val(0, e.e0);
+            pair(ux, 1, 1, 2);
+            pair(uy, 1, 3, 4);
+            pair(uz, 1, 5, 6);
+            pair(vadd(ux, uy), 0, 7, 14);
+            pair(vsub(ux, uy), 0, 13, 8);
+            pair(vadd(ux, uz), 0, 11, 18);
+            pair(vsub(ux, uz), 0, 12, 17);
+            pair(vadd(uy, uz), 0, 9, 16);
+            pair(vsub(uy, uz), 0, 15, 10);
           };
-          auto pair = [&](float2 cu, int axis, int ip, int im) {
-            const float2 cu2 = vmul(cu, cu);
-            const float2 even = vfma(e.kh, cu2, e.k1);
-            const float2 odd = vmul(vfma(e.k6, cu2, e.kc), cu);
-            float2 vp = vadd(even, odd), vm = vsub(even, odd);
-            if (!OFF && axis) {
-              vp = vmul(splat<float2>(2.f), vp);
-              vm = vmul(splat<float2>(2.f), vm);
-            }
-            put(ip, vp);
-            put(im, vm);
-          };
-          put(0, e.e0);
-          pair(ux, 1, 1, 2);
-          pair(uy, 1, 3, 4);
-          pair(uz, 1, 5, 6);
-          pair(vadd(ux, uy), 0, 7, 14);
-          pair(vsub(ux, uy), 0, 13, 8);
-          pair(vadd(ux, uz), 0, 11, 18);
-          pair(vsub(ux, uz), 0, 12, 17);
-          pair(vadd(uy, uz), 0, 9, 16);
-          pair(vsub(uy, uz), 0, 15, 10);
+          if constexpr (EXACT) {
+            // Exact mass conservation: rounded to integers (and saturated to
+            // +-32767), the new values' mass 12 h_0 + 2 sum_axis h +
+            // sum_diag h differs from the gathered one (which the collision
+            // conserves in real arithmetic) by a few units, more where a
+            // value saturated; the difference goes to h_0 (in multiples of
+            // 12) and, one unit each, to the first diagonal populations.
+            // Streaming and bounce-back move stored values, so every
+            // lattice's total mass stays exactly what it was uploaded with
+            // (unless h_0 itself saturates).
+            auto rnd = [](float v) { return fminf(fmaxf(rintf(v), -32767.f), 32767.f); };
+            float2 mout = make_float2(0.f, 0.f);
+            emit_all([&](int q, float2 v) {
+              const float k = Conn<19>::wclass(q) == 0 ? 12.f : (Conn<19>::wclass(q) == 1 ? 2.f : 1.f);
+              mout = vfma(splat<float2>(k), make_float2(rnd(v.x), rnd(v.y)), mout);
+            });
+            const int dx = __float2int_rz(m_cur[c].mass.x - mout.x), dy = __float2int_rz(m_cur[c].mass.y - mout.y);
+            const int d0x = dx / 12, d0y = dy / 12;
+            const int rx = dx - 12 * d0x, ry = dy - 12 * d0y;
+            emit_all([&](int q, float2 v) {
+              float2 h = make_float2(rnd(v.x), rnd(v.y));
+              if (q == 0) {
+                h.x += float(d0x);
+                h.y += float(d0y);
+              } else if (Conn<19>::wclass(q) == 2) {
+                const int k = q - 7;  // diagonal index 0..11
+                if (k < abs(rx)) h.x += rx > 0 ? 1.f : -1.f;
+                if (k < abs(ry)) h.y += ry > 0 ? 1.f : -1.f;
+              }
+              IO::st(fo[c] + (P.qn[q] + own), IO::enc(h));
+            });
+          } else {
+            emit_all([&](int q, float2 v) { IO::st(fo[c] + (P.qn[q] + own), IO::enc(v)); });
+          }
         }
       }
       cur = 1 - cur;

@@ -97,6 +97,8 @@ def main():
     ap.add_argument("--perturb", type=float, default=0.02)
     ap.add_argument("--seed", type=int, default=11)
     ap.add_argument("--checkpoints", default="500,1000,2000,5000")
+    ap.add_argument("--forms", default="fp32,fp16,i16",
+                    help="comma-separated forms compared with FP64 (which always runs)")
     ap.add_argument("--fp16-origin", type=float, action="append", default=[],
                     help="also run the FP16 form with offsets from this density instead of the mean "
                          "(a tiny value such as 1e-12 stores plain scaled f_q / w_q)")
@@ -115,7 +117,9 @@ def main():
     report = {"workload": what,
               "fp64": {"time_s": round(t64, 2), "mlups": round(sites * args.steps / t64 / 1e6, 1),
                        "mass_drift": {cp: ref[cp][2] for cp in cps}}}
-    forms = [("fp32", lbgpu.FP32, (0.0, 0.0)), ("fp16", lbgpu.FP16, (0.0, 0.0)), ("i16", lbgpu.I16, (0.0, 0.0))]
+    wanted = set(args.forms.split(","))
+    forms = [(n, prec, (0.0, 0.0)) for n, prec in (("fp32", lbgpu.FP32), ("fp16", lbgpu.FP16), ("i16", lbgpu.I16))
+             if n in wanted]
     forms += [(f"fp16 origin {v:g}", lbgpu.FP16, (v, v)) for v in args.fp16_origin]
     for name, prec, rho0 in forms:
         res, t = run_form(p, prec, args.steps, cps, args.seed, rho0=rho0)
