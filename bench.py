@@ -6,8 +6,19 @@ whole lattice): the droplet-in-channel configuration, 256x128x128 sites,
 bounce-back walls on the z = 0 and z = 127 planes, periodic in x and y, a red
 sphere of radius 24 (rho_red 1.0 / rho_blue 0.05) in a blue bath (0.05 / 1.0),
 body force 1e-6 along x, tau = 1, g = 3.6, psi = 1 - exp(-rho), BDist2
-equilibrium.  The headline form is FP64 (the reference's arithmetic); FP32
-and FP16-offset-storage forms of the same workload are reported beside it.
+equilibrium.  The headline form is FP64 (the reference's arithmetic); beside
+it in the same JSON line:
+
+* ``forms``: the FP32, FP16-offset and I16-offset forms of the same
+  workload, each with its roofline and end-to-end figure;
+* ``general_tau``: FP32 and FP16 on the same channel with tau = 0.9 (the
+  general collision);
+* ``d2q9``: the 4096^2 D2Q9 periodic spinodal in FP64, FP32 and FP16;
+* ``spinodal512``: the 512^3 periodic spinodal in every form;
+* ``batched`` and ``served``: 256 lattices in one batch, and Poisson request
+  streams through the serving loop;
+* ``e2e``, ``cpu_baseline``, ``clocks``, ``gpu_launches`` and ``roofline``
+  of the headline form.
 
 Prints one JSON line (rank 0).  ``--impl reference`` times the reference's
 algorithm on the host cores instead (the CPU oracle, all threads).
