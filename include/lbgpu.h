@@ -58,7 +58,8 @@ extern "C" {
 #define LBGPU_FP32 1        /* float storage + float arithmetic */
 #define LBGPU_FP16 2        /* half storage of f - w_q*rho0 (scaled) + float arithmetic */
 #define LBGPU_I16 3         /* 16-bit fixed-point storage of f/w_q - rho0 (scaled) + float arithmetic;
-                             * D3Q19 with an even z extent and the BDist2 equilibrium only */
+                             * D3Q19 with an even z extent and the BDist2 equilibrium only; every
+                             * collision conserves the site's stored (integer) mass exactly */
 
 typedef struct lbgpu_config {
   int32_t d, q;               /* 3/19 (D3Q19), 2/9 (D2Q9), 1/3 (D1Q3) or 1/5 (D1Q5): gconn
