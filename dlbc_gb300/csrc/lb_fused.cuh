@@ -592,8 +592,8 @@ __device__ __forceinline__ void fused_body(const FusedParams& P, const T* __rest
             // Exact mass conservation (the pair kernel's rule): the new
             // values rounded to integers and saturated, their mass 12 h_0 +
             // 2 sum_axis h + sum_diag h made equal to the gathered one, the
-            // difference to h_0 in multiples of 12 and one unit each to the
-            // first diagonal populations
+            // difference to h_0 in multiples of 12 and the rest to the
+            // opposite pair h_7, h_14 (half each, an odd unit to h_7)
             float m_out = 0.f;
 #pragma unroll
             for (int q = 0; q < 19; ++q) {
@@ -603,11 +603,10 @@ __device__ __forceinline__ void fused_body(const FusedParams& P, const T* __rest
               m_out = fmaf(k == 0 ? 12.f : (k == 1 ? 2.f : 1.f), eq[q], m_out);
             }
             const int d = __float2int_rz(sh.pops[cur][c][NP - 1][t] - m_out);
-            const int d0 = d / 12, r = d - 12 * d0;
+            const int d0 = d / 12, r = d - 12 * d0, hr = r / 2;
             eq[0] += float(d0);
-#pragma unroll
-            for (int k = 0; k < 12; ++k)
-              if (k < abs(r)) eq[7 + k] += r > 0 ? 1.f : -1.f;
+            eq[7] += float(r - hr);
+            eq[14] += float(hr);
             if (!solid) {
 #pragma unroll
               for (int q = 0; q < 19; ++q) FStore<int16_t>::store_h(fo[c] + (P.qn[q] + s), eq[q]);

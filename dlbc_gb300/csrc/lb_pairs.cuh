@@ -601,32 +601,38 @@ __device__ __forceinline__ void pair_body(const FusedParams& P, const T* __restr
             // +-32767), the new values' mass 12 h_0 + 2 sum_axis h +
             // sum_diag h differs from the gathered one (which the collision
             // conserves in real arithmetic) by a few units, more where a
-            // value saturated; the difference goes to h_0 (in multiples of
-            // 12) and, one unit each, to the first diagonal populations.
-            // Streaming and bounce-back move stored values, so every
-            // lattice's total mass stays exactly what it was uploaded with
-            // (unless h_0 itself saturates).
+            // value saturated.  The difference goes to h_0 in multiples of
+            // 12 and the rest to the opposite pair h_7, h_14 (half each, an
+            // odd unit to h_7: no momentum but that unit), which are stored
+            // last; the other 16 are stored as they are formed.  Streaming
+            // and bounce-back move stored values, so every lattice's total
+            // mass stays exactly what it was uploaded with (unless one of
+            // the three adjusted values saturates).
             auto rnd = [](float v) { return fminf(fmaxf(rintf(v), -32767.f), 32767.f); };
-            float2 mout = make_float2(0.f, 0.f);
+            float2 mout = make_float2(0.f, 0.f), h0, h7, h14;
             emit_all([&](int q, float2 v) {
+              const float2 r = make_float2(rnd(v.x), rnd(v.y));
               const float k = Conn<19>::wclass(q) == 0 ? 12.f : (Conn<19>::wclass(q) == 1 ? 2.f : 1.f);
-              mout = vfma(splat<float2>(k), make_float2(rnd(v.x), rnd(v.y)), mout);
+              mout = vfma(splat<float2>(k), r, mout);
+              if (q == 0)
+                h0 = r;
+              else if (q == 7)
+                h7 = r;
+              else if (q == 14)
+                h14 = r;
+              else
+                IO::st(fo[c] + (P.qn[q] + own), IO::enc(r));
             });
             const int dx = __float2int_rz(m_cur[c].mass.x - mout.x), dy = __float2int_rz(m_cur[c].mass.y - mout.y);
             const int d0x = dx / 12, d0y = dy / 12;
             const int rx = dx - 12 * d0x, ry = dy - 12 * d0y;
-            emit_all([&](int q, float2 v) {
-              float2 h = make_float2(rnd(v.x), rnd(v.y));
-              if (q == 0) {
-                h.x += float(d0x);
-                h.y += float(d0y);
-              } else if (Conn<19>::wclass(q) == 2) {
-                const int k = q - 7;  // diagonal index 0..11
-                if (k < abs(rx)) h.x += rx > 0 ? 1.f : -1.f;
-                if (k < abs(ry)) h.y += ry > 0 ? 1.f : -1.f;
-              }
-              IO::st(fo[c] + (P.qn[q] + own), IO::enc(h));
-            });
+            const int hx = rx / 2, hy = ry / 2;
+            h0 = vadd(h0, make_float2(float(d0x), float(d0y)));
+            h7 = vadd(h7, make_float2(float(rx - hx), float(ry - hy)));
+            h14 = vadd(h14, make_float2(float(hx), float(hy)));
+            IO::st(fo[c] + (P.qn[0] + own), IO::enc(h0));
+            IO::st(fo[c] + (P.qn[7] + own), IO::enc(h7));
+            IO::st(fo[c] + (P.qn[14] + own), IO::enc(h14));
           } else {
             emit_all([&](int q, float2 v) { IO::st(fo[c] + (P.qn[q] + own), IO::enc(v)); });
           }
