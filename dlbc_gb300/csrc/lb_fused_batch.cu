@@ -33,7 +33,8 @@ cudaError_t go_pairs_batch(const PairSim* sims, int nsims, int parity, int ctas_
                            int64_t total_units, int* counters) {
   static KernelInfo info;
   auto kern = k_pairs_batch<T>;
-  const int smem = int(sizeof(PairShared<2, false, T>));
+  // (FP32 and FP16 members all have tau = 1: the smaller layout)
+  const int smem = int(sizeof(PairShared<2, !pairs_general<T>(), T>));
   int per_sm = 0;
   cudaError_t e = kernel_setup(kern, smem, kPairThreads, device, info, &per_sm);
   if (e != cudaSuccess) return e;

@@ -645,18 +645,25 @@ __device__ __forceinline__ void pair_body(const FusedParams& P, const T* __restr
 }
 
 // resident CTAs per SM the single-lattice kernel is compiled for (two: 20
-// warps per SM at up to 96 registers; the tau != 1 FP32 variant's shared
-// memory allows one)
+// warps per SM at up to 96 registers)
 #ifndef LB_PAIRS_MINB
 #define LB_PAIRS_MINB 2
 #endif
+
+// The variants that run: every tau = 1 (MOM) for FP32 and FP16, and for the
+// I16 form also tau != 1 (pairs_eligible: FP32 and FP16 lattices with a
+// tau != 1 run the one-site kernel).
+template <typename T>
+constexpr bool pairs_general() {
+  return std::is_same<T, int16_t>::value;
+}
 
 // The single-lattice kernel: persistent CTAs take runs of run_len planes of
 // one tile from the counter, x-chunk-major (neighbouring tiles march over
 // the same planes together and share their ring rows through L2), over the
 // planes [x_begin, x_end) of every tile.
 template <typename T, int C, bool MOM>
-__global__ void __launch_bounds__(kPairThreads, (MOM || sizeof(T) == 2) ? LB_PAIRS_MINB : 1)
+__global__ void __launch_bounds__(kPairThreads, LB_PAIRS_MINB)
     k_pairs(const T* __restrict__ f, T* __restrict__ fout, double* __restrict__ force_out, FusedParams P) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   auto& sh = *reinterpret_cast<PairShared<C, MOM, T>*>(smem_raw);
@@ -742,12 +749,13 @@ __global__ void __launch_bounds__(kPairThreads, 2)
     T* fout = const_cast<T*>(static_cast<const T*>(sims[i].f[1 - par]));
     const long long r0 = s_w[0], r1 = s_w[1];
     __syncthreads();
-    if (Ps.unit_tau)
+    if (!pairs_general<T>() || Ps.unit_tau) {
       pair_body<T, 2, true>(Ps, fin, fout, sims[i].force_out, r0, r1,
                             *reinterpret_cast<PairShared<2, true, T>*>(smem_raw));
-    else
+    } else if constexpr (pairs_general<T>()) {
       pair_body<T, 2, false>(Ps, fin, fout, sims[i].force_out, r0, r1,
                              *reinterpret_cast<PairShared<2, false, T>*>(smem_raw));
+    }
   }
 }
 
@@ -774,8 +782,13 @@ cudaError_t go_pairs(const StepBuffers& b, const FusedParams& F, cudaStream_t st
 template <typename T>
 cudaError_t launch_pairs(int c, bool mom, const StepBuffers& b, const FusedParams& F, cudaStream_t st, int device) {
   if (b.mask) return cudaErrorInvalidValue;  // solid sites: the one-site kernel
-  if (c == 2) return mom ? go_pairs<T, 2, true>(b, F, st, device) : go_pairs<T, 2, false>(b, F, st, device);
-  return mom ? go_pairs<T, 1, true>(b, F, st, device) : go_pairs<T, 1, false>(b, F, st, device);
+  if constexpr (pairs_general<T>()) {
+    if (c == 2) return mom ? go_pairs<T, 2, true>(b, F, st, device) : go_pairs<T, 2, false>(b, F, st, device);
+    return mom ? go_pairs<T, 1, true>(b, F, st, device) : go_pairs<T, 1, false>(b, F, st, device);
+  } else {
+    if (!mom) return cudaErrorInvalidValue;  // tau != 1: the one-site kernel
+    return c == 2 ? go_pairs<T, 2, true>(b, F, st, device) : go_pairs<T, 1, true>(b, F, st, device);
+  }
 }
 
 }  // namespace lbk
