@@ -159,7 +159,10 @@ int build_table(lbgpu_batch* b, const Shape& sh) {
       lbk::PairSim ps;
       memset(&ps, 0, sizeof ps);
       ps.P = lbk::make_fused_params(h->P, 8);
-      ps.P.tiles_y = (h->ny + lbk::kPairTY - 1) / lbk::kPairTY;
+      const int pty = lbk::pair_ty(b->precision == LBGPU_FP16  ? lbk::kStoreF16
+                                   : b->precision == LBGPU_I16 ? lbk::kStoreI16
+                                                               : lbk::kStoreF32);
+      ps.P.tiles_y = (h->ny + pty - 1) / pty;
       ps.P.tiles_z = (h->nz + lbk::kPairTZ - 1) / lbk::kPairTZ;
       ps.P.work = int64_t(ps.P.tiles_y) * ps.P.tiles_z * h->nx;
       ps.P.run_len = h->nx < sh.prun ? h->nx : sh.prun;

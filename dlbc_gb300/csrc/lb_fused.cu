@@ -89,7 +89,7 @@ cudaError_t launch_fused_range(int kind, int q, int c, const StepBuffers& b, con
                                            : launch_fused2d(kind, c, w, c == 2 && P.unit_tau && P.eq_form == 2, b, G,
                                                             st, device);
   if (pairs_eligible(kind, P, b)) {
-    G.tiles_y = (P.ny + kPairTY - 1) / kPairTY;
+    G.tiles_y = (P.ny + pair_ty(kind) - 1) / pair_ty(kind);
     G.tiles_z = (P.nz + kPairTZ - 1) / kPairTZ;
     G.work = int64_t(G.tiles_y) * G.tiles_z * P.nx;
     const bool mom = P.unit_tau != 0;
@@ -127,7 +127,7 @@ cudaError_t launch_fused(int kind, int q, int c, const StepBuffers& b, const Ste
   } else if (pairs_eligible(kind, P, b)) {
     // two z-adjacent sites per thread (lb_pairs.cuh): 8 x 64 tiles
     FusedParams G = F;
-    G.tiles_y = (P.ny + kPairTY - 1) / kPairTY;
+    G.tiles_y = (P.ny + pair_ty(kind) - 1) / pair_ty(kind);
     G.tiles_z = (P.nz + kPairTZ - 1) / kPairTZ;
     G.work = int64_t(G.tiles_y) * G.tiles_z * P.nx;
     const bool mom = P.unit_tau != 0;

@@ -36,13 +36,13 @@ cudaError_t go_pairs_batch(const PairSim* sims, int nsims, int parity, int ctas_
   // (FP32 and FP16 members all have tau = 1: the smaller layout)
   const int smem = int(sizeof(PairShared<2, !pairs_general<T>(), T>));
   int per_sm = 0;
-  cudaError_t e = kernel_setup(kern, smem, kPairThreads, device, info, &per_sm);
+  cudaError_t e = kernel_setup(kern, smem, pair_threads<T>(), device, info, &per_sm);
   if (e != cudaSuccess) return e;
   if (ctas_per_sm > 0 && ctas_per_sm < per_sm) per_sm = ctas_per_sm;
   int64_t grid = int64_t(per_sm) * sm_count(device);
   if (grid > total_units) grid = total_units;
   if (grid < 1) return cudaSuccess;
-  kern<<<unsigned(grid), kPairThreads, smem, st>>>(sims, nsims, parity, total_units, counters);
+  kern<<<unsigned(grid), pair_threads<T>(), smem, st>>>(sims, nsims, parity, total_units, counters);
   return cudaGetLastError();
 }
 

@@ -2,11 +2,12 @@
 // bandwidth forms: float arithmetic on float, half-offset or 16-bit
 // fixed-point storage).
 //
-// Layout of the work.  A CTA owns a tile of kPairTY rows (y) x 64 sites (z)
-// and marches along x.  Ten warps: warp w < kPairTY owns row y0 + w, lane l
+// Layout of the work.  A CTA owns a tile of TY rows (y) x 64 sites (z) and
+// marches along x (TY = pair_ty: 8, or 14 for half offsets).  TY + 2 warps:
+// warp w < TY owns row y0 + w, lane l
 // the sites z0 + 2l and z0 + 2l + 1 (one 4-byte or 8-byte word of every
 // population array); the two ring warps gather the rows y0 - 1 and
-// y0 + kPairTY and the sites z0 - 1 / z0 + 64 of every row, whose psi the
+// y0 + TY and the sites z0 - 1 / z0 + 64 of every row, whose psi the
 // stencil needs but which other tiles own.  Per plane:
 //
 //   1. every warp pull-gathers its row of plane x+1 with one aligned word
@@ -65,8 +66,20 @@ namespace lbk {
 
 // (kPairTZ = 64 sites per tile row, 32 lanes x 2: lb_launch.h)
 constexpr int kPairRZ = kPairTZ + 4;        // shared row: [1] left ring, [2, 2 + tzv) tile, [2 + tzv] right ring
-constexpr int kPairWarps = kPairTY + 2;     // row warps + the two ring warps
-constexpr int kPairThreads = kPairWarps * 32;
+// the storage kind, tile height, threads (row warps + the two ring warps)
+// and resident CTAs per SM of the pair kernel for storage T
+template <typename T>
+constexpr int pair_kind() {
+  return std::is_same<T, __half>::value ? kStoreF16 : (std::is_same<T, int16_t>::value ? kStoreI16 : kStoreF32);
+}
+template <typename T>
+constexpr int pair_ty_of() {
+  return pair_ty(pair_kind<T>());
+}
+template <typename T>
+constexpr int pair_threads() {
+  return (pair_ty_of<T>() + 2) * 32;
+}
 
 // ---------------------------------------------------------------------------
 // float and float2 arithmetic with the same per-lane rounding
@@ -233,13 +246,13 @@ template <int C, bool MOM, typename T>
 struct PairShared {
   // four plane slots: the ring warps gather the z-ring of plane x + 2 while
   // the row warps collide plane x with the slots of x - 1, x, x + 1
-  float psi[4][C][kPairTY + 2][kPairRZ];
+  float psi[4][C][pair_ty_of<T>() + 2][kPairRZ];
   // tau != 1: the row warps' gathered words of the next plane, [buffer][c][q][row][lane]
-  typename PairIO<T>::W pops[MOM ? 1 : 2][C][MOM ? 1 : 19][MOM ? 1 : kPairTY][32];
+  typename PairIO<T>::W pops[MOM ? 1 : 2][C][MOM ? 1 : 19][MOM ? 1 : pair_ty_of<T>()][32];
   // tau = 1: the row warps' density and momentum of the next plane,
   // [buffer][c][rho, jx, jy, jz][row][lane] (kept here rather than in
   // registers across the gather of the following plane)
-  float2 mom[MOM ? 2 : 1][C][4][MOM ? kPairTY : 1][32];
+  float2 mom[MOM ? 2 : 1][C][4][MOM ? pair_ty_of<T>() : 1][32];
 };
 
 // BDist2 equilibrium constants of one component for one pair: value_q =
@@ -284,6 +297,7 @@ __device__ __forceinline__ void pair_body(const FusedParams& P, const T* __restr
   constexpr bool OFF = IO::kOffsets;
   // the I16 form conserves every site's mass exactly (see the collision)
   constexpr bool EXACT = std::is_same<T, int16_t>::value;
+  constexpr int TY = pair_ty_of<T>();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t plane_sz = uint32_t(P.ny) * uint32_t(P.nz);
   const T* fc[C];
@@ -303,12 +317,12 @@ __device__ __forceinline__ void pair_body(const FusedParams& P, const T* __restr
     const int tile = int(w / P.nx);
     const int xs = int(w - int64_t(tile) * P.nx);
     const int run = int(min(w1 - w, int64_t(P.nx - xs)));
-    const int y0 = (tile / P.tiles_z) * kPairTY, z0 = (tile % P.tiles_z) * kPairTZ;
-    const int tyv = min(kPairTY, P.ny - y0), tzv = min(kPairTZ, P.nz - z0);
+    const int y0 = (tile / P.tiles_z) * TY, z0 = (tile % P.tiles_z) * kPairTZ;
+    const int tyv = min(TY, P.ny - y0), tzv = min(kPairTZ, P.nz - z0);
     // this warp's gathered row: r (shared row index) and y; ring warps take
     // rows 0 and tyv + 1
-    const bool ring_warp = warp >= kPairTY;
-    const int r = ring_warp ? (warp == kPairTY ? 0 : tyv + 1) : warp + 1;
+    const bool ring_warp = warp >= TY;
+    const int r = ring_warp ? (warp == TY ? 0 : tyv + 1) : warp + 1;
     const bool row_on = ring_warp || warp < tyv;
     const int y = wrap(y0 + r - 1, P.ny);
     // this lane's pair; idle lanes (beyond the row's end) repeat the first
@@ -323,11 +337,11 @@ __device__ __forceinline__ void pair_body(const FusedParams& P, const T* __restr
     const uint32_t r3[3] = {uint32_t(wrap(y - 1, P.ny)) * uint32_t(P.nz) + uint32_t(zl),
                             uint32_t(y) * uint32_t(P.nz) + uint32_t(zl),
                             uint32_t(wrap(y + 1, P.ny)) * uint32_t(P.nz) + uint32_t(zl)};
-    // ring warps' scalar sites: warp kPairTY the left column (z0 - 1), the
+    // ring warps' scalar sites: warp TY the left column (z0 - 1), the
     // other the right column (z0 + tzv), lane = shared row
     const bool has_zring = ring_warp && lane < tyv + 2;
-    const int zr = warp == kPairTY ? zleft : zright;
-    const int zr_i = warp == kPairTY ? 1 : 2 + tzv;  // shared column
+    const int zr = warp == TY ? zleft : zright;
+    const int zr_i = warp == TY ? 1 : 2 + tzv;  // shared column
     const int yr = wrap(y0 + lane - 1, P.ny);
     int yrs[3], zrs[3];
     yrs[0] = wrap(yr - 1, P.ny);
@@ -644,11 +658,12 @@ __device__ __forceinline__ void pair_body(const FusedParams& P, const T* __restr
   }
 }
 
-// resident CTAs per SM the single-lattice kernel is compiled for (two: 20
-// warps per SM at up to 96 registers)
-#ifndef LB_PAIRS_MINB
-#define LB_PAIRS_MINB 2
-#endif
+// resident CTAs per SM the kernels are compiled for: two of 10 warps at up
+// to 96 registers, one of 16 warps for half offsets (14 rows)
+template <typename T>
+constexpr int pair_minb() {
+  return pair_ty_of<T>() > 8 ? 1 : 2;
+}
 
 // The variants that run: every tau = 1 (MOM) for FP32 and FP16, and for the
 // I16 form also tau != 1 (pairs_eligible: FP32 and FP16 lattices with a
@@ -663,7 +678,7 @@ constexpr bool pairs_general() {
 // the same planes together and share their ring rows through L2), over the
 // planes [x_begin, x_end) of every tile.
 template <typename T, int C, bool MOM>
-__global__ void __launch_bounds__(kPairThreads, LB_PAIRS_MINB)
+__global__ void __launch_bounds__(pair_threads<T>(), pair_minb<T>())
     k_pairs(const T* __restrict__ f, T* __restrict__ fout, double* __restrict__ force_out, FusedParams P) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   auto& sh = *reinterpret_cast<PairShared<C, MOM, T>*>(smem_raw);
@@ -701,7 +716,7 @@ struct PairSim {
 // parameters (staged in shared memory), so it computes exactly what its
 // lone lattice computes.
 template <typename T>
-__global__ void __launch_bounds__(kPairThreads, 2)
+__global__ void __launch_bounds__(pair_threads<T>(), pair_minb<T>())
     k_pairs_batch(const PairSim* __restrict__ sims, int nsims, int parity, int64_t total_units,
                   int* __restrict__ counters) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -767,7 +782,7 @@ cudaError_t go_pairs(const StepBuffers& b, const FusedParams& F, cudaStream_t st
   auto kern = k_pairs<T, C, MOM>;
   const int smem = int(sizeof(PairShared<C, MOM, T>));
   int per_sm = 0;
-  cudaError_t e = kernel_setup(kern, smem, kPairThreads, device, info, &per_sm);
+  cudaError_t e = kernel_setup(kern, smem, pair_threads<T>(), device, info, &per_sm);
   if (e != cudaSuccess) return e;
   int64_t grid = int64_t(per_sm) * sm_count(device);
   FusedParams G = F;
@@ -775,7 +790,8 @@ cudaError_t go_pairs(const StepBuffers& b, const FusedParams& F, cudaStream_t st
   plan_runs(G, tiles, grid);
   const int64_t units = sched_units(G, int(tiles));
   if (grid > units) grid = units;
-  kern<<<unsigned(grid), kPairThreads, smem, st>>>(static_cast<const T*>(b.f), static_cast<T*>(b.fout), b.force, G);
+  kern<<<unsigned(grid), pair_threads<T>(), smem, st>>>(static_cast<const T*>(b.f), static_cast<T*>(b.fout), b.force,
+                                                        G);
   return cudaGetLastError();
 }
 
