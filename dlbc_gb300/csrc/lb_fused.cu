@@ -125,7 +125,7 @@ cudaError_t launch_fused(int kind, int q, int c, const StepBuffers& b, const Ste
             ? launch_pairs2d(kind, b, F, st, device)
             : launch_fused2d(kind, c, w, c == 2 && P.unit_tau && P.eq_form == 2, b, F, st, device);
   } else if (pairs_eligible(kind, P, b)) {
-    // two z-adjacent sites per thread (lb_pairs.cuh): 8 x 64 tiles
+    // two z-adjacent sites per thread (lb_pairs.cuh): pair_ty x 64 tiles
     FusedParams G = F;
     G.tiles_y = (P.ny + pair_ty(kind) - 1) / pair_ty(kind);
     G.tiles_z = (P.nz + kPairTZ - 1) / kPairTZ;

@@ -50,7 +50,7 @@ cudaError_t launch_fused_single_f16(int c, bool walls, bool mom, const StepBuffe
 cudaError_t launch_fused_single_i16(int c, bool walls, bool mom, const StepBuffers& b, const FusedParams& F,
                                     cudaStream_t st, int device);
 // The single-lattice pair step (lb_pairs.cuh), lattices without solid
-// sites: F holds the 8 x 64 pair tiling; mom: every tau = 1 (the gathered
+// sites: F holds the pair tiling (pair_ty x 64); mom: every tau = 1 (the gathered
 // populations are not kept).
 cudaError_t launch_pairs_single_f32(int c, bool mom, const StepBuffers& b, const FusedParams& F, cudaStream_t st,
                                     int device);

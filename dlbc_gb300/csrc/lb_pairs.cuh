@@ -701,7 +701,7 @@ __global__ void __launch_bounds__(pair_threads<T>(), pair_minb<T>())
 // One simulation of a batch for the pair kernel.  The step reads
 // populations f[(parity + phase) & 1] and writes the other buffer.
 struct PairSim {
-  FusedParams P;           // pair tiling (8 x 64), run_len set
+  FusedParams P;           // pair tiling (pair_ty x 64), run_len set
   const void* f[2];
   double* force_out;       // nullptr unless recording
   int64_t unit_begin;      // first run of this simulation in the batch
