@@ -99,7 +99,7 @@ __host__ __device__ __forceinline__ int sched_units(const FusedParams& P, int nt
   const int tail = (P.x_end - P.x_split + P.tail_len - 1) / P.tail_len;
   return ntl * (bulk + tail);
 }
-__device__ __forceinline__ void sched_run(const FusedParams& P, int ntl, int item, int& tile, int& x0, int& x1) {
+__host__ __device__ __forceinline__ void sched_run(const FusedParams& P, int ntl, int item, int& tile, int& x0, int& x1) {
   const int ub = ntl * ((P.x_split - P.x_begin) / P.run_len);
   if (item < ub) {
     const int ch = item / ntl;
