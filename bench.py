@@ -330,15 +330,17 @@ def fp64_rate(device):
 
 
 def step_kernel(precision, walls, unit_tau=True, nz_even=True, q=19):
-    """The kernel that runs the BDist2 step (the library's dispatch rule,
-    lbk::pairs_eligible): k_collide for FP64; for D2Q9 k_fused2d; for D3Q19
-    k_pairs without solid sites and with an even nz for I16 and for FP32/FP16
-    with every tau = 1; k_fused otherwise."""
+    """The kernel that runs the BDist2 step (the library's dispatch rules,
+    lbk::pairs_eligible and lbk::pairs2d_eligible): k_collide for FP64; for
+    D2Q9 k_pairs2d for FP16 with every tau = 1, no solid site and an even ny
+    (nz_even stands for it), k_fused2d otherwise; for D3Q19 k_pairs without
+    solid sites and with an even nz for I16 and for FP32/FP16 with every
+    tau = 1; k_fused otherwise."""
     from dlbc_gb300 import lbgpu
     if precision == lbgpu.FP64:
         return "k_collide"
     if q == 9:
-        return "k_fused2d"
+        return "k_pairs2d" if precision == lbgpu.FP16 and unit_tau and not walls and nz_even else "k_fused2d"
     if not walls and nz_even and (precision == lbgpu.I16 or unit_tau):
         return "k_pairs"
     return "k_fused"
