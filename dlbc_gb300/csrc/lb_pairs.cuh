@@ -134,7 +134,11 @@ struct PairIO<float> {
   }
   __device__ static __forceinline__ float2 val(W w) { return w; }
   __device__ static __forceinline__ W enc(float2 v) { return v; }
-  __device__ static __forceinline__ void st(float* p, W w) { *reinterpret_cast<float2*>(p) = w; }
+  // evict-first (streaming) stores: the new populations are not read again
+  // in this step, and the L2 keeps the ring rows that a neighbouring tile
+  // gathers again (measured at 512^3: 16 570 -> 16 950 MLUPS; the 16-bit
+  // forms were not faster with them)
+  __device__ static __forceinline__ void st(float* p, W w) { __stcs(reinterpret_cast<float2*>(p), w); }
 };
 
 // The 16-bit storages share their word handling: site z in the low half,
