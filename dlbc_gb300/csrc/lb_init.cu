@@ -8,8 +8,10 @@
 // :346-366, initPlates/Tube/Box/Walls :377-467 and initEqDistWall :469-477.
 // Compiled with -fmad=false: the double arithmetic is the reference's, so
 // the deterministic initialisers give the reference's values bit for bit.
-// The random initialisers use a counter-based generator (splitmix64 of seed,
-// component, population and site) instead of the sequential Mt19937 stream.
+// The random initialisers draw either the reference's sequence (Mt19937,
+// generated on the host in the reference's order and copied to the device,
+// lbgpu_init.rng = 1) or from a counter-based generator (splitmix64 of
+// seed, component, population and site).
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <math.h>
@@ -23,6 +25,7 @@
 
 #include "../../include/lbgpu.h"
 #include "lb_core.cuh"
+#include "lb_draws.h"
 #include "lb_handle.h"
 
 namespace {
@@ -45,6 +48,9 @@ struct InitDev {
   int mask_init, mask_axis, wall_offset, wall_thickness;
   int dhw[3][2];
   double eqpop[19];
+  // the reference's draws of component c for the physical sites ([site]
+  // or, ConstRandom, [site][q]; null: counter-based draws)
+  const uint32_t* draws[2];
 };
 
 enum {
@@ -60,6 +66,12 @@ __device__ __forceinline__ uint32_t hash_u32(unsigned long long seed, int c, int
   z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
   z = z ^ (z >> 31);
   return uint32_t(z >> 32);
+}
+
+// draw q (0 unless ConstRandom) of component c at physical site `site`
+__device__ __forceinline__ uint32_t draw_u32(const InitDev& I, int c, int q, int64_t site) {
+  if (I.draws[c]) return I.draws[c][I.fluid_init[c] == kConstRandom ? site * I.Q + q : site];
+  return hash_u32(I.seed, c, q, site);
 }
 
 // std.random.uniform!"[)"(a, b) with a 32-bit draw u
@@ -121,19 +133,19 @@ __device__ void site_pops(const InitDev& I, int c, const int g[3], int64_t site,
       for (int q = 0; q < Q; ++q) pop[q] = dens[0];
       return;
     case kConstRandom:
-      for (int q = 0; q < Q; ++q) pop[q] = dens[0] * uniform_ab(hash_u32(I.seed, c, q, site), 0.0, 2.0);
+      for (int q = 0; q < Q; ++q) pop[q] = dens[0] * uniform_ab(draw_u32(I, c, q, site), 0.0, 2.0);
       return;
     case kEqDist:
       val = dens[0];
       break;
     case kEqDistRandom:
-      val = dens[0] * uniform_ab(hash_u32(I.seed, c, 0, site), 0.0, 2.0);
+      val = dens[0] * uniform_ab(draw_u32(I, c, 0, site), 0.0, 2.0);
       break;
     case kEqDistPerturb:
-      val = dens[0] + uniform_ab(hash_u32(I.seed, c, 0, site), -I.perturb[c], I.perturb[c]);
+      val = dens[0] + uniform_ab(draw_u32(I, c, 0, site), -I.perturb[c], I.perturb[c]);
       break;
     case kEqDistPerturbFrac:
-      val = dens[0] * (1.0 + uniform_ab(hash_u32(I.seed, c, 0, site), -I.perturb[c], I.perturb[c]));
+      val = dens[0] * (1.0 + uniform_ab(draw_u32(I, c, 0, site), -I.perturb[c], I.perturb[c]));
       break;
     case kEqDistSphere:
     case kEqDistSphereFrac:
@@ -376,6 +388,62 @@ int build_init(const lbgpu_handle* h, const lbgpu_init* ini, InitDev* I, std::st
   return LBGPU_OK;
 }
 
+bool random_init(int fi) {
+  return fi == kEqDistPerturb || fi == kEqDistPerturbFrac || fi == kConstRandom || fi == kEqDistRandom;
+}
+
+// Device copies of the reference's draws, freed with the initialisation
+struct ReferenceDraws {
+  uint32_t* d[2] = {nullptr, nullptr};
+  ~ReferenceDraws() {
+    for (uint32_t* p : d)
+      if (p) cudaFree(p);
+  }
+};
+
+// The reference's draws of the random components (lb_draws.h), copied to
+// the device
+int make_reference_draws(lbgpu_handle* h, const lbgpu_init* ini, ReferenceDraws* out, InitDev* I) {
+  lbk::DrawSpec S;
+  S.n[0] = h->nx;
+  S.n[1] = h->ny;
+  S.n[2] = h->nz;
+  S.halo[0] = kHalo;
+  S.halo[1] = h->hy;
+  S.halo[2] = h->hz;
+  for (int i = 0; i < 3; ++i) S.nc[i] = (i < h->d && ini->nc[i] > 0) ? ini->nc[i] : 1;
+  S.seed = uint32_t(ini->seed);
+  S.shift_seed_by_rank = ini->shift_seed_by_rank != 0;
+  S.components = h->C;
+  bool any = false;
+  for (int c = 0; c < h->C; ++c) {
+    const int fi = ini->fluid_init[c];
+    S.per_site[c] = !random_init(fi) ? 0 : (fi == kConstRandom ? h->Q : 1);
+    S.reseed[c] = ini->random_reseed[c] != 0;
+    S.random_seed[c] = uint32_t(ini->random_seed[c]);
+    any = any || S.per_site[c] != 0;
+  }
+  if (!any) return LBGPU_OK;
+  std::vector<uint32_t> host[2];
+  if (!lbk::reference_draws(S, host))
+    return h->fail(LBGPU_E_INVALID, "the lattice does not divide evenly over lbgpu_init.nc");
+  for (int c = 0; c < h->C; ++c) {
+    if (host[c].empty()) continue;
+    const size_t bytes = host[c].size() * sizeof(uint32_t);
+    cudaError_t e = cudaMalloc(&out->d[c], bytes);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      out->d[c] = nullptr;
+      return h->fail(LBGPU_E_NOMEM, "no device memory for the initialiser's random draws");
+    }
+    e = cudaMemcpyAsync(out->d[c], host[c].data(), bytes, cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return h->cuda_fail(e, "initialiser draws");
+    I->draws[c] = out->d[c];
+  }
+  return LBGPU_OK;
+}
+
 int reduce_stats(lbgpu_handle* h, const InitDev& I, int pass, const double* d_rho0, double* d_partial, int nblocks,
                  double out[2], bool is_max) {
   k_init_stats<<<nblocks, kInitThreads, 0, h->stream>>>(I, h->n, pass, d_rho0, d_partial);
@@ -400,6 +468,10 @@ extern "C" int lbgpu_init_fields(lbgpu_handle* h, const lbgpu_init* ini) {
   InitDev I;
   std::string why;
   if (int rc = build_init(h, ini, &I, &why)) return h->fail(rc, why);
+  if (ini->rng != 0 && ini->rng != 1) return h->fail(LBGPU_E_INVALID, "lbgpu_init.rng must be 0 or 1");
+  ReferenceDraws draws;
+  if (ini->rng == 1)
+    if (int rc = make_reference_draws(h, ini, &draws, &I)) return rc;
   cudaError_t e;
   // the solid-site counter and the statistics partials use the staging buffer
   const int nblocks = int(std::max<size_t>(1, std::min<size_t>(512, (h->staging_bytes / sizeof(double) - 8) / 2)));

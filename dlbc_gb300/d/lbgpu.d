@@ -80,6 +80,11 @@ struct lbgpu_init {
   int wall_offset;
   int wall_thickness;
   int[2][3] dimension_has_wall;
+  int rng;
+  int[LBGPU_MAX_COMPONENTS] random_reseed;
+  int[3] nc;
+  int shift_seed_by_rank;
+  ulong[LBGPU_MAX_COMPONENTS] random_seed;
 }
 
 struct lbgpu_handle;

@@ -443,11 +443,19 @@ class LbgpuInit(C.Structure):
         ("init_axis", C.c_int32), ("interface_thickness", C.c_double), ("n_lamellae", C.c_int32),
         ("lamellae_widths", C.c_double * 8), ("mask_init", C.c_int32), ("mask_axis", C.c_int32),
         ("wall_offset", C.c_int32), ("wall_thickness", C.c_int32), ("dimension_has_wall", (C.c_int32 * 2) * 3),
+        ("rng", C.c_int32), ("random_reseed", C.c_int32 * MAXC), ("nc", C.c_int32 * 3),
+        ("shift_seed_by_rank", C.c_int32), ("random_seed", C.c_uint64 * MAXC),
     ]
 
 
-def make_init(p, seed: int = 0) -> LbgpuInit:
-    """Device initialiser description from :class:`dlbc_gb300.params.LBParams`."""
+def make_init(p, seed: int = 0, reference_rng: bool = False) -> LbgpuInit:
+    """Device initialiser description from :class:`dlbc_gb300.params.LBParams`.
+
+    ``reference_rng``: the random initialisers draw the reference's Mt19937
+    sequences on the process grid ``p.nc``, seeded with ``p.seed`` (``seed``
+    is then unused) and ``p.random_seed`` where ``p.random_reseed``, plus the
+    rank where ``p.shift_seed_by_rank``; otherwise counter-based draws keyed
+    by ``seed``."""
     ini = LbgpuInit()
     for f in range(p.components):
         ini.fluid_init[f] = p.fluid_init[f]
@@ -457,6 +465,16 @@ def make_init(p, seed: int = 0) -> LbgpuInit:
             ini.densities[f][j] = v
         ini.perturb[f] = p.fluid_perturb[f]
     ini.seed = seed & 0xFFFFFFFFFFFFFFFF
+    if reference_rng:
+        ini.rng = 1
+        ini.seed = int(p.seed) & 0xFFFFFFFFFFFFFFFF
+        ini.shift_seed_by_rank = int(bool(p.shift_seed_by_rank))
+        for i in range(min(p.d, 3, len(p.nc))):
+            ini.nc[i] = max(1, int(p.nc[i]))
+        for f in range(p.components):
+            if f < len(p.random_reseed) and p.random_reseed[f]:
+                ini.random_reseed[f] = 1
+                ini.random_seed[f] = int(p.random_seed[f]) & 0xFFFFFFFFFFFFFFFF
     ini.init_radius = p.init_radius
     for i in range(p.d):
         ini.init_offset[i] = p.init_offset[i]
@@ -485,19 +503,21 @@ def _init_lib():
     return L
 
 
-def _gpulattice_init_device(self, seed: int = 0) -> None:
-    """Fill the lattice on the device from its parameters (lbgpu_init_fields)."""
-    ini = make_init(self.p, seed)
+def _gpulattice_init_device(self, seed: int = 0, reference_rng: bool = False) -> None:
+    """Fill the lattice on the device from its parameters (lbgpu_init_fields);
+    ``reference_rng`` as :func:`make_init`."""
+    ini = make_init(self.p, seed, reference_rng)
     self._check(_init_lib().lbgpu_init_fields(self.h, C.byref(ini)), "lbgpu_init_fields")
 
 
 GPULattice.init_device = _gpulattice_init_device
 
 
-def _batch_add_device(self, p, seed: int = 0, rho0=(0.0, 0.0)) -> int:
-    """Admit a lattice whose initial fields are computed on the device."""
+def _batch_add_device(self, p, seed: int = 0, rho0=(0.0, 0.0), reference_rng: bool = False) -> int:
+    """Admit a lattice whose initial fields are computed on the device
+    (``reference_rng`` as :func:`make_init`)."""
     cfg = make_config(p, self.precision, self.device, rho0)
-    ini = make_init(p, seed)
+    ini = make_init(p, seed, reference_rng)
     sid = C.c_int32()
     self._check(_init_lib().lbgpu_batch_add_init(self.h, C.byref(cfg), C.byref(ini), C.byref(sid)),
                 "lbgpu_batch_add_init")

@@ -121,10 +121,17 @@ int lbgpu_collide(lbgpu_handle* h);
  * lamellae initialisers (and their Frac forms), EqDist, Const and every mask
  * but File give exactly the values the reference computes.  The random
  * initialisers (EqDistPerturb, EqDistPerturbFrac, EqDistRandom, ConstRandom)
- * draw from a counter-based generator keyed by `seed`, component and site,
- * not from the reference's sequential Mt19937 stream: same distribution,
- * different numbers (use lbgpu_upload with host-generated fields to
- * reproduce a reference run exactly).  FluidInit/MaskInit codes are the
+ * with rng = 1 draw the reference's sequences: on each rank of the process
+ * grid `nc`, Mt19937 seeded with `seed` (random.seed, plus the rank with
+ * shift_seed_by_rank; src/dlbc/random.d:43-53), one draw per haloed site of
+ * the rank's block in row-major order (ConstRandom: per population),
+ * component 0 before component 1 unless random_reseed
+ * (src/dlbc/lb/init.d:105-125); the draws are generated on the host, the
+ * fields on the device, and the result equals the reference's bit for bit.  With rng = 0 they draw from a
+ * counter-based generator keyed by `seed`, component and site (nothing
+ * generated on the host; same distribution, different numbers).  rng = 1
+ * holds the draws of the random components on the device during the call
+ * (4 bytes per site, ConstRandom 4 per population).  FluidInit/MaskInit codes are the
  * reference's enum orders (FluidInit: None 0, File 1, Const 2, EqDist 3,
  * EqDistPerturb 4, EqDistPerturbFrac 5, ConstRandom 6, EqDistRandom 7,
  * EqDistSphere 8, EqDistSphereFrac 9, EqDistCylinder 10, EqDistCylinderFrac 11,
@@ -149,6 +156,11 @@ typedef struct lbgpu_init {
   int32_t wall_offset;                           /* lb.mask.wallOffset */
   int32_t wall_thickness;                        /* lb.mask.wallThickness */
   int32_t dimension_has_wall[3][2];              /* lb.mask.dimensionHasWall */
+  int32_t rng;                                   /* 0: counter-based draws; 1: the reference's Mt19937 sequence */
+  int32_t random_reseed[LBGPU_MAX_COMPONENTS];   /* lb.init.randomReseed (rng = 1) */
+  int32_t nc[3];                                 /* parallel.nc whose per-rank sequences are drawn (rng = 1; 0 = 1) */
+  int32_t shift_seed_by_rank;                    /* random.shiftSeedByRank (rng = 1) */
+  uint64_t random_seed[LBGPU_MAX_COMPONENTS];    /* lb.init.randomSeed (rng = 1) */
 } lbgpu_init;
 
 int lbgpu_init_fields(lbgpu_handle* h, const lbgpu_init* ini);

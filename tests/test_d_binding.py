@@ -1,4 +1,5 @@
-"""The D binding (dlbc_gb300/d/lbgpu.d) against the C header it mirrors.
+"""The D binding (dlbc_gb300/d/lbgpu.d) and the Python ctypes structs
+(dlbc_gb300/lbgpu.py) against the C header they mirror.
 
 There is no D compiler here, so the binding is checked as text: the same
 functions with the same parameter and return types, the same constants, and
@@ -6,6 +7,7 @@ struct layouts that C's rules give identically for both (offsets and sizes
 of the C structs taken from gcc, the D fields laid out with C alignment, as
 extern(C) D structs are).
 """
+import ctypes
 import os
 import re
 import shutil
@@ -133,3 +135,16 @@ def test_struct_layouts_match(struct):
     c_layout = _c_layout(struct, list(d_layout))
     assert c_layout.pop("__size__")[0] == d_size
     assert c_layout == d_layout
+
+
+@pytest.mark.parametrize("struct,cls", [("lbgpu_config", "LbgpuConfig"), ("lbgpu_init", "LbgpuInit")])
+def test_python_struct_layouts_match(struct, cls):
+    """The ctypes mirrors in dlbc_gb300/lbgpu.py against the C header."""
+    from dlbc_gb300 import lbgpu
+
+    ct = getattr(lbgpu, cls)
+    names = [f[0] for f in ct._fields_]
+    c_layout = _c_layout(struct, names)
+    assert c_layout.pop("__size__")[0] == ctypes.sizeof(ct)
+    py = {n: (getattr(ct, n).offset, getattr(ct, n).size) for n in names}
+    assert py == c_layout
