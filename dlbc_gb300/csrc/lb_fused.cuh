@@ -173,6 +173,8 @@ struct FStore<int16_t, Q> {
   __device__ static __forceinline__ void store(int16_t* p, float v, int c, int q, const FusedParams& P) {
     store_h(p, fmaf(v, P.inv_wscale[c][Conn<Q>::wclass(q)], P.hoff[c][Conn<Q>::wclass(q)]));
   }
+  // an offset already integral within +-32767
+  __device__ static __forceinline__ void store_int(int16_t* p, float h) { *p = int16_t(__float2int_rz(h)); }
   // an offset in units of the scale, rounded and saturated
   __device__ static __forceinline__ void store_h(int16_t* p, float hf) {
     const int h = __float2int_rn(hf);
@@ -609,7 +611,12 @@ __device__ __forceinline__ void fused_body(const FusedParams& P, const T* __rest
             eq[14] += float(hr);
             if (!solid) {
 #pragma unroll
-              for (int q = 0; q < 19; ++q) FStore<int16_t>::store_h(fo[c] + (P.qn[q] + s), eq[q]);
+              for (int q = 0; q < 19; ++q) {
+                if (q == 0 || q == 7 || q == 14)
+                  FStore<int16_t>::store_h(fo[c] + (P.qn[q] + s), eq[q]);
+                else
+                  FStore<int16_t>::store_int(fo[c] + (P.qn[q] + s), eq[q]);
+              }
             }
             continue;
           }
