@@ -76,3 +76,22 @@ def test_reference_draws_reject_an_uneven_grid(harness, tmp_path):
     args = [harness, str(tmp_path / "x.bin"), "9", "4", "4", "2", "2", "2", "2", "1", "1", "0", "1", "1", "1",
             "0", "0", "0", "0", "0"]
     assert subprocess.run(args, timeout=60).returncode == 3
+
+
+def test_make_init_describes_the_reference_draws():
+    """The Python side of rng = 1 (dlbc_gb300.lbgpu.make_init): the
+    reference's seed, process grid, seed shift and reseeded components."""
+    lbgpu = pytest.importorskip("dlbc_gb300.lbgpu")
+    from lbcases import spinodal
+
+    p = spinodal((24, 20, 16), seed=-3)
+    p.nc = [2, 0, 2]
+    p.shift_seed_by_rank = False
+    p.random_reseed = [False, True]
+    p.random_seed = [0, 43]
+    ini = lbgpu.make_init(p, seed=99, reference_rng=True)
+    assert ini.rng == 1 and ini.seed == (-3) & 0xFFFFFFFFFFFFFFFF
+    assert list(ini.nc) == [2, 1, 2] and ini.shift_seed_by_rank == 0
+    assert list(ini.random_reseed) == [0, 1] and list(ini.random_seed) == [0, 43]
+    ini = lbgpu.make_init(p, seed=99)
+    assert ini.rng == 0 and ini.seed == 99 and list(ini.nc) == [0, 0, 0]
