@@ -42,8 +42,9 @@ WORKLOAD = "droplet-channel 256x128x128 D3Q19 two-component Shan-Chen, walls z=0
 LATTICE = (256, 128, 128)
 
 
-def workload_params(n=LATTICE, eq="BDist2", tau=1.0):
+def workload_params(n=None, eq="BDist2", tau=1.0):
     from dlbc_gb300 import params
+    n = LATTICE if n is None else n
     lines = [
         "[lattice]", f"gn = [{n[0]}, {n[1]}, {n[2]}]",
         "[lb]", "components = 2", 'fieldNames = ["red", "blue"]', f"tau = [{tau!r}, {tau!r}]",
