@@ -330,19 +330,23 @@ def fp64_rate(device):
         return None
 
 
-def step_kernel(precision, walls, unit_tau=True, nz_even=True, q=19):
+def step_kernel(precision, walls, unit_tau=True, nz_even=True, q=19, planar_walls=True):
     """The kernel that runs the BDist2 step (the library's dispatch rules,
     lbk::pairs_eligible and lbk::pairs2d_eligible): k_collide for FP64; for
     D2Q9 k_pairs2d for FP16 with every tau = 1, no solid site and an even ny
     (nz_even stands for it), k_fused2d otherwise; for D3Q19 k_pairs without
     solid sites and with an even nz for I16 and for FP32/FP16 with every
-    tau = 1; k_fused otherwise."""
+    tau = 1, and for FP16 with every tau = 1 also with planar z-walls (the
+    channel's: solid exactly at z = 0 and nz - 1, nz a multiple of 64, no
+    wall force; planar_walls); k_fused otherwise."""
     from dlbc_gb300 import lbgpu
     if precision == lbgpu.FP64:
         return "k_collide"
     if q == 9:
         return "k_pairs2d" if precision == lbgpu.FP16 and unit_tau and not walls and nz_even else "k_fused2d"
     if not walls and nz_even and (precision == lbgpu.I16 or unit_tau):
+        return "k_pairs"
+    if walls and planar_walls and nz_even and precision == lbgpu.FP16 and unit_tau:
         return "k_pairs"
     return "k_fused"
 
@@ -358,6 +362,8 @@ def roofline(precision, sites, kernel_ms, peak, peak_kind, traffic=None, fp64_pe
     from dlbc_gb300 import lbgpu
     if kernel is None:
         kernel = step_kernel(precision, walls, q=q)
+    if traffic and traffic.get("kernel") not in (None, kernel):
+        traffic = None  # the recorded capture is of another kernel
     out = {"bound": "hbm", "kernel": kernel, "achieved": round(achieved, 1), "peak": peak,
            "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
            "traffic": traffic["bytes"] if traffic else None,
@@ -388,7 +394,7 @@ def read_traffic(key):
         src = f"ncu one-pass capture of {e['kernel']} at commit {e['commit']} ({e['command']})"
         if e.get("scaled"):
             src += "; " + e["scaled"]
-        return {"bytes": e["bytes"], "source": src}
+        return {"bytes": e["bytes"], "source": src, "kernel": e["kernel"].split("<")[0]}
     except Exception:
         return None
 

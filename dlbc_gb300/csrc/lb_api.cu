@@ -571,6 +571,16 @@ __global__ void k_tile_walls(const uint32_t* __restrict__ nbm, uint8_t* __restri
   out[i] = any != 0;
 }
 
+// Sets *bad if a site's solid flag differs from "z = 0 or z = nz - 1" (the
+// channel's planar walls, which the pair kernel handles on its edge lanes).
+__global__ void k_zwall_check(const uint8_t* __restrict__ mask, Geo g, int* __restrict__ bad) {
+  const int64_t s = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (s >= g.n) return;
+  const int z = int(s % g.nz);
+  const bool wall = z == 0 || z == g.nz - 1;
+  if ((mask[s] != 0) != wall) *bad = 1;
+}
+
 int lb_sync_solids(lbgpu_handle* h, int cur, cudaStream_t st) {
   if (!h->mask || !h->fused || h->solids_synced) return LBGPU_OK;
   cudaError_t e = cudaMemcpyAsync(h->f[1 - cur], h->f[cur], h->fbytes, cudaMemcpyDeviceToDevice, st);
@@ -586,6 +596,9 @@ int lb_update_nbmask(lbgpu_handle* h) {
   const bool want = h->mask != nullptr;
   const int tiles_y = (h->ny + 7) / 8, tiles_z = (h->nz + 31) / 32;
   const int64_t nflags = int64_t(h->nx) * tiles_y * tiles_z;
+  // the flags, then (4-byte aligned) the planar-wall check's result
+  const int64_t flag_off = (nflags + 3) / 4 * 4, tw_bytes = flag_off + 4;
+  h->zwall = false;
   if (!want) {
     if (h->nbmask) {
       cudaFree(h->nbmask);
@@ -594,7 +607,7 @@ int lb_update_nbmask(lbgpu_handle* h) {
     }
     if (h->tile_walls) {
       cudaFree(h->tile_walls);
-      h->device_bytes -= nflags;
+      h->device_bytes -= tw_bytes;
       h->tile_walls = nullptr;
     }
     return LBGPU_OK;
@@ -624,19 +637,34 @@ int lb_update_nbmask(lbgpu_handle* h) {
   // (batch members use other tile shapes)
   if (h->Q != 19 || !h->fused || h->lite) return LBGPU_OK;
   if (!h->tile_walls) {
-    e = cudaMalloc(&h->tile_walls, size_t(nflags));
+    e = cudaMalloc(&h->tile_walls, size_t(tw_bytes));
     if (e != cudaSuccess) {
       cudaGetLastError();
       h->tile_walls = nullptr;
       return h->fail(LBGPU_E_NOMEM, "tile wall flags allocation failed");
     }
-    h->device_bytes += nflags;
+    h->device_bytes += tw_bytes;
   }
   k_tile_walls<<<unsigned(ceil_div(nflags, 128)), 128, 0, h->stream>>>(h->nbmask, h->tile_walls, geo_of(h), tiles_y,
                                                                     tiles_z);
   h->launches++;
   e = cudaGetLastError();
   if (e != cudaSuccess) return h->cuda_fail(e, "tile wall flags kernel");
+  // planar z-walls (the pair kernel's walled case)
+  {
+    int* d_bad = reinterpret_cast<int*>(h->tile_walls + flag_off);
+    int bad = 1;
+    e = cudaMemsetAsync(d_bad, 0, sizeof(int), h->stream);
+    if (e == cudaSuccess) {
+      k_zwall_check<<<nb_blocks, 256, 0, h->stream>>>(h->mask, geo_of(h), d_bad);
+      h->launches++;
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return h->cuda_fail(e, "planar wall check");
+    h->zwall = bad == 0 && h->d == 3 && h->nz >= 4;
+  }
   return LBGPU_OK;
 }
 
@@ -911,6 +939,7 @@ int lbgpu_step(lbgpu_handle* h, int32_t nsteps) {
     b.mask = h->mask;
     b.nbmask = h->nbmask;
     b.tile_walls = h->tile_walls;
+    b.zwall = h->zwall ? 1 : 0;
     b.work_counter = h->work_counter;
     b.rho = h->rho;
     b.psi = h->psi;
@@ -1060,6 +1089,7 @@ int step_host_wave(lbgpu_handle* h, const double* const* in, double* const* out,
   b.mask = h->mask;
   b.nbmask = h->nbmask;
   b.tile_walls = h->tile_walls;
+  b.zwall = h->zwall ? 1 : 0;
   b.work_counter = h->work_counter;
   b.rho = h->rho;
   b.psi = h->psi;

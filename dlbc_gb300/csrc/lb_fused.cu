@@ -57,14 +57,27 @@ FusedParams make_fused_params(const StepParams& P, int ty, int q) {
 }
 
 
-bool pairs_eligible(int kind, const StepParams& P, const StepBuffers& b) {
+// solid sites the pair kernel handles: none, or (FP16) exactly the planes
+// z = 0 and z = nz - 1 of a two-component lattice whose z extent is a
+// multiple of the tile width, with no wall force and every tau = 1 (the
+// edge lanes of the first and last z-tile take the bounce-back and the
+// wall's psi).  Measured on the 256x128x128 droplet channel: FP16 12 530 ->
+// 13 660 MLUPS; FP32 and I16 walled lattices stay on the one-site kernel.
+bool pairs_walls_ok(int kind, int c, const StepParams& P, const StepBuffers& b) {
+  if (b.mask == nullptr) return true;
+  return kind == kStoreF16 && b.zwall != 0 && c == 2 && P.nz % kPairTZ == 0 && P.gwc[0] == 0.0 &&
+         P.gwc[1] == 0.0 && P.unit_tau != 0;
+}
+
+bool pairs_eligible(int kind, int c, const StepParams& P, const StepBuffers& b) {
   // aligned two-site words need an even z extent; the pair kernel computes
   // the BDist2 equilibrium and schedules through the work counter
   if (!(P.nz % 2 == 0 && P.eq_form == 2 && b.work_counter != nullptr)) return false;
-  // where it is the faster kernel (measured on GB300): no solid site, and
-  // every tau = 1 or the I16 storage (walls, and for FP32/FP16 the
-  // relaxation's shared-memory populations, favour one site per thread)
-  return b.mask == nullptr && (kind == kStoreI16 || P.unit_tau != 0);
+  // where it is the faster kernel (measured on GB300): no solid site (FP16:
+  // or planar z-walls), and every tau = 1 or the I16 storage (general
+  // walls, and for FP32/FP16 the relaxation's shared-memory populations,
+  // favour one site per thread)
+  return pairs_walls_ok(kind, c, P, b) && (kind == kStoreI16 || P.unit_tau != 0);
 }
 
 // the fused step over planes [x0, x1) of every tile (the host transfers
@@ -88,7 +101,8 @@ cudaError_t launch_fused_range(int kind, int q, int c, const StepBuffers& b, con
     return pairs2d_eligible(kind, c, P, b) ? launch_pairs2d(kind, b, G, st, device)
                                            : launch_fused2d(kind, c, w, c == 2 && P.unit_tau && P.eq_form == 2, b, G,
                                                             st, device);
-  if (pairs_eligible(kind, P, b)) {
+  if (pairs_eligible(kind, c, P, b)) {
+    G.zwall = b.mask != nullptr;
     G.tiles_y = (P.ny + pair_ty(kind) - 1) / pair_ty(kind);
     G.tiles_z = (P.nz + kPairTZ - 1) / kPairTZ;
     G.work = int64_t(G.tiles_y) * G.tiles_z * P.nx;
@@ -124,9 +138,10 @@ cudaError_t launch_fused(int kind, int q, int c, const StepBuffers& b, const Ste
     e = pairs2d_eligible(kind, c, P, b)
             ? launch_pairs2d(kind, b, F, st, device)
             : launch_fused2d(kind, c, w, c == 2 && P.unit_tau && P.eq_form == 2, b, F, st, device);
-  } else if (pairs_eligible(kind, P, b)) {
+  } else if (pairs_eligible(kind, c, P, b)) {
     // two z-adjacent sites per thread (lb_pairs.cuh): pair_ty x 64 tiles
     FusedParams G = F;
+    G.zwall = b.mask != nullptr;
     G.tiles_y = (P.ny + pair_ty(kind) - 1) / pair_ty(kind);
     G.tiles_z = (P.nz + kPairTZ - 1) / kPairTZ;
     G.work = int64_t(G.tiles_y) * G.tiles_z * P.nx;

@@ -84,6 +84,9 @@ struct FusedParams {
   // the single-lattice schedule: planes [x_begin, x_split) of every tile in
   // runs of run_len, then [x_split, x_end) in runs of tail_len
   int32_t x_split, tail_len;
+  // the pair kernel: the solid sites are exactly the planes z = 0 and
+  // z = nz - 1 (nz a multiple of the tile width, no wall force)
+  int32_t zwall;
 };
 
 // The dynamic schedule of the single-lattice kernels (k_fused, k_pairs,

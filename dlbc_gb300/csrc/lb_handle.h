@@ -30,6 +30,7 @@ struct lbgpu_handle {
   uint8_t* mask = nullptr;
   uint32_t* nbmask = nullptr;       // neighbour masks for the fused step (walls only)
   uint8_t* tile_walls = nullptr;    // per (x, 8x32 tile) wall flags for the fused step
+  bool zwall = false;               // the solid sites are exactly the planes z = 0 and z = nz - 1
   int* work_counter = nullptr;      // the fused step's dynamic scheduling counter
   void* rho = nullptr;
   void* psi = nullptr;

@@ -34,6 +34,7 @@ struct StepBuffers {
   const uint8_t* mask;  // nullptr: no walls
   const uint32_t* nbmask = nullptr;  // neighbour masks (fused step; set iff mask is)
   const uint8_t* tile_walls = nullptr;  // per (x, 8x32 tile) wall flags (fused step)
+  int zwall = 0;                        // the solid sites are exactly the planes z = 0 and nz - 1
   int* work_counter = nullptr;          // dynamic scheduling counter (fused step)
   void* rho;            // C*N (double for FP64, float otherwise)
   void* psi;            // C*N
@@ -82,7 +83,7 @@ namespace lbk {
 cudaError_t launch_fused(int kind, int q, int c, const StepBuffers& b, const StepParams& P, cudaStream_t stream,
                          int64_t* launches, const StepEvents* ev, int device);
 // whether launch_fused runs the pair kernel (lb_pairs.cuh) for this lattice
-bool pairs_eligible(int kind, const StepParams& P, const StepBuffers& b);
+bool pairs_eligible(int kind, int c, const StepParams& P, const StepBuffers& b);
 // the fused step over the planes [x0, x1) only (every tile), for the host
 // transfers' wavefront; it reads the populations of planes x0 - 2 .. x1 + 1
 cudaError_t launch_fused_range(int kind, int q, int c, const StepBuffers& b, const StepParams& P, int x0, int x1,

@@ -139,6 +139,12 @@ struct PairIO<float> {
   // gathers again (measured at 512^3: 16 570 -> 16 950 MLUPS; the 16-bit
   // forms were not faster with them)
   __device__ static __forceinline__ void st(float* p, W w) { __stcs(reinterpret_cast<float2*>(p), w); }
+  // planar z-walls: one site of the pair replaced, or stored, alone (the
+  // wall code compiles for every storage; FP16 runs it)
+  __device__ static __forceinline__ W with_lo(W w, W b) { return make_float2(b.x, w.y); }
+  __device__ static __forceinline__ W with_hi(W w, W b) { return make_float2(w.x, b.y); }
+  __device__ static __forceinline__ void st_lo(float* p, W w) { __stcs(p, w.x); }
+  __device__ static __forceinline__ void st_hi(float* p, W w) { __stcs(p + 1, w.y); }
 };
 
 // The 16-bit storages share their word handling: site z in the low half,
@@ -162,6 +168,15 @@ struct PairIO16 {
     return __byte_perm(w, next, 0x5432);  // (w.hi, next.lo)
   }
   __device__ static __forceinline__ void st(T* p, W w) { *reinterpret_cast<unsigned int*>(p) = w; }
+  // planar z-walls: one site of the pair replaced, or stored, alone
+  __device__ static __forceinline__ W with_lo(W w, W b) { return (b & 0xffffu) | (w & 0xffff0000u); }
+  __device__ static __forceinline__ W with_hi(W w, W b) { return (w & 0xffffu) | (b & 0xffff0000u); }
+  __device__ static __forceinline__ void st_lo(T* p, W w) {
+    *reinterpret_cast<unsigned short*>(p) = static_cast<unsigned short>(w & 0xffffu);
+  }
+  __device__ static __forceinline__ void st_hi(T* p, W w) {
+    *reinterpret_cast<unsigned short*>(p + 1) = static_cast<unsigned short>(w >> 16);
+  }
 };
 
 template <>
@@ -298,8 +313,14 @@ __device__ __forceinline__ PairEq pair_eq_constants(float2 rho, float2 cst, floa
 }
 
 // Process plane-tiles [w0, w1) of one lattice (tile-major: w = tile*nx + x).
-// Every thread of the CTA calls this with the same range.
-template <typename T, int C, bool MOM>
+// Every thread of the CTA calls this with the same range.  ZW: the solid
+// sites are exactly the planes z = 0 and z = nz - 1 (P.zwall; nz a multiple
+// of the tile width, no wall force): the lane holding z = 0 and 1 and the
+// one holding nz - 2 and nz - 1 take the bounce-back of the populations
+// pulled from the wall (advectFieldsKernel, advection.d:61-89: the site's
+// own opposite population), the site's own psi for a wall neighbour
+// (addShanChenForcePsi, force.d:273) and store their fluid site alone.
+template <typename T, int C, bool MOM, bool ZW = false>
 __device__ __forceinline__ void pair_body(const FusedParams& P, const T* __restrict__ f, T* __restrict__ fout,
                                           double* __restrict__ force_out, int64_t w0, int64_t w1,
                                           PairShared<C, MOM, T>& sh) {
@@ -342,6 +363,17 @@ __device__ __forceinline__ void pair_body(const FusedParams& P, const T* __restr
     const int zl = z0 + (active ? 2 * lane : 0);
     const bool lane0 = lane == 0;
     const bool lastl = 2 * lane == tzv - 2;
+    const bool wlo = ZW && active && z0 == 0 && lane == 0;
+    const bool whi = ZW && active && lastl && z0 + tzv == P.nz;
+    // a word of new populations: both sites, or the wall lanes' fluid site
+    auto put = [&](T* p, W wv) {
+      if (ZW && wlo)
+        IO::st_hi(p, wv);
+      else if (ZW && whi)
+        IO::st_lo(p, wv);
+      else
+        IO::st(p, wv);
+    };
     const int zleft = z0 > 0 ? z0 - 1 : P.nz - 1;
     const int zright = z0 + tzv < P.nz ? z0 + tzv : 0;
     const int dl = zleft + IO::kLeftEdge - zl, dr = zright - zl;
@@ -385,6 +417,10 @@ __device__ __forceinline__ void pair_body(const FusedParams& P, const T* __restr
           W word = IO::ld(fc[c] + off);
           if (cz == 1) word = IO::up(word, lane0, fc[c] + (off + uint32_t(dl)));
           if (cz == -1) word = IO::down(word, lastl, fc[c] + (off + uint32_t(dr)));
+          if (ZW && cz == 1 && wlo)
+            word = IO::with_hi(word, IO::ld(fc[c] + (p3[1] + r3[1] + P.qn[Conn<19>::bounce(q)])));
+          if (ZW && cz == -1 && whi)
+            word = IO::with_lo(word, IO::ld(fc[c] + (p3[1] + r3[1] + P.qn[Conn<19>::bounce(q)])));
           if (!MOM && keep >= 0 && !ring_warp) sh.pops[keep][c][q][warp][lane] = word;
           v[q] = IO::val(word);
         }
@@ -489,7 +525,9 @@ __device__ __forceinline__ void pair_body(const FusedParams& P, const T* __restr
             };
             auto Lv = [&](int dx, int dy) { return sh.psi[slot[dx + 1]][c][r + dy][zi - 1]; };
             auto Rv = [&](int dx, int dy) { return sh.psi[slot[dx + 1]][c][r + dy][zi + 2]; };
-            // psi_c(x + c_q) at both sites
+            // psi_c(x + c_q) at both sites (planar z-walls: a wall neighbour
+            // contributes the site's own psi)
+            const float2 ownp = ZW ? psi_own(c) : make_float2(0.f, 0.f);
             auto nbv = [&](int q) -> float2 {
               const int cx = Conn<19>::cx(q), cy = Conn<19>::cy(q), cz = Conn<19>::cz(q);
               float2 v;
@@ -498,9 +536,11 @@ __device__ __forceinline__ void pair_body(const FusedParams& P, const T* __restr
               } else if (cz == 1) {
                 const float2 m = M(cx, cy);
                 v = make_float2(m.y, Rv(cx, cy));
+                if (ZW && whi) v.x = ownp.x;
               } else {
                 const float2 m = M(cx, cy);
                 v = make_float2(Lv(cx, cy), m.x);
+                if (ZW && wlo) v.y = ownp.y;
               }
               return v;
             };
@@ -552,8 +592,9 @@ __device__ __forceinline__ void pair_body(const FusedParams& P, const T* __restr
           for (int c = 0; c < C; ++c)
 #pragma unroll
             for (int vd = 0; vd < 3; ++vd) {
-              force_out[(size_t(c) * P.n + own) * 3 + vd] = double(F[c][vd].x);
-              force_out[(size_t(c) * P.n + own + 1) * 3 + vd] = double(F[c][vd].y);
+              // (planar z-walls: no force on the wall sites)
+              force_out[(size_t(c) * P.n + own) * 3 + vd] = (ZW && wlo) ? 0.0 : double(F[c][vd].x);
+              force_out[(size_t(c) * P.n + own + 1) * 3 + vd] = (ZW && whi) ? 0.0 : double(F[c][vd].y);
             }
         }
         // --- BDist2 weighted velocity: sum_c j_c / tau_c / sum_c rho_c
@@ -646,7 +687,7 @@ __device__ __forceinline__ void pair_body(const FusedParams& P, const T* __restr
               else if (q == 14)
                 h14 = r;
               else
-                IO::st(fo[c] + (P.qn[q] + own), IO::enc_int(r));
+                put(fo[c] + (P.qn[q] + own), IO::enc_int(r));
             });
             const int dx = __float2int_rz(m_cur[c].mass.x - mout.x), dy = __float2int_rz(m_cur[c].mass.y - mout.y);
             const int d0x = dx / 12, d0y = dy / 12;
@@ -655,11 +696,11 @@ __device__ __forceinline__ void pair_body(const FusedParams& P, const T* __restr
             h0 = vadd(h0, make_float2(float(d0x), float(d0y)));
             h7 = vadd(h7, make_float2(float(rx - hx), float(ry - hy)));
             h14 = vadd(h14, make_float2(float(hx), float(hy)));
-            IO::st(fo[c] + (P.qn[0] + own), IO::enc(h0));
-            IO::st(fo[c] + (P.qn[7] + own), IO::enc(h7));
-            IO::st(fo[c] + (P.qn[14] + own), IO::enc(h14));
+            put(fo[c] + (P.qn[0] + own), IO::enc(h0));
+            put(fo[c] + (P.qn[7] + own), IO::enc(h7));
+            put(fo[c] + (P.qn[14] + own), IO::enc(h14));
           } else {
-            emit_all([&](int q, float2 v) { IO::st(fo[c] + (P.qn[q] + own), IO::enc(v)); });
+            emit_all([&](int q, float2 v) { put(fo[c] + (P.qn[q] + own), IO::enc(v)); });
           }
         }
       }
@@ -687,8 +728,8 @@ constexpr bool pairs_general() {
 // The single-lattice kernel: persistent CTAs take runs of run_len planes of
 // one tile from the counter, x-chunk-major (neighbouring tiles march over
 // the same planes together and share their ring rows through L2), over the
-// planes [x_begin, x_end) of every tile.
-template <typename T, int C, bool MOM>
+// planes [x_begin, x_end) of every tile.  ZW: planar z-walls (pair_body).
+template <typename T, int C, bool MOM, bool ZW = false>
 __global__ void __launch_bounds__(pair_threads<T>(), pair_minb<T>())
     k_pairs(const T* __restrict__ f, T* __restrict__ fout, double* __restrict__ force_out, FusedParams P) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -705,7 +746,7 @@ __global__ void __launch_bounds__(pair_threads<T>(), pair_minb<T>())
     int tile, x0, x1;
     sched_run(P, ntl, item, tile, x0, x1);
     const int64_t w0 = int64_t(tile) * P.nx + x0;
-    pair_body<T, C, MOM>(P, f, fout, force_out, w0, w0 + (x1 - x0), sh);
+    pair_body<T, C, MOM, ZW>(P, f, fout, force_out, w0, w0 + (x1 - x0), sh);
   }
 }
 
@@ -787,10 +828,10 @@ __global__ void __launch_bounds__(pair_threads<T>(), pair_minb<T>())
 
 // Host side: one persistent launch of k_pairs (F holds the pair tiling, the
 // plane range and the zeroed work counter).
-template <typename T, int C, bool MOM>
+template <typename T, int C, bool MOM, bool ZW = false>
 cudaError_t go_pairs(const StepBuffers& b, const FusedParams& F, cudaStream_t st, int device) {
   static KernelInfo info;
-  auto kern = k_pairs<T, C, MOM>;
+  auto kern = k_pairs<T, C, MOM, ZW>;
   const int smem = int(sizeof(PairShared<C, MOM, T>));
   int per_sm = 0;
   cudaError_t e = kernel_setup(kern, smem, pair_threads<T>(), device, info, &per_sm);
@@ -808,7 +849,13 @@ cudaError_t go_pairs(const StepBuffers& b, const FusedParams& F, cudaStream_t st
 
 template <typename T>
 cudaError_t launch_pairs(int c, bool mom, const StepBuffers& b, const FusedParams& F, cudaStream_t st, int device) {
-  if (b.mask) return cudaErrorInvalidValue;  // solid sites: the one-site kernel
+  if (b.mask) {
+    // planar z-walls in FP16 (two components, every tau = 1, nz a multiple
+    // of the tile width); other solid sites run the one-site kernel
+    if (!F.zwall || c != 2 || !mom || F.nz % kPairTZ != 0) return cudaErrorInvalidValue;
+    if constexpr (std::is_same<T, __half>::value) return go_pairs<T, 2, true, true>(b, F, st, device);
+    return cudaErrorInvalidValue;
+  }
   if constexpr (pairs_general<T>()) {
     if (c == 2) return mom ? go_pairs<T, 2, true>(b, F, st, device) : go_pairs<T, 2, false>(b, F, st, device);
     return mom ? go_pairs<T, 1, true>(b, F, st, device) : go_pairs<T, 1, false>(b, F, st, device);

@@ -69,3 +69,24 @@ def test_recorded_traffic_covers_the_bandwidth_forms():
                ["spinodal512/" + f for f in ("fp32", "fp16", "i16")] + ["d2q9_4096/fp32", "d2q9_4096/fp16"]:
         t = bench.read_traffic(key)
         assert t is not None and t["bytes"] > 0 and "commit" in t["source"], key
+
+
+def test_kernel_labels_follow_the_dispatch():
+    from dlbc_gb300 import lbgpu
+
+    assert bench.step_kernel(lbgpu.FP64, True) == "k_collide"
+    assert bench.step_kernel(lbgpu.FP16, True) == "k_pairs"  # planar z-walls of the channel
+    assert bench.step_kernel(lbgpu.FP16, True, planar_walls=False) == "k_fused"
+    assert bench.step_kernel(lbgpu.FP32, True) == "k_fused" and bench.step_kernel(lbgpu.I16, True) == "k_fused"
+    assert bench.step_kernel(lbgpu.FP16, True, unit_tau=False) == "k_fused"
+    assert bench.step_kernel(lbgpu.FP32, False) == "k_pairs" and bench.step_kernel(lbgpu.I16, False, False) == "k_pairs"
+    assert bench.step_kernel(lbgpu.FP16, False, q=9) == "k_pairs2d"
+    assert bench.step_kernel(lbgpu.FP32, False, q=9) == "k_fused2d"
+
+
+def test_traffic_of_another_kernel_is_not_reported():
+    t = {"bytes": 123, "source": "capture", "kernel": "k_fused"}
+    r = bench.roofline(2, 1000, 0.01, 6650.0, "measured", t, walls=True)
+    assert r["kernel"] == "k_pairs" and r["traffic"] is None and r["traffic_source"] is None
+    r = bench.roofline(1, 1000, 0.01, 6650.0, "measured", t, walls=True)
+    assert r["kernel"] == "k_fused" and r["traffic"] == 123

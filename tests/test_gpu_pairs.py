@@ -1,8 +1,10 @@
 """The pair kernel (two z-adjacent sites per thread, lb_pairs.cuh): the
 fused single-pass step of lattices without solid sites, with an even z
 extent and the BDist2 equilibrium, in the I16 form and, with every tau = 1,
-the FP32 and FP16 forms.  Elsewhere the one-site-per-thread kernel
-(lb_fused.cuh) runs, which the same tests cover (the walled cases).
+the FP32 and FP16 forms; in FP16 also lattices whose solid sites are
+exactly the planes z = 0 and z = nz - 1 (planar walls, nz a multiple of 64,
+no wall force).  Elsewhere the one-site-per-thread kernel (lb_fused.cuh)
+runs, which the same tests cover (the other walled cases).
 
 * Against the two-kernel float step (LBGPU_TWO_KERNEL=1, a different
   kernel with the reference's per-site operation order): populations within
@@ -82,6 +84,10 @@ CASES = {
     "wall-force": lambda: droplet_channel((12, 10, 66), radius=4.0, acc=1e-3, gwc=(0.25, -0.15)),
     "tau": lambda: droplet_channel((12, 11, 40), radius=4.0, acc=1e-3, gwc=(0.1, 0.0), tau=(0.8, 1.3)),
     "one-component": lambda: _one_component(spinodal((10, 12, 64), perturb=0.03)),
+    # planar z-walls (the FP16 pair kernel's walled case): one z-tile holding
+    # both wall lanes, and two z-tiles with one each, partial y tiles
+    "planar-walls": lambda: droplet_channel((14, 18, 64), radius=5.0, acc=1e-3),
+    "planar-walls-2tiles": lambda: droplet_channel((10, 9, 128), radius=4.0, acc=1e-3),
 }
 
 
@@ -101,7 +107,7 @@ def test_pairs_match_two_kernel_step(case, precision):
 
 
 @pytest.mark.parametrize("case", ["two-z-tiles", "partial-tiles", "nz2", "walls", "wall-force", "tau",
-                                  "one-component"])
+                                  "one-component", "planar-walls", "planar-walls-2tiles"])
 def test_i16_close_to_fp32(case):
     """The 16-bit fixed-point form (I16): populations after 20 steps within
     2e-3 of the largest population of the FP32 form's, forces within 3e-4
@@ -149,6 +155,23 @@ def test_pairs_walled_channel_translation_invariant_bitwise(precision, shift):
     wall force reading the solid sites' densities, and still every site
     computes the same bits wherever it sits."""
     p = droplet_channel((12, 20, 70), radius=4.0, acc=1e-3, gwc=(0.2, -0.1))
+    fl, m = init.init_fields(p)
+    a, fa = _run(p, 15, precision, fields=(fl, m), rho0=(0.5, 0.5))
+    fs, ms = _shifted(fl, m, shift)
+    b, fb = _run(p, 15, precision, fields=(fs, ms), rho0=(0.5, 0.5))
+    for c in range(2):
+        assert np.array_equal(np.roll(a[c], shift, axis=(0, 1, 2)), b[c]), c
+        assert np.array_equal(np.roll(fa[c], shift, axis=(0, 1, 2)), fb[c], equal_nan=True), c
+
+
+@pytest.mark.parametrize("precision", [lbgpu.FP32, lbgpu.FP16, lbgpu.I16])
+@pytest.mark.parametrize("shift", [(3, 5, 0), (1, 8, 0)])
+def test_pairs_planar_walls_translation_invariant_bitwise(precision, shift):
+    """Planar z-walls (walls exactly at z = 0 and z = nz - 1, no wall force,
+    tau = 1: FP16 on the pair kernel's wall lanes, FP32 and I16 on the
+    one-site kernel), shifted along x and y: the wall lanes' bounce-back,
+    psi and stores give every site the same bits wherever it sits."""
+    p = droplet_channel((12, 20, 128), radius=4.0, acc=1e-3)
     fl, m = init.init_fields(p)
     a, fa = _run(p, 15, precision, fields=(fl, m), rho0=(0.5, 0.5))
     fs, ms = _shifted(fl, m, shift)
