@@ -19,7 +19,7 @@ module dlbc.gpu.lbgpu;
 
 extern(C) nothrow @nogc:
 
-enum int LBGPU_ABI_VERSION = 1;
+enum int LBGPU_ABI_VERSION = 2;
 enum int LBGPU_MAX_COMPONENTS = 2;
 
 enum int LBGPU_OK = 0;

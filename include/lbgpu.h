@@ -34,7 +34,7 @@
 extern "C" {
 #endif
 
-#define LBGPU_ABI_VERSION 1
+#define LBGPU_ABI_VERSION 2  /* 2: lbgpu_init gained rng, random_reseed, nc, shift_seed_by_rank, random_seed */
 #define LBGPU_MAX_COMPONENTS 2
 
 /* status codes */

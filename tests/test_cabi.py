@@ -33,7 +33,7 @@ def test_library_exports_all_declared_symbols(libpath):
 
 def test_abi_version_without_gpu(libpath):
     lib = ctypes.CDLL(libpath)
-    assert lib.lbgpu_abi_version() == 1
+    assert lib.lbgpu_abi_version() == 2
 
 
 def test_create_rejects_bad_configs_without_touching_the_gpu(libpath):
@@ -93,7 +93,7 @@ def test_header_compiles_links_and_runs_from_c_and_cpp(libpath, tmp_path, lang):
     subprocess.run([cc, std, "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe),
                     "-L", libdir, "-llbgpu", f"-Wl,-rpath,{libdir}"], check=True, capture_output=True)
     out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()
-    assert out == ["1", "-1", "1", "msg"], out
+    assert out == ["2", "-1", "1", "msg"], out
 
 
 def test_noalloc_rejects_lattices_beyond_the_scratch(libpath):
