@@ -95,3 +95,29 @@ def test_make_init_describes_the_reference_draws():
     assert list(ini.random_reseed) == [0, 1] and list(ini.random_seed) == [0, 43]
     ini = lbgpu.make_init(p, seed=99)
     assert ini.rng == 0 and ini.seed == 99 and list(ini.nc) == [0, 0, 0]
+
+
+def test_reference_draws_random_shapes(harness, tmp_path):
+    """Twenty seeded random shapes, grids, seeds and reseed choices (3D,
+    2D and 1D), both components."""
+    rng = np.random.default_rng(11)
+    for i in range(20):
+        d = int(rng.integers(1, 4))
+        nc = [int(rng.integers(1, 4)) if k < d else 1 for k in range(3)]
+        n = [nc[k] * int(rng.integers(1, 5)) if k < d else 1 for k in range(3)]
+        halo = [2 if k < d else 0 for k in range(3)]
+        per_site = (int(rng.choice([0, 1, 3])), int(rng.choice([1, 5])))
+        reseed = (bool(rng.integers(0, 2)), bool(rng.integers(0, 2)))
+        rseed = (int(rng.integers(-5, 100)), int(rng.integers(-5, 100)))
+        seed, shift = int(rng.integers(-1000, 1000)), bool(rng.integers(0, 2))
+        case = (tuple(n), tuple(halo), tuple(nc), seed, shift, per_site, reseed, rseed)
+        for comp in range(2):
+            if per_site[comp] == 0:
+                continue
+            path = str(tmp_path / f"r{i}_{comp}.bin")
+            args = [harness, path, *map(str, n), *map(str, halo), *map(str, nc), str(seed), str(int(shift)),
+                    *map(str, per_site), *(str(int(r)) for r in reseed), *map(str, rseed), str(comp)]
+            subprocess.run(args, check=True, timeout=60)
+            got = np.fromfile(path, np.uint32)
+            want = expected(n, halo, nc, seed, shift, per_site, reseed, rseed, comp)
+            assert np.array_equal(got, want), (case, comp)
